@@ -1,0 +1,446 @@
+"""Traversal benchmark: Mrays/s of the MTBVH closest-hit and any-hit kernels.
+
+Workload (one step): for each triangle-soup scene of N = 1M, 4M, 16M
+triangles (centroids uniform in the unit cube, equilateral triangles with
+edge U(0.001, 0.01), random orientation; seeds 101/104/116), trace 2^24
+coherent primary rays (pinhole at (0.5, -1, 0.5) looking along +y, 45 degree
+fov, 4096x4096) and 2^24 incoherent rays (cosine-distributed from the primary
+hit points), each as a closest-hit query and as an any-hit query with
+tmax ~ U(0, 1): 12 launches and 12 * 2^24 rays per step.  Inputs are seeded
+synthetic data (the reference publishes no benchmark scenes).
+
+``value`` is device-resident throughput (rays / summed CUDA-event time of the
+steps); ``e2e`` is the same metric through the C ABI with pinned host arrays
+(host->device copy of rays, kernel, device->host copy of results per call).
+
+``--impl reference`` times the reference algorithm on the host cores: the
+reference's traversal is GLSL that needs OpenGL (unavailable on this machine), so
+its CPU stand-in is the oracle restatement, run with every host thread on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SIZES = {"1M": 1 << 20, "4M": 1 << 22, "16M": 1 << 24}
+SEEDS = {1 << 20: 101, 1 << 22: 104, 1 << 24: 116}
+METRIC = "Mrays/s traversal"
+UNIT = "Mrays/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sizes", default="1M,4M,16M")
+    ap.add_argument("--side", type=int, default=4096, help="primary rays = side^2")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 8:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# --------------------------------------------------------------------------
+# workload construction
+# --------------------------------------------------------------------------
+def build_scene(N: int):
+    from zillumgl_gb300.synthetic import triangle_soup
+
+    return triangle_soup(N, SEEDS.get(N, 7))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "trace_closest_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+def run_ours(args):
+    import torch
+
+    from zillumgl_gb300 import BVH
+    from zillumgl_gb300.synthetic import incoherent_rays, primary_rays, shadow_tmax
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sizes = [SIZES[s] for s in args.sizes.split(",")]
+    side = args.side
+    nray = side * side
+
+    o_p, d_p = primary_rays(side, side)
+    specs = []  # (name, acc, o, d, tmax, query)
+    scenes = []
+    t_setup = time.time()
+    for N in sizes:
+        v, idx = build_scene(N)
+        t0 = time.time()
+        acc = BVH(v, idx).build()
+        log(f"[bench] N={N}: build+upload {time.time() - t0:.1f}s, {acc.node_count} nodes")
+        to = torch.from_numpy(o_p).to(dev)
+        td = torch.from_numpy(d_p).to(dev)
+        hid, ht = acc.trace_closest(to, td, stream=stream)
+        stream.synchronize()
+        o_i, d_i = incoherent_rays(v, idx, o_p, d_p, hid.cpu().numpy(), ht.cpu().numpy(), seed=SEEDS.get(N, 7) + 1)
+        tm_p = torch.from_numpy(shadow_tmax(nray, SEEDS.get(N, 7) + 2)).to(dev)
+        tm_i = torch.from_numpy(shadow_tmax(nray, SEEDS.get(N, 7) + 3)).to(dev)
+        fam = {"primary": (to, td, tm_p, o_p, d_p), "incoherent": (torch.from_numpy(o_i).to(dev),
+                                                                   torch.from_numpy(d_i).to(dev), tm_i, o_i, d_i)}
+        for fname, (o, d, tm, oh, dh) in fam.items():
+            for q in ("closest", "any"):
+                specs.append({"name": f"{N >> 20}M/{fname}/{q}", "N": N, "acc": acc, "o": o, "d": d, "tmax": tm,
+                              "o_host": oh, "d_host": dh, "query": q})
+        scenes.append((N, v, idx, acc))
+        del v, idx
+    log(f"[bench] setup {time.time() - t_setup:.1f}s, {len(specs)} launches/step")
+
+    # outputs (device)
+    out_id = torch.empty(nray, dtype=torch.int32, device=dev)
+    out_t = torch.empty(nray, dtype=torch.float32, device=dev)
+    out_occ = torch.empty(nray, dtype=torch.uint8, device=dev)
+
+    # algorithmic bytes: 32 B per table entry visited, 36 B per triangle test,
+    # 24 B ray in, 8 B hit out (closest) / 4 B tmax in + 1 B flag out (any)
+    for sp in specs:
+        vis, tst = sp["acc"].trace_count(sp["o"], sp["d"], sp["tmax"], any_hit=sp["query"] == "any", stream=stream)
+        stream.synchronize()
+        V = int(vis.sum(dtype=torch.int64).item())
+        T = int(tst.sum(dtype=torch.int64).item())
+        io = (24 + 8) if sp["query"] == "closest" else (24 + 4 + 1)
+        sp["V"], sp["T"] = V, T
+        sp["bytes"] = 32 * V + 36 * T + io * nray
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def launch(sp):
+        if sp["query"] == "closest":
+            sp["acc"].trace_closest(sp["o"], sp["d"], out_id, out_t, stream=stream)
+        else:
+            sp["acc"].trace_any(sp["o"], sp["d"], sp["tmax"], out_occ, stream=stream)
+
+    def one_step(record):
+        evs = []
+        for sp in specs:
+            if record:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                launch(sp)
+                e1.record(stream)
+                evs.append((sp, e0, e1))
+            else:
+                launch(sp)
+        return evs
+
+    for _ in range(args.warmup):
+        one_step(False)
+    stream.synchronize()
+
+    per_launch = {sp["name"]: [] for sp in specs}
+    step_ms = []
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # L2 flush (256 MiB write) outside the timed events
+            evs = one_step(True)
+            stream.synchronize()
+            tot = 0.0
+            for sp, e0, e1 in evs:
+                ms = e0.elapsed_time(e1)
+                per_launch[sp["name"]].append(ms)
+                tot += ms
+            step_ms.append(tot)
+    torch.cuda.synchronize(dev)
+    total_ms = sum(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        total_ms = float(t.item())
+    rays_per_step = len(specs) * nray
+    value = rays_per_step * args.steps * world / (total_ms * 1e-3) / 1e6
+
+    # roofline of the dominant kernel (closest-hit trace)
+    closest = [sp for sp in specs if sp["query"] == "closest"]
+    anyq = [sp for sp in specs if sp["query"] == "any"]
+    t_closest = sum(statistics.mean(per_launch[sp["name"]]) for sp in closest)
+    t_any = sum(statistics.mean(per_launch[sp["name"]]) for sp in anyq)
+    dom = closest if t_closest >= t_any else anyq
+    dom_ms = sum(statistics.mean(per_launch[sp["name"]]) for sp in dom) / len(dom)
+    dom_bytes = sum(sp["bytes"] for sp in dom) / len(dom)
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic()
+    roofline = {"bound": "hbm", "kernel": "trace_closest_kernel" if dom is closest else "trace_any_kernel",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": f"{peak_kind} hbm_gbs (copy bandwidth)",
+                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                "traffic_note": traffic.get("note") if traffic else "no ncu capture committed yet",
+                "algorithmic_bytes_per_launch": int(dom_bytes),
+                "avg_launch_ms": round(dom_ms, 4)}
+
+    workloads = []
+    for sp in specs:
+        ms = statistics.mean(per_launch[sp["name"]])
+        workloads.append({"name": sp["name"], "ms": round(ms, 4), "mrays_s": round(nray / (ms * 1e-3) / 1e6, 1),
+                          "visits_per_ray": round(sp["V"] / nray, 2), "tests_per_ray": round(sp["T"] / nray, 3),
+                          "gbs": round(sp["bytes"] / (ms * 1e-3) / 1e9, 1)})
+
+    # end to end through the C ABI with pinned host arrays
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        for sp in specs:
+            key = (sp["N"], sp["name"].split("/")[1])
+            if key not in host:
+                host[key] = (torch.from_numpy(sp["o_host"]).pin_memory(), torch.from_numpy(sp["d_host"]).pin_memory(),
+                             sp["tmax"].cpu().pin_memory())
+            sp["host"] = host[key]
+        h_id = torch.empty(nray, dtype=torch.int32).pin_memory()
+        h_t = torch.empty(nray, dtype=torch.float32).pin_memory()
+        h_occ = torch.empty(nray, dtype=torch.uint8).pin_memory()
+        h2d = d2h = 0
+        for sp in specs:
+            h2d += 24 * nray + (4 * nray if sp["query"] == "any" else 0)
+            d2h += (8 if sp["query"] == "closest" else 1) * nray
+
+        def e2e_step():
+            for sp in specs:
+                o, d, tm = sp["host"]
+                if sp["query"] == "closest":
+                    sp["acc"].trace_closest(o, d, h_id, h_t, stream=stream)
+                else:
+                    sp["acc"].trace_any(o, d, tm, h_occ, stream=stream)
+
+        e2e_step()
+        stream.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        stream.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(rays_per_step * args.steps * world / e2e_s / 1e6, 1), "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "note": "C-ABI calls on pinned host arrays; each call stages H2D, traces, copies results back and "
+                       "synchronises"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scenes, specs, args.cpu_seconds)
+
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "MTBVH traversal microbench (triangle soups, 2^24 coherent primary + 2^24 "
+                                   "incoherent rays, closest-hit and any-hit)",
+                       "triangles": sizes, "rays_per_launch": nray, "launches_per_step": len(specs),
+                       "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write); inputs > L2"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": len(specs) * args.steps,
+            "clocks": clk.summary(), "workloads": workloads}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for N, v, idx, acc in scenes:
+        acc.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def cpu_baseline(scenes, specs, target_s: float):
+    """The oracle traversal on every host thread over a bounded ray sample."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    packed = {}
+    for N, v, idx, acc in scenes:
+        p = acc.export()
+        packed[N] = (p.bounds, p.hitTable, v, idx)
+
+    def run(sample):
+        rays = 0
+        t0 = time.perf_counter()
+        for sp in specs:
+            b, h, v, idx = packed[sp["N"]]
+            o = sp["o_host"][:sample]
+            d = sp["d_host"][:sample]
+            if sp["query"] == "closest":
+                oracle.trace(b, h, v, idx, o, d, nthreads=nthreads)
+            else:
+                tm = sp["tmax"][:sample].cpu().numpy()
+                oracle.trace(b, h, v, idx, o, d, tmax=tm, any_hit=True, nthreads=nthreads)
+            rays += o.shape[0]
+        return rays, time.perf_counter() - t0
+
+    probe = 2048
+    r, s = run(probe)
+    sample = int(min(specs[0]["o_host"].shape[0], max(probe, probe * target_s / max(s, 1e-3))))
+    r, s = run(sample)
+    return {"value": round(r / s / 1e6, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"first {sample} rays of each of the {len(specs)} launches ({r} rays, {s:.1f}s) on the "
+                      f"oracle restatement with {nthreads} threads"}
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle restatement (the reference's own traversal is
+    GLSL behind OpenGL, unavailable on this machine) on a bounded sample of the workload."""
+    import oracle
+    from zillumgl_gb300.synthetic import incoherent_rays, primary_rays, shadow_tmax
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    sizes = [SIZES[s] for s in args.sizes.split(",")]
+    side = args.side
+    o_p, d_p = primary_rays(side, side)
+    sample = 4096
+    rng = np.random.default_rng(0)
+    sel = np.sort(rng.choice(o_p.shape[0], sample, replace=False))
+    work = []
+    for N in sizes:
+        v, idx = build_scene(N)
+        b, h, _ = oracle.bvh_build(v, idx)
+        o, d = o_p[sel], d_p[sel]
+        hid, ht, _, _ = oracle.trace(b, h, v, idx, o, d, nthreads=nthreads)
+        o_i, d_i = incoherent_rays(v, idx, o, d, hid, ht, seed=SEEDS.get(N, 7) + 1)
+        tm = shadow_tmax(sample, SEEDS.get(N, 7) + 2)
+        work.append((b, h, v, idx, o, d, o_i, d_i, tm))
+
+    def step():
+        rays = 0
+        for b, h, v, idx, o, d, o_i, d_i, tm in work:
+            for oo, dd in ((o, d), (o_i, d_i)):
+                oracle.trace(b, h, v, idx, oo, dd, nthreads=nthreads)
+                oracle.trace(b, h, v, idx, oo, dd, tmax=tm, any_hit=True, nthreads=nthreads)
+                rays += 2 * oo.shape[0]
+        return rays
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    rays = sum(step() for _ in range(args.steps))
+    dt = time.perf_counter() - t0
+    value = rays / dt / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "MTBVH traversal microbench (triangle soups, 2^24 coherent primary + 2^24 "
+                                   "incoherent rays, closest-hit and any-hit)",
+                       "triangles": sizes, "rays_per_launch": side * side, "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{sample} sampled primary rays + their incoherent rays per scene, closest "
+                                       f"and any-hit, oracle restatement (the reference traversal is GLSL/OpenGL, "
+                                       f"unavailable on this box)"},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,53 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares (no GPU work)."""
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols() -> list[str]:
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:zgl_status|int32_t|const char\*|void)\s+(zgl_\w+)\s*\(", text, flags=re.M)
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "zgl_trace_closest" in names and "zgl_accel_build" in names
+    assert len(names) == len(set(names))
+
+
+def test_library_exports_every_declared_symbol(zgl_lib):
+    missing = [n for n in declared_symbols() if not hasattr(zgl_lib, n)]
+    assert not missing, f"libzgl.so lacks {missing}"
+
+
+def test_python_binding_covers_header(zgl_lib):
+    from zillumgl_gb300._lib import SIGNATURES
+
+    assert set(declared_symbols()) == set(SIGNATURES)
+
+
+def test_version_and_error_string(zgl_lib):
+    assert zgl_lib.zgl_version() >= 100
+    assert isinstance(zgl_lib.zgl_last_error(), bytes)
+
+
+def test_invalid_arguments_return_status_not_abort(zgl_lib):
+    from zillumgl_gb300 import BVH, ZglError
+
+    v = np.zeros((3, 3), np.float32)
+    with pytest.raises(ZglError) as e:
+        BVH(v, np.array([0, 1, 7], np.uint32)).build_host()
+    assert e.value.status == 1 and "out of range" in str(e.value)
+    bad = v.copy()
+    bad[1, 1] = np.nan
+    with pytest.raises(ZglError):
+        BVH(bad, np.array([0, 1, 2], np.uint32)).build_host()

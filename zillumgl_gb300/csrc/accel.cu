@@ -1,0 +1,385 @@
+// accel.cu — MTBVH upload and the closest-hit / any-hit trace kernels, plus
+// the zgl_accel_* and zgl_trace_* entry points.
+#include <algorithm>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "accel.h"
+#include "traverse.cuh"
+#include "zgl_internal.h"
+
+namespace zgl {
+namespace {
+
+constexpr int kTraceBlock = 128;
+
+__global__ void pack_nodes_kernel(const float* __restrict__ bounds, const int32_t* __restrict__ hit,
+                                  int64_t M, float4* __restrict__ nodes) {
+    int64_t total = 6 * M;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int32_t node = hit[3 * e + 0];
+        int32_t prim = hit[3 * e + 1];
+        int32_t miss = hit[3 * e + 2];
+        const float* b = bounds + 6 * (int64_t)node;
+        nodes[2 * e + 0] = make_float4(b[0], b[1], b[2], __int_as_float(prim));
+        nodes[2 * e + 1] = make_float4(b[3], b[4], b[5], __int_as_float(miss));
+    }
+}
+
+__device__ __forceinline__ float3 load3(const float* p, int64_t i) {
+    return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+trace_closest_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                     int64_t n, int32_t* __restrict__ hit_id, float* __restrict__ hit_t) {
+    int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    if (i >= n) return;
+    TraceRay r = make_trace_ray(load3(org, i), load3(dir, i));
+    float dist = 1e8f;
+    int v = 0, t = 0;
+    int id = traverse<false, false>(a, r, dist, v, t);
+    hit_id[i] = id;
+    hit_t[i] = dist;
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+trace_any_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                 const float* __restrict__ tmax, int64_t n, uint8_t* __restrict__ occ) {
+    int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    if (i >= n) return;
+    TraceRay r = make_trace_ray(load3(org, i), load3(dir, i));
+    float dist = tmax[i];
+    int v = 0, t = 0;
+    occ[i] = (uint8_t)traverse<true, false>(a, r, dist, v, t);
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                   const float* __restrict__ tmax, int64_t n, int any_hit,
+                   int32_t* __restrict__ visits, int32_t* __restrict__ tests) {
+    int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    if (i >= n) return;
+    TraceRay r = make_trace_ray(load3(org, i), load3(dir, i));
+    int v = 0, t = 0;
+    if (any_hit) {
+        float dist = tmax[i];
+        traverse<true, true>(a, r, dist, v, t);
+    } else {
+        float dist = 1e8f;
+        traverse<false, true>(a, r, dist, v, t);
+    }
+    visits[i] = v;
+    tests[i] = t;
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
+                              cudaStream_t s) {
+    if (M == 0) return cudaSuccess;
+    int64_t total = 6 * M;
+    unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64);
+    pack_nodes_kernel<<<grid, 256, 0, s>>>(bounds, hit, M, nodes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
+                                 int32_t* hit_id, float* hit_t, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
+                             int64_t n, uint8_t* occ, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir, const float* tmax,
+                               int64_t n, int any_hit, int32_t* visits, int32_t* tests,
+                               cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    trace_count_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, any_hit,
+                                                                       visits, tests);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Pointer staging: trace calls accept host or device arrays.
+// ---------------------------------------------------------------------------
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+// Moves the arguments of one trace call to device memory when they are host
+// arrays and copies outputs back.  Device arrays pass through untouched.
+class Staging {
+public:
+    Staging(const zgl_accel* a, cudaStream_t s) : a_(a), s_(s) {}
+
+    // Registers an argument and returns its slot.
+    int add(const void* p, size_t bytes, bool in, bool out) {
+        Slot sl;
+        sl.user = const_cast<void*>(p);
+        sl.bytes = bytes;
+        sl.in = in;
+        sl.out = out;
+        sl.staged = p != nullptr && bytes > 0 && !is_device_ptr(p);
+        if (sl.staged) {
+            sl.off = offset_;
+            offset_ += (bytes + 255) & ~size_t(255);
+        }
+        slots_.push_back(sl);
+        return (int)slots_.size() - 1;
+    }
+
+    // Allocates (or reuses) the staging area and copies inputs in.
+    void commit() {
+        if (offset_ == 0) return;
+        if (a_->stage_bytes < offset_) {
+            if (a_->d_stage) ZGL_CUDA(cudaFree(a_->d_stage));
+            a_->d_stage = nullptr;
+            a_->stage_bytes = 0;
+            ZGL_CUDA(cudaMalloc(&a_->d_stage, offset_));
+            a_->stage_bytes = offset_;
+        }
+        for (auto& sl : slots_)
+            if (sl.staged && sl.in)
+                ZGL_CUDA(cudaMemcpyAsync(dev(sl), sl.user, sl.bytes, cudaMemcpyHostToDevice, s_));
+    }
+
+    void* ptr(int slot) const {
+        const Slot& sl = slots_[(size_t)slot];
+        return sl.staged ? dev(sl) : sl.user;
+    }
+
+    // Copies staged outputs back and waits for them.
+    void finish() {
+        if (offset_ == 0) return;
+        for (auto& sl : slots_)
+            if (sl.staged && sl.out)
+                ZGL_CUDA(cudaMemcpyAsync(sl.user, dev(sl), sl.bytes, cudaMemcpyDeviceToHost, s_));
+        ZGL_CUDA(cudaStreamSynchronize(s_));
+    }
+
+private:
+    struct Slot {
+        void* user = nullptr;
+        size_t bytes = 0;
+        bool in = false, out = false, staged = false;
+        size_t off = 0;
+    };
+    void* dev(const Slot& sl) const { return static_cast<char*>(a_->d_stage) + sl.off; }
+    const zgl_accel* a_;
+    cudaStream_t s_;
+    std::vector<Slot> slots_;
+    size_t offset_ = 0;
+};
+
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int dev) {
+        ZGL_CUDA(cudaGetDevice(&prev_));
+        if (prev_ != dev) ZGL_CUDA(cudaSetDevice(dev));
+        dev_ = dev;
+    }
+    ~DeviceGuard() {
+        if (prev_ != dev_) cudaSetDevice(prev_);
+    }
+
+private:
+    int prev_ = 0, dev_ = 0;
+};
+
+int host_threads() {
+    unsigned n = std::thread::hardware_concurrency();
+    return n == 0 ? 1 : (int)n;
+}
+
+}  // namespace zgl
+
+using namespace zgl;
+
+extern "C" {
+
+static void validate_mesh(const char* fn, const float* vertices, size_t n_vertices, const uint32_t* indices,
+                          size_t n_triangles) {
+    if (n_triangles > 0 && (!vertices || !indices))
+        fail(ZGL_ERR_INVALID_ARG, "%s: NULL vertex or index array", fn);
+    if (n_triangles > (size_t)0x3fffffff)
+        fail(ZGL_ERR_INVALID_ARG, "%s: %zu triangles exceed the 2^30 limit", fn, n_triangles);
+    for (size_t i = 0; i < 3 * n_triangles; i++)
+        if (indices[i] >= n_vertices)
+            fail(ZGL_ERR_INVALID_ARG, "%s: index %zu = %u out of range (%zu vertices)", fn, i, indices[i],
+                 n_vertices);
+    for (size_t i = 0; i < 3 * n_vertices; i++)
+        if (!(vertices[i] == vertices[i])) fail(ZGL_ERR_INVALID_ARG, "%s: vertex component %zu is NaN", fn, i);
+}
+
+zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices, const uint32_t* indices,
+                              size_t n_triangles, float* bounds, int32_t* hit_table) {
+    ZGL_API_BEGIN
+    validate_mesh("zgl_bvh_build_host", vertices, n_vertices, indices, n_triangles);
+    if (n_triangles > 0 && (!bounds || !hit_table))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_bvh_build_host: NULL output array");
+    HostBVH h;
+    build_bvh(vertices, indices, (int64_t)n_triangles, h, host_threads());
+    if (h.M > 0) {
+        std::memcpy(bounds, h.bounds.data(), sizeof(float) * h.M * 6);
+        std::memcpy(hit_table, h.hitTable.data(), sizeof(int32_t) * h.M * 18);
+    }
+    ZGL_API_END
+}
+
+zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint32_t* indices,
+                           size_t n_triangles, zgl_accel** out) {
+    ZGL_API_BEGIN
+    if (!out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build: out is NULL");
+    *out = nullptr;
+    validate_mesh("zgl_accel_build", vertices, n_vertices, indices, n_triangles);
+
+    auto* a = new zgl_accel();
+    try {
+        ZGL_CUDA(cudaGetDevice(&a->device));
+        a->ntri = (int64_t)n_triangles;
+        build_bvh(vertices, indices, a->ntri, a->host, host_threads());
+        a->M = a->host.M;
+        if (a->M > 0) {
+            size_t nb = sizeof(float) * a->M * 6, nh = sizeof(int32_t) * a->M * 18;
+            float* d_bounds = nullptr;
+            int32_t* d_hit = nullptr;
+            ZGL_CUDA(cudaMalloc(&a->d_nodes, sizeof(float4) * 12 * a->M));
+            ZGL_CUDA(cudaMalloc(&a->d_tris, sizeof(float4) * 3 * a->ntri));
+            ZGL_CUDA(cudaMalloc(&d_bounds, nb));
+            ZGL_CUDA(cudaMalloc(&d_hit, nh));
+            ZGL_CUDA(cudaMemcpy(d_bounds, a->host.bounds.data(), nb, cudaMemcpyHostToDevice));
+            ZGL_CUDA(cudaMemcpy(d_hit, a->host.hitTable.data(), nh, cudaMemcpyHostToDevice));
+            ZGL_CUDA(launch_pack_nodes(d_bounds, d_hit, a->M, a->d_nodes, 0));
+            // triangles: a, ab = b - a, ac = c - a (float32, as intersection.glsl:68-69)
+            std::vector<float4> tris((size_t)a->ntri * 3);
+            for (int64_t t = 0; t < a->ntri; t++) {
+                const float* A = vertices + 3 * (size_t)indices[3 * t];
+                const float* B = vertices + 3 * (size_t)indices[3 * t + 1];
+                const float* C = vertices + 3 * (size_t)indices[3 * t + 2];
+                float abx = B[0] - A[0], aby = B[1] - A[1], abz = B[2] - A[2];
+                float acx = C[0] - A[0], acy = C[1] - A[1], acz = C[2] - A[2];
+                tris[3 * t + 0] = make_float4(A[0], A[1], A[2], abx);
+                tris[3 * t + 1] = make_float4(aby, abz, acx, acy);
+                tris[3 * t + 2] = make_float4(acz, 0.0f, 0.0f, 0.0f);
+            }
+            ZGL_CUDA(cudaMemcpy(a->d_tris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice));
+            ZGL_CUDA(cudaDeviceSynchronize());
+            ZGL_CUDA(cudaFree(d_bounds));
+            ZGL_CUDA(cudaFree(d_hit));
+        }
+    } catch (...) {
+        if (a->d_nodes) cudaFree(a->d_nodes);
+        if (a->d_tris) cudaFree(a->d_tris);
+        delete a;
+        throw;
+    }
+    *out = a;
+    ZGL_API_END
+}
+
+zgl_status zgl_accel_node_count(const zgl_accel* accel, size_t* out) {
+    ZGL_API_BEGIN
+    if (!accel || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_node_count: NULL argument");
+    *out = (size_t)accel->M;
+    ZGL_API_END
+}
+
+zgl_status zgl_accel_export(const zgl_accel* accel, float* bounds, int32_t* hit_table) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_export: NULL accel");
+    if (accel->M > 0 && (!bounds || !hit_table))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_export: NULL output array");
+    if (accel->M > 0) {
+        std::memcpy(bounds, accel->host.bounds.data(), sizeof(float) * accel->M * 6);
+        std::memcpy(hit_table, accel->host.hitTable.data(), sizeof(int32_t) * accel->M * 18);
+    }
+    ZGL_API_END
+}
+
+zgl_status zgl_accel_destroy(zgl_accel* accel) {
+    ZGL_API_BEGIN
+    if (!accel) return ZGL_OK;
+    if (accel->d_nodes) cudaFree(accel->d_nodes);
+    if (accel->d_tris) cudaFree(accel->d_tris);
+    if (accel->d_stage) cudaFree(accel->d_stage);
+    delete accel;
+    ZGL_API_END
+}
+
+zgl_status zgl_trace_closest(const zgl_accel* accel, const float* origins, const float* dirs, size_t n,
+                             int32_t* hit_id, float* hit_t, void* stream) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest: NULL accel");
+    if (n == 0) return ZGL_OK;
+    if (!origins || !dirs || !hit_id || !hit_t) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest: NULL array");
+    DeviceGuard dg(accel->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    Staging st(accel, s);
+    int so = st.add(origins, 12 * n, true, false), sd = st.add(dirs, 12 * n, true, false);
+    int si = st.add(hit_id, 4 * n, false, true), sx = st.add(hit_t, 4 * n, false, true);
+    st.commit();
+    ZGL_CUDA(launch_trace_closest(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
+                                  (int64_t)n, (int32_t*)st.ptr(si), (float*)st.ptr(sx), s));
+    st.finish();
+    ZGL_API_END
+}
+
+zgl_status zgl_trace_any(const zgl_accel* accel, const float* origins, const float* dirs, const float* tmax,
+                         size_t n, uint8_t* occluded, void* stream) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_any: NULL accel");
+    if (n == 0) return ZGL_OK;
+    if (!origins || !dirs || !tmax || !occluded) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_any: NULL array");
+    DeviceGuard dg(accel->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    Staging st(accel, s);
+    int so = st.add(origins, 12 * n, true, false), sd = st.add(dirs, 12 * n, true, false);
+    int sm = st.add(tmax, 4 * n, true, false), sc = st.add(occluded, n, false, true);
+    st.commit();
+    ZGL_CUDA(launch_trace_any(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
+                              (const float*)st.ptr(sm), (int64_t)n, (uint8_t*)st.ptr(sc), s));
+    st.finish();
+    ZGL_API_END
+}
+
+zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const float* dirs, const float* tmax,
+                           size_t n, int32_t any_hit, int32_t* visits, int32_t* tests, void* stream) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_count: NULL accel");
+    if (n == 0) return ZGL_OK;
+    if (!origins || !dirs || !visits || !tests || (any_hit && !tmax))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_trace_count: NULL array");
+    DeviceGuard dg(accel->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    Staging st(accel, s);
+    int so = st.add(origins, 12 * n, true, false), sd = st.add(dirs, 12 * n, true, false);
+    int sm = st.add(any_hit ? tmax : nullptr, 4 * n, true, false);
+    int sv = st.add(visits, 4 * n, false, true), sx = st.add(tests, 4 * n, false, true);
+    st.commit();
+    ZGL_CUDA(launch_trace_count(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
+                                (const float*)st.ptr(sm), (int64_t)n, any_hit, (int32_t*)st.ptr(sv),
+                                (int32_t*)st.ptr(sx), s));
+    st.finish();
+    ZGL_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+// accel.h — device-resident MTBVH.
+//
+// HBM layout (GB300-first; the reference keeps bounds, hit table, indices and
+// vertices as separate GL buffer textures, src/core/Scene.cpp:245-250):
+//
+//   node records  float4[6][M][2]   32-byte record per threaded-table entry,
+//                                   in traversal order of its face:
+//                                     [0] = pMin.xyz, prim (int bits, -1 = inner)
+//                                     [1] = pMax.xyz, miss (int bits)
+//                 Each face stores every node in its own visiting order, so the
+//                 common step k -> k+1 reads the next 32 bytes (streaming,
+//                 sector-aligned, two 16-byte read-only loads).
+//   triangles     float4[ntri][3]   a.xyz ab.x | ab.yz ac.xy | ac.z, 0
+//                                   (ab = b - a and ac = c - a evaluated on the
+//                                   host in float32, exactly the values the
+//                                   ray-triangle test forms, intersection.glsl:68-69)
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bvh_build.h"
+
+struct zgl_accel {
+    int device = 0;
+    int64_t ntri = 0;
+    int64_t M = 0;
+    zgl::HostBVH host;
+    float4* d_nodes = nullptr;  // 6*M*2
+    float4* d_tris = nullptr;   // ntri*3
+    // staging for calls made with host arrays
+    mutable void* d_stage = nullptr;
+    mutable size_t stage_bytes = 0;
+};
+
+namespace zgl {
+
+struct DeviceAccel {
+    const float4* nodes;
+    const float4* tris;
+    int32_t M;
+};
+
+inline DeviceAccel device_view(const zgl_accel* a) {
+    return DeviceAccel{a->d_nodes, a->d_tris, (int32_t)a->M};
+}
+
+// Kernel launchers (accel.cu).  All pointers are device pointers.
+cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
+                              cudaStream_t s);
+cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
+                                 int32_t* hit_id, float* hit_t, cudaStream_t s);
+cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
+                             int64_t n, uint8_t* occluded, cudaStream_t s);
+cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir, const float* tmax,
+                               int64_t n, int any_hit, int32_t* visits, int32_t* tests,
+                               cudaStream_t s);
+
+}  // namespace zgl
