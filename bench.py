@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent"])
+    ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
     return ap.parse_args()
 
 
@@ -167,13 +169,15 @@ def run_ours(args):
         v, idx = build_scene(N)
         t0 = time.time()
         acc = BVH(v, idx).build()
+        acc.set_trace_schedule(args.schedule)
         log(f"[bench] N={N}: build+upload {time.time() - t0:.1f}s, {acc.node_count} nodes")
         to = torch.from_numpy(o_p).to(dev)
         td = torch.from_numpy(d_p).to(dev)
         hid, ht = acc.trace_closest(to, td, stream=stream)
         stream.synchronize()
         o_i, d_i = incoherent_rays(v, idx, o_p, d_p, hid.cpu().numpy(), ht.cpu().numpy(), seed=SEEDS.get(N, 7) + 1)
-        tm_p = torch.from_numpy(shadow_tmax(nray, SEEDS.get(N, 7) + 2)).to(dev)
+        # the camera sits 1 unit in front of the cube: primary shadow distances are 1 + U(0, 1)
+        tm_p = torch.from_numpy(1.0 + shadow_tmax(nray, SEEDS.get(N, 7) + 2)).to(dev)
         tm_i = torch.from_numpy(shadow_tmax(nray, SEEDS.get(N, 7) + 3)).to(dev)
         fam = {"primary": (to, td, tm_p, o_p, d_p), "incoherent": (torch.from_numpy(o_i).to(dev),
                                                                    torch.from_numpy(d_i).to(dev), tm_i, o_i, d_i)}
@@ -183,6 +187,9 @@ def run_ours(args):
                               "o_host": oh, "d_host": dh, "query": q})
         scenes.append((N, v, idx, acc))
         del v, idx
+    if args.only:
+        keep = [k for k in args.only.split(",") if k]
+        specs = [sp for sp in specs if any(k in sp["name"] for k in keep)]
     log(f"[bench] setup {time.time() - t_setup:.1f}s, {len(specs)} launches/step")
 
     # outputs (device)
@@ -371,6 +378,7 @@ def cpu_baseline(scenes, specs, target_s: float):
         return rays, time.perf_counter() - t0
 
     probe = 2048
+    run(256)  # warm: loads the oracle library
     r, s = run(probe)
     sample = int(min(specs[0]["o_host"].shape[0], max(probe, probe * target_s / max(s, 1e-3))))
     r, s = run(sample)
@@ -392,7 +400,7 @@ def run_reference(args):
     sizes = [SIZES[s] for s in args.sizes.split(",")]
     side = args.side
     o_p, d_p = primary_rays(side, side)
-    sample = 4096
+    sample = 16384
     rng = np.random.default_rng(0)
     sel = np.sort(rng.choice(o_p.shape[0], sample, replace=False))
     work = []
@@ -402,13 +410,14 @@ def run_reference(args):
         o, d = o_p[sel], d_p[sel]
         hid, ht, _, _ = oracle.trace(b, h, v, idx, o, d, nthreads=nthreads)
         o_i, d_i = incoherent_rays(v, idx, o, d, hid, ht, seed=SEEDS.get(N, 7) + 1)
-        tm = shadow_tmax(sample, SEEDS.get(N, 7) + 2)
-        work.append((b, h, v, idx, o, d, o_i, d_i, tm))
+        tm_p = 1.0 + shadow_tmax(sample, SEEDS.get(N, 7) + 2)
+        tm_i = shadow_tmax(sample, SEEDS.get(N, 7) + 3)
+        work.append((b, h, v, idx, o, d, o_i, d_i, tm_p, tm_i))
 
     def step():
         rays = 0
-        for b, h, v, idx, o, d, o_i, d_i, tm in work:
-            for oo, dd in ((o, d), (o_i, d_i)):
+        for b, h, v, idx, o, d, o_i, d_i, tm_p, tm_i in work:
+            for oo, dd, tm in ((o, d, tm_p), (o_i, d_i, tm_i)):
                 oracle.trace(b, h, v, idx, oo, dd, nthreads=nthreads)
                 oracle.trace(b, h, v, idx, oo, dd, tmax=tm, any_hit=True, nthreads=nthreads)
                 rays += 2 * oo.shape[0]

@@ -83,6 +83,15 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices,
                               const uint32_t* indices, size_t n_triangles,
                               float* bounds, int32_t* hit_table);
 
+/* Trace kernel schedule of an accelerator: ZGL_TRACE_AUTO (0, default),
+ * ZGL_TRACE_THREAD_PER_RAY (1: one thread per ray, neighbouring rays share a
+ * warp) or ZGL_TRACE_PERSISTENT (2: persistent warps that refill idle lanes
+ * by atomic fetch).  Results are identical; only speed differs.  The
+ * reference has one fixed schedule (one invocation per pixel or path,
+ * src/integrator/NaivePath.cpp:94-100). */
+enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2 };
+zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule);
+
 /* Closest hit of n rays (origins/dirs float[n*3]): hit_id int32[n] (primitive
  * id, -1 on miss) and hit_t float[n] (1e8 on miss).
  * Replaces bvhHit (src/shader/intersection.glsl:395-427). */

@@ -64,20 +64,30 @@ def test_primary_and_incoherent_closest_bit_exact(soup, cuda):
     _check_closest(acc, packed, v, idx, o2, d2, cuda)
 
 
-def test_mixed_rays_closest_bit_exact(soup, cuda):
+@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent"])
+def test_mixed_rays_closest_bit_exact(soup, cuda, schedule):
     acc, packed, v, idx = soup
-    o, d = _rays_mixed(np.random.default_rng(3), 20000)
-    _check_closest(acc, packed, v, idx, o, d, cuda)
+    acc.set_trace_schedule(schedule)
+    try:
+        o, d = _rays_mixed(np.random.default_rng(3), 20000)
+        _check_closest(acc, packed, v, idx, o, d, cuda)
+    finally:
+        acc.set_trace_schedule("auto")
 
 
-def test_any_hit_bit_exact(soup, cuda):
+@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent"])
+def test_any_hit_bit_exact(soup, cuda, schedule):
     import torch
 
     acc, packed, v, idx = soup
     o, d = _rays_mixed(np.random.default_rng(4), 20000)
     tmax = shadow_tmax(o.shape[0], 5)
-    occ = acc.trace_any(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda),
-                        torch.from_numpy(tmax).to(cuda)).cpu().numpy()
+    acc.set_trace_schedule(schedule)
+    try:
+        occ = acc.trace_any(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda),
+                            torch.from_numpy(tmax).to(cuda)).cpu().numpy()
+    finally:
+        acc.set_trace_schedule("auto")
     oocc, _, ovis, otst = oracle.trace(packed.bounds, packed.hitTable, v, idx, o, d, tmax=tmax, any_hit=True)
     assert np.array_equal(occ.astype(np.int32), oocc)
     vis, tst = acc.trace_count(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda),

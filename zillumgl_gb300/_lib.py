@@ -49,6 +49,7 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_accel_export": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_accel_destroy": (C.c_int32, [C.c_void_p]),
     "zgl_bvh_build_host": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "zgl_accel_set_trace_schedule": (C.c_int32, [C.c_void_p, C.c_int32]),
     "zgl_trace_closest": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
     "zgl_trace_any": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,

@@ -116,6 +116,12 @@ class Accelerator:
         call("zgl_accel_export", self._h, _ptr(bounds), _ptr(hit))
         return PackedBVH(bounds, hit)
 
+    SCHEDULES = {"auto": 0, "thread_per_ray": 1, "persistent": 2}
+
+    def set_trace_schedule(self, schedule: str) -> None:
+        """Select the trace kernel schedule (results are identical)."""
+        call("zgl_accel_set_trace_schedule", self._h, self.SCHEDULES[schedule])
+
     # -- queries -------------------------------------------------------------
     def trace_closest(self, origins, dirs, hit_id=None, hit_t=None, stream=None):
         """bvhHit: closest primitive id (-1 on miss) and distance (1e8 on miss)."""

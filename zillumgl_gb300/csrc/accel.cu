@@ -77,6 +77,97 @@ trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// ---------------------------------------------------------------------------
+// Persistent traversal: each warp keeps all 32 lanes busy by refilling a lane
+// with the next ray as soon as its traversal ends.  Idle lanes are counted
+// with __ballot_sync/__popc, one lane grabs that many ray indices with a
+// single atomicAdd on the work counter, and each idle lane takes its rank.
+// Every ray is still traversed by one lane in exactly the reference order, so
+// results are identical to the one-thread-per-ray kernels.
+// ---------------------------------------------------------------------------
+constexpr int kPersistBlock = 128;
+constexpr unsigned kFull = 0xffffffffu;
+
+template <bool ANY>
+__global__ void __launch_bounds__(kPersistBlock)
+trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                        const float* __restrict__ tmax, int64_t n, int32_t* __restrict__ hit_id,
+                        float* __restrict__ hit_t, uint8_t* __restrict__ occ,
+                        unsigned long long* __restrict__ counter) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int M = a.M;
+    bool active = false;
+    bool exhausted = false;  // warp-uniform
+    int64_t ray = 0;
+    TraceRay r;
+    const float4* __restrict__ base = a.nodes;
+    float dist = 0.0f;
+    int k = 0, closest = -1;
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            const unsigned cnt = __popc(idle);
+            unsigned long long b = 0;
+            if (lane == leader) b = atomicAdd(counter, (unsigned long long)cnt);
+            b = __shfl_sync(kFull, b, leader);
+            if (b + cnt >= (unsigned long long)n) exhausted = true;
+            if (!active) {
+                const unsigned long long idx = b + __popc(idle & lt);
+                if (idx < (unsigned long long)n) {
+                    ray = (int64_t)idx;
+                    r = make_trace_ray(load3(org, ray), load3(dir, ray));
+                    base = a.nodes + (size_t)r.face * (size_t)M * 2;
+                    dist = ANY ? tmax[ray] : 1e8f;
+                    k = 0;
+                    closest = -1;
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(kFull, active) == 0u) break;
+        if (active) {
+            const float4 lo = __ldg(base + 2 * (size_t)k);
+            const float4 hi = __ldg(base + 2 * (size_t)k + 1);
+            float tmin;
+            const bool h = box_hit(lo, hi, r, tmin) && !(tmin > dist);
+            const int prim = __float_as_int(lo.w);
+            int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+            if (h && prim >= 0) {
+                float t;
+                if (tri_hit(a.tris, prim, r, t) && t < dist) {
+                    dist = t;
+                    closest = prim;
+                    if (ANY) next = M;
+                }
+            }
+            k = next;
+            if (k >= M) {
+                if (ANY) {
+                    occ[ray] = (uint8_t)(closest >= 0);
+                } else {
+                    hit_id[ray] = closest;
+                    hit_t[ray] = dist;
+                }
+                active = false;
+            }
+        }
+    }
+}
+
+int persistent_grid(const void* kernel) {
+    static int cached = 0;
+    if (cached) return cached;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistBlock, 0);
+    if (per_sm < 1) per_sm = 1;
+    cached = sms * per_sm;
+    return cached;
+}
+
 }  // namespace
 
 cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
@@ -89,16 +180,36 @@ cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M
 }
 
 cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
-                                 int32_t* hit_id, float* hit_t, cudaStream_t s) {
+                                 int32_t* hit_id, float* hit_t, unsigned long long* counter, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
+    if (a.M == 0 || counter == nullptr) {
+        trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    int grid = persistent_grid((const void*)trace_persistent_kernel<false>);
+    int64_t need = (n + 31) / 32 * 32 / kPersistBlock + 1;
+    if (need < grid) grid = (int)need;
+    trace_persistent_kernel<false><<<grid, kPersistBlock, 0, s>>>(a, org, dir, nullptr, n, hit_id, hit_t, nullptr,
+                                                                  counter);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
-                             int64_t n, uint8_t* occ, cudaStream_t s) {
+                             int64_t n, uint8_t* occ, unsigned long long* counter, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
+    if (a.M == 0 || counter == nullptr) {
+        trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    int grid = persistent_grid((const void*)trace_persistent_kernel<true>);
+    int64_t need = (n + 31) / 32 * 32 / kPersistBlock + 1;
+    if (need < grid) grid = (int)need;
+    trace_persistent_kernel<true><<<grid, kPersistBlock, 0, s>>>(a, org, dir, tmax, n, nullptr, nullptr, occ,
+                                                                 counter);
     return cudaGetLastError();
 }
 
@@ -205,6 +316,12 @@ private:
     int prev_ = 0, dev_ = 0;
 };
 
+// The auto schedule is thread-per-ray: neighbouring rays of a batch stay in
+// one warp, which keeps their node fetches coalesced.
+unsigned long long* persistent_counter(const zgl_accel* a) {
+    return a->trace_schedule == ZGL_TRACE_PERSISTENT ? a->d_counter : nullptr;
+}
+
 int host_threads() {
     unsigned n = std::thread::hardware_concurrency();
     return n == 0 ? 1 : (int)n;
@@ -255,6 +372,7 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint3
     auto* a = new zgl_accel();
     try {
         ZGL_CUDA(cudaGetDevice(&a->device));
+        ZGL_CUDA(cudaMalloc(&a->d_counter, 256));
         a->ntri = (int64_t)n_triangles;
         build_bvh(vertices, indices, a->ntri, a->host, host_threads());
         a->M = a->host.M;
@@ -287,6 +405,7 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint3
             ZGL_CUDA(cudaFree(d_hit));
         }
     } catch (...) {
+        if (a->d_counter) cudaFree(a->d_counter);
         if (a->d_nodes) cudaFree(a->d_nodes);
         if (a->d_tris) cudaFree(a->d_tris);
         delete a;
@@ -321,7 +440,17 @@ zgl_status zgl_accel_destroy(zgl_accel* accel) {
     if (accel->d_nodes) cudaFree(accel->d_nodes);
     if (accel->d_tris) cudaFree(accel->d_tris);
     if (accel->d_stage) cudaFree(accel->d_stage);
+    if (accel->d_counter) cudaFree(accel->d_counter);
     delete accel;
+    ZGL_API_END
+}
+
+zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: NULL accel");
+    if (schedule < ZGL_TRACE_AUTO || schedule > ZGL_TRACE_PERSISTENT)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: unknown schedule %d", schedule);
+    accel->trace_schedule = schedule;
     ZGL_API_END
 }
 
@@ -338,7 +467,7 @@ zgl_status zgl_trace_closest(const zgl_accel* accel, const float* origins, const
     int si = st.add(hit_id, 4 * n, false, true), sx = st.add(hit_t, 4 * n, false, true);
     st.commit();
     ZGL_CUDA(launch_trace_closest(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
-                                  (int64_t)n, (int32_t*)st.ptr(si), (float*)st.ptr(sx), s));
+                                  (int64_t)n, (int32_t*)st.ptr(si), (float*)st.ptr(sx), persistent_counter(accel), s));
     st.finish();
     ZGL_API_END
 }
@@ -356,7 +485,8 @@ zgl_status zgl_trace_any(const zgl_accel* accel, const float* origins, const flo
     int sm = st.add(tmax, 4 * n, true, false), sc = st.add(occluded, n, false, true);
     st.commit();
     ZGL_CUDA(launch_trace_any(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
-                              (const float*)st.ptr(sm), (int64_t)n, (uint8_t*)st.ptr(sc), s));
+                              (const float*)st.ptr(sm), (int64_t)n, (uint8_t*)st.ptr(sc), persistent_counter(accel),
+                              s));
     st.finish();
     ZGL_API_END
 }

@@ -29,6 +29,10 @@ struct zgl_accel {
     zgl::HostBVH host;
     float4* d_nodes = nullptr;  // 6*M*2
     float4* d_tris = nullptr;   // ntri*3
+    // work counter of the persistent trace kernels (reset before each launch;
+    // launches of one handle are serialised on its caller's stream)
+    unsigned long long* d_counter = nullptr;
+    int trace_schedule = 0;  // ZGL_TRACE_*
     // staging for calls made with host arrays
     mutable void* d_stage = nullptr;
     mutable size_t stage_bytes = 0;
@@ -49,10 +53,11 @@ inline DeviceAccel device_view(const zgl_accel* a) {
 // Kernel launchers (accel.cu).  All pointers are device pointers.
 cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
                               cudaStream_t s);
+// `counter` non-null selects the persistent schedule.
 cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
-                                 int32_t* hit_id, float* hit_t, cudaStream_t s);
+                                 int32_t* hit_id, float* hit_t, unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
-                             int64_t n, uint8_t* occluded, cudaStream_t s);
+                             int64_t n, uint8_t* occluded, unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir, const float* tmax,
                                int64_t n, int any_hit, int32_t* visits, int32_t* tests,
                                cudaStream_t s);

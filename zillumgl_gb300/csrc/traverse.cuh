@@ -20,8 +20,11 @@ namespace zgl {
 
 struct TraceRay {
     float3 o, d, dinv;
-    int mode;  // 0/1/2: |d.axis| > 1 - 1e-6 (axis-dominant branch), 3: general
-    bool sx, sy, sz;  // |d.axis| < 1e-6 (near-zero-component branches)
+    // 0/1/2: |d.axis| > 1 - 1e-6 (axis-dominant branch of boxHit)
+    // 3: general slab test, no component below 1e-6 in magnitude
+    // 4: general slab test with near-zero-component branches
+    int mode;
+    bool sx, sy, sz;  // |d.axis| < 1e-6
     int face;         // cubemapFace(-dir) (math.glsl:112-131)
 };
 
@@ -33,10 +36,10 @@ __device__ __forceinline__ TraceRay make_trace_ray(float3 o, float3 d) {
     const float eps = 1e-6f;
     const float big = 1.0f - eps;
     float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    r.mode = (ax > big) ? 0 : (ay > big) ? 1 : (az > big) ? 2 : 3;
     r.sx = ax < eps;
     r.sy = ay < eps;
     r.sz = az < eps;
+    r.mode = (ax > big) ? 0 : (ay > big) ? 1 : (az > big) ? 2 : ((r.sx || r.sy || r.sz) ? 4 : 3);
     // cubemapFace(-d): maxExtent(|-d|) with strict '>', sign of -d
     float nx = -d.x, ny = -d.y, nz = -d.z;
     int m = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
@@ -44,33 +47,22 @@ __device__ __forceinline__ TraceRay make_trace_ray(float3 o, float3 d) {
     return r;
 }
 
-// boxHit.  fminf/fmaxf return the non-NaN operand like GPU GLSL min/max; the
-// returned tMin only takes part in comparisons, so the sign of a zero result
-// never matters.
-__device__ __forceinline__ bool box_hit(const float4 lo, const float4 hi, const TraceRay& r,
-                                        float& tmin) {
+// boxHit specialised by ray mode.  fminf/fmaxf return the non-NaN operand
+// like GPU GLSL min/max; the returned tMin only takes part in comparisons, so
+// the sign of a zero result never matters.
+template <int MODE>
+__device__ __forceinline__ bool box_hit_m(const float4 lo, const float4 hi, const TraceRay& r, float& tmin) {
     const float3 o = r.o;
-    if (r.mode == 0) {
-        if (o.y > lo.y && o.y < hi.y && o.z > lo.z && o.z < hi.z) {
-            float ta = (lo.x - o.x) * r.dinv.x, tb = (hi.x - o.x) * r.dinv.x;
-            tmin = fminf(ta, tb);
-            float tmax = fmaxf(ta, tb);
-            return tmax >= 0.0f && tmax >= tmin;
-        }
-        return false;
-    }
-    if (r.mode == 1) {
-        if (o.x > lo.x && o.x < hi.x && o.z > lo.z && o.z < hi.z) {
-            float ta = (lo.y - o.y) * r.dinv.y, tb = (hi.y - o.y) * r.dinv.y;
-            tmin = fminf(ta, tb);
-            float tmax = fmaxf(ta, tb);
-            return tmax >= 0.0f && tmax >= tmin;
-        }
-        return false;
-    }
-    if (r.mode == 2) {
-        if (o.x > lo.x && o.x < hi.x && o.y > lo.y && o.y < hi.y) {
-            float ta = (lo.z - o.z) * r.dinv.z, tb = (hi.z - o.z) * r.dinv.z;
+    if (MODE == 0 || MODE == 1 || MODE == 2) {
+        // slab along the dominant axis, strict inside test on the other two
+        const float oa = MODE == 0 ? o.x : MODE == 1 ? o.y : o.z;
+        const float ia = MODE == 0 ? r.dinv.x : MODE == 1 ? r.dinv.y : r.dinv.z;
+        const float la = MODE == 0 ? lo.x : MODE == 1 ? lo.y : lo.z;
+        const float ha = MODE == 0 ? hi.x : MODE == 1 ? hi.y : hi.z;
+        const float ob = MODE == 0 ? o.y : o.x, lb = MODE == 0 ? lo.y : lo.x, hb = MODE == 0 ? hi.y : hi.x;
+        const float oc = MODE == 2 ? o.y : o.z, lc = MODE == 2 ? lo.y : lo.z, hc = MODE == 2 ? hi.y : hi.z;
+        if (ob > lb && ob < hb && oc > lc && oc < hc) {
+            float ta = (la - oa) * ia, tb = (ha - oa) * ia;
             tmin = fminf(ta, tb);
             float tmax = fmaxf(ta, tb);
             return tmax >= 0.0f && tmax >= tmin;
@@ -84,27 +76,36 @@ __device__ __forceinline__ bool box_hit(const float4 lo, const float4 hi, const 
     float dx = fx - nx, dy = fy - ny, dz = fz - nz;
     float tyz = fz - ny, tzx = fx - nz, txy = fy - nx;
     float tmax;
-    if (r.sx && dy + dz > tyz) {
-        tmin = fmaxf(ny, nz);
-        tmax = fminf(fy, fz);
-        return tmax >= 0.0f && tmax >= tmin;
+    if (MODE == 4) {
+        if (r.sx && dy + dz > tyz) {
+            tmin = fmaxf(ny, nz);
+            tmax = fminf(fy, fz);
+            return tmax >= 0.0f && tmax >= tmin;
+        }
+        if (r.sy && dz + dx > tzx) {
+            tmin = fmaxf(nz, nx);
+            tmax = fminf(fz, fx);
+            return tmax >= 0.0f && tmax >= tmin;
+        }
+        if (r.sz && dx + dy > txy) {
+            tmin = fmaxf(nx, ny);
+            tmax = fminf(fx, fy);
+            return tmax >= 0.0f && tmax >= tmin;
+        }
     }
-    if (r.sy && dz + dx > tzx) {
-        tmin = fmaxf(nz, nx);
-        tmax = fminf(fz, fx);
-        return tmax >= 0.0f && tmax >= tmin;
+    tmin = fmaxf(fmaxf(nx, ny), nz);
+    tmax = fminf(fminf(fx, fy), fz);
+    return (dy + dz > tyz) && (dz + dx > tzx) && (dx + dy > txy) && tmax >= 0.0f && tmax >= tmin;
+}
+
+__device__ __forceinline__ bool box_hit(const float4 lo, const float4 hi, const TraceRay& r, float& tmin) {
+    switch (r.mode) {
+        case 0: return box_hit_m<0>(lo, hi, r, tmin);
+        case 1: return box_hit_m<1>(lo, hi, r, tmin);
+        case 2: return box_hit_m<2>(lo, hi, r, tmin);
+        case 3: return box_hit_m<3>(lo, hi, r, tmin);
+        default: return box_hit_m<4>(lo, hi, r, tmin);
     }
-    if (r.sz && dx + dy > txy) {
-        tmin = fmaxf(nx, ny);
-        tmax = fminf(fx, fy);
-        return tmax >= 0.0f && tmax >= tmin;
-    }
-    if (dy + dz > tyz && dz + dx > tzx && dx + dy > txy) {
-        tmin = fmaxf(fmaxf(nx, ny), nz);
-        tmax = fminf(fminf(fx, fy), fz);
-        return tmax >= 0.0f && tmax >= tmin;
-    }
-    return false;
 }
 
 // intersectTriangle with precomputed a, ab = b - a, ac = c - a.
@@ -144,37 +145,47 @@ __device__ __forceinline__ bool tri_hit(const float4* __restrict__ tris, int pri
 // bvhHit (ANY = false): returns the closest primitive or -1 and lowers `dist`.
 // bvhTest (ANY = true): returns 1 at the first t < dist, else 0.
 // The loop index only grows (k = max(miss, k + 1)), so it ends within M steps
-// even on a corrupted table.
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ int traverse(const DeviceAccel& a, const TraceRay& r, float& dist,
-                                        int& visits, int& tests) {
+// even on a corrupted table.  The loop is instantiated per ray mode so that
+// the common general case carries no per-visit mode tests.
+template <bool ANY, bool COUNT, int MODE>
+__device__ __forceinline__ int traverse_m(const DeviceAccel& a, const TraceRay& r, float& dist, int& visits,
+                                          int& tests) {
     const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
     int closest = -1;
     int k = 0;
     const int M = a.M;
     while (k < M) {
-        const float4 lo = __ldg(base + 2 * (size_t)k);
-        const float4 hi = __ldg(base + 2 * (size_t)k + 1);
+        const float4 lo = __ldg(base + 2 * k);
+        const float4 hi = __ldg(base + 2 * k + 1);
         if (COUNT) visits++;
         float tmin;
-        bool h = box_hit(lo, hi, r, tmin);
-        if (!h || tmin > dist) {
-            k = max(__float_as_int(hi.w), k + 1);
-            continue;
-        }
-        int prim = __float_as_int(lo.w);
-        if (prim >= 0) {
+        const bool h = box_hit_m<MODE>(lo, hi, r, tmin) && !(tmin > dist);
+        const int prim = __float_as_int(lo.w);
+        int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+        if (h && prim >= 0) {
             if (COUNT) tests++;
             float t;
             if (tri_hit(a.tris, prim, r, t) && t < dist) {
-                if (ANY) return 1;
-                dist = t;
                 closest = prim;
+                if (ANY) break;
+                dist = t;
             }
         }
-        k++;
+        k = next;
     }
-    return ANY ? 0 : closest;
+    return ANY ? (closest >= 0 ? 1 : 0) : closest;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ int traverse(const DeviceAccel& a, const TraceRay& r, float& dist, int& visits,
+                                        int& tests) {
+    switch (r.mode) {
+        case 3: return traverse_m<ANY, COUNT, 3>(a, r, dist, visits, tests);
+        case 4: return traverse_m<ANY, COUNT, 4>(a, r, dist, visits, tests);
+        case 0: return traverse_m<ANY, COUNT, 0>(a, r, dist, visits, tests);
+        case 1: return traverse_m<ANY, COUNT, 1>(a, r, dist, visits, tests);
+        default: return traverse_m<ANY, COUNT, 2>(a, r, dist, visits, tests);
+    }
 }
 
 }  // namespace zgl
