@@ -112,6 +112,130 @@ zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const f
                            const float* tmax, size_t n, int32_t any_hit,
                            int32_t* visits, int32_t* tests, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Scene: flattened geometry, materials, lights, environment, camera         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct zgl_scene zgl_scene;
+
+/* World-space scene arrays (host pointers, borrowed for the call).  Object
+ * triangles come first and light triangles after them, exactly as
+ * Scene::createGLContext flattens them (src/core/Scene.cpp:148-195): a light
+ * triangle k gets primitive id obj_n_triangles + k.  Per-vertex normals are
+ * required; texture coordinates are optional (textures are not supported yet,
+ * every obj_mat_tex entry must have texture index -1, i.e. 0xffff in the upper
+ * half).  Materials are 16 floats each in the layout of struct Material
+ * (src/core/Material.h:32-53) with the type stored as int32 bits in float
+ * slot 13.  Light instance k owns light triangles [light_first[k],
+ * light_first[k+1]) and total power light_power[3k..3k+2], split over its
+ * triangles by area (Scene.cpp:200-243).  env_rgb is an optional float RGB
+ * image (env_width x env_height), uploaded as RGB16F like EnvironmentMap
+ * (src/core/EnvironmentMap.cpp:8-59); NULL means a black environment.  The
+ * camera follows Camera::update (src/core/Camera.cpp:149-162). */
+typedef struct zgl_scene_desc {
+    const float* obj_vertices;
+    size_t obj_n_vertices;
+    const float* obj_normals;
+    const uint32_t* obj_indices;
+    size_t obj_n_triangles;
+    const int32_t* obj_mat_tex;     /* per object triangle: (tex << 16) | mat */
+    const float* materials;         /* 16 floats per material */
+    size_t n_materials;
+    const float* light_vertices;
+    size_t light_n_vertices;
+    const float* light_normals;
+    const uint32_t* light_indices;  /* local to the light vertex array */
+    size_t light_n_triangles;
+    const uint32_t* light_first;    /* n_light_instances + 1 offsets */
+    const float* light_power;       /* rgb per instance */
+    size_t n_light_instances;
+    const float* env_rgb;
+    int32_t env_width, env_height;
+    float env_rotation;
+    float cam_pos[3];
+    float cam_angle[3];             /* degrees: yaw, pitch; roll as Camera.cpp uses it */
+    float cam_fov;                  /* degrees, clamped to [0.1, 90] like Camera::setFOV */
+    float cam_lens_radius;
+    float cam_focal_dist;
+    int32_t film_width, film_height;
+    int32_t sampler;                /* 0 independent (rand), 1 sobol */
+} zgl_scene_desc;
+
+enum { ZGL_SCENE_HOST_ONLY = 1 };
+
+/* Build the scene tables (light power/alias, environment alias tables, Sobol
+ * matrices, per-pixel seeds) and, unless flags has ZGL_SCENE_HOST_ONLY, the
+ * MTBVH and all device buffers on the current device.  Replaces
+ * Scene::createGLContext (src/core/Scene.cpp:133-270). */
+zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene** out);
+
+/* Copy a named host table into `out` (`bytes` must match exactly):
+ *   "light_power" float[nL*3], "light_alias" int32[nL], "light_prob" float[nL],
+ *   "env_alias" int32[(W+1)*H], "env_prob" float[(W+1)*H],
+ *   "env_texels" float[W*H*3] (after RGB16F rounding), "sobol" uint32[256*32],
+ *   "noise" float[filmW*filmH*2], "pixel_seeds" uint32[filmW*filmH*2],
+ *   "camera" float[19] (front, right, up, inverse camera matrix column-major,
+ *   tan(fov/2)), "scalars" float[4] (lightSum, envSum as used by the shaders,
+ *   objPrimCount, nLightTriangles). */
+zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out, size_t bytes);
+
+zgl_status zgl_scene_destroy(zgl_scene* scene);
+
+/* Alias table of a discrete pdf (Walker/Vose), host only: alias int32[n] and
+ * prob float[n].  Same construction as AliasTable::build<int32_t>
+ * (src/math/AliasTable.h:12-54), which the light-selection table uses. */
+zgl_status zgl_alias_table_build(const float* pdf, size_t n, int32_t* alias, float* prob);
+
+/* ------------------------------------------------------------------------ */
+/* Integrators (class Integrator, src/core/Integrator.h:25-52)               */
+/* ------------------------------------------------------------------------ */
+
+typedef struct zgl_integrator zgl_integrator;
+
+enum { ZGL_INTEGRATOR_PATH = 0 };
+
+/* Parameters of PathIntegParam (src/core/Integrator.h:56-66) plus
+ * rr_start_depth: Russian roulette runs from this bounce on (1 = every
+ * bounce, the reference's behaviour). */
+typedef struct zgl_integrator_params {
+    int32_t max_depth;                /* 4 */
+    int32_t russian_roulette;         /* 0 */
+    int32_t rr_start_depth;           /* 1 */
+    int32_t sample_light;             /* 1 */
+    int32_t light_env_uniform_sample; /* 0 */
+    float light_portion;              /* 0.5 */
+    int32_t finite_sample;            /* 0 */
+    int32_t max_sample;               /* 64 */
+} zgl_integrator_params;
+
+/* Fill the reference defaults. */
+zgl_status zgl_integrator_params_default(zgl_integrator_params* params);
+
+/* Integrator::init (NaivePath.cpp:69-75): allocate the frame (film size of
+ * the scene) on the scene's device.  The scene must outlive the integrator. */
+zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integrator_params* params,
+                                 zgl_integrator** out);
+
+/* Integrator::renderOnePass (NaivePath.cpp:77-105): one sample per pixel,
+ * accumulated into the frame; asynchronous on `stream`. */
+zgl_status zgl_integrator_render_pass(zgl_integrator* integ, void* stream);
+
+/* Integrator::reset (NaivePath.cpp:107-115): the next pass restarts the
+ * progressive sum at sample 0. */
+zgl_status zgl_integrator_reset(zgl_integrator* integ);
+
+/* Integrator::getFrame: the frame holds the running SUM of samples, RGBA
+ * float[filmW*filmH*4], row y = 0 first (GL convention: bottom row).  `out`
+ * may be host or device memory; spp (may be NULL) receives the passes done.
+ * Synchronous for host memory. */
+zgl_status zgl_integrator_frame(zgl_integrator* integ, float* out, int32_t* spp, void* stream);
+
+/* Integrator::resultScale (Integrator.h:79): 1 / (samples + 1) for the path
+ * tracer (the reference's display scale; divide the sum by spp for the mean). */
+zgl_status zgl_integrator_result_scale(const zgl_integrator* integ, float* out);
+
+zgl_status zgl_integrator_destroy(zgl_integrator* integ);
+
 #ifdef __cplusplus
 }
 #endif

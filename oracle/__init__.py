@@ -99,3 +99,176 @@ def trace(packed_bounds, packed_hit, vertices, indices, origins, dirs, tmax=None
     lib().orc_trace(_p(b), _p(h), b.shape[0], _p(v), _p(idx), _p(o), _p(d), _p(tm), n, int(any_hit), _p(hid),
                     _p(ht), _p(vis), _p(tst), nthreads or threads())
     return hid, ht, vis, tst
+
+
+# ---------------------------------------------------------------------------
+# Path tracer oracle
+# ---------------------------------------------------------------------------
+class OrcScene(C.Structure):
+    _fields_ = [
+        ("vertices", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p), ("matTexIndex", C.c_void_p),
+        ("nTriangles", C.c_int64), ("objPrimCount", C.c_int32),
+        ("bounds", C.c_void_p), ("hitTable", C.c_void_p), ("bvhSize", C.c_int64),
+        ("materials", C.c_void_p),
+        ("nLightTriangles", C.c_int32), ("lightPower", C.c_void_p), ("lightAlias", C.c_void_p),
+        ("lightProb", C.c_void_p), ("lightSum", C.c_float),
+        ("envTexels", C.c_void_p), ("envWidth", C.c_int32), ("envHeight", C.c_int32), ("envAlias", C.c_void_p),
+        ("envProb", C.c_void_p), ("envSum", C.c_float), ("envRotation", C.c_float),
+        ("sobolMatrices", C.c_void_p), ("noise", C.c_void_p), ("sampler", C.c_int32),
+        ("camF", C.c_float * 3), ("camR", C.c_float * 3), ("camU", C.c_float * 3), ("camPos", C.c_float * 3),
+        ("camMatInv", C.c_float * 9), ("tanFOV", C.c_float), ("lensRadius", C.c_float), ("focalDist", C.c_float),
+        ("camAsp", C.c_float), ("filmW", C.c_int32), ("filmH", C.c_int32),
+        ("maxDepth", C.c_int32), ("russianRoulette", C.c_int32), ("sampleLight", C.c_int32),
+        ("lightEnvUniformSample", C.c_int32), ("lightPortion", C.c_float), ("rrStartDepth", C.c_int32),
+    ]
+
+
+def _render_lib():
+    L = lib()
+    if not getattr(L, "_render_ready", False):
+        L.orc_light_tables.restype = C.c_float
+        L.orc_light_tables.argtypes = [C.c_void_p] * 4 + [C.c_int32] + [C.c_void_p] * 3
+        L.orc_env_tables.restype = C.c_float
+        L.orc_env_tables.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
+        L.orc_noise.restype = None
+        L.orc_noise.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
+        L.orc_camera.restype = None
+        L.orc_camera.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
+        L.orc_render_pt.restype = None
+        L.orc_render_pt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                    C.c_void_p, C.c_int32]
+        L.orc_alias_build.restype = None
+        L.orc_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+        L.orc_transc.restype = None
+        L.orc_transc.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L._render_ready = True
+    return L
+
+
+def light_tables(data):
+    """(lightPower (nL,3), alias, prob, lightSum) restating Scene.cpp:200-243."""
+    nl = data.light_indices.size // 3
+    power = np.zeros((nl, 3), np.float32)
+    alias = np.zeros(nl, np.int32)
+    prob = np.zeros(nl, np.float32)
+    if nl == 0:
+        return power, alias, prob, np.float32(0)
+    s = _render_lib().orc_light_tables(_p(data.light_vertices), _p(data.light_indices), _p(data.light_first),
+                                       _p(data.light_power), data.light_power.shape[0], _p(power), _p(alias),
+                                       _p(prob))
+    return power, alias, prob, np.float32(s)
+
+
+def alias_build(pdf):
+    pdf = np.ascontiguousarray(pdf, np.float32)
+    alias = np.zeros(pdf.size, np.int32)
+    prob = np.zeros(pdf.size, np.float32)
+    _render_lib().orc_alias_build(_p(pdf), pdf.size, _p(alias), _p(prob))
+    return alias, prob
+
+
+def ref_alias_build(pdf):
+    """AliasTable::build from the reference header itself (None without the tree)."""
+    ref = ref_lib()
+    if ref is None:
+        return None
+    pdf = np.ascontiguousarray(pdf, np.float32)
+    alias = np.zeros(pdf.size, np.int32)
+    prob = np.zeros(pdf.size, np.float32)
+    ref.ref_alias_build(_p(pdf), pdf.size, _p(alias), _p(prob))
+    return alias, prob
+
+
+def env_tables(rgb):
+    """(alias, prob, sum) restating EnvironmentMap.cpp:8-114 for an (H, W, 3) image."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    H, W = rgb.shape[:2]
+    alias = np.zeros((W + 1) * H, np.int32)
+    prob = np.zeros((W + 1) * H, np.float32)
+    s = _render_lib().orc_env_tables(_p(rgb), W, H, _p(alias), _p(prob))
+    return alias, prob, np.float32(s)
+
+
+def noise(W, H):
+    out = np.zeros(W * H * 2, np.float32)
+    _render_lib().orc_noise(W, H, _p(out))
+    return out
+
+
+def camera(angle, fov):
+    out = np.zeros(19, np.float32)
+    a = np.ascontiguousarray(angle, np.float32)
+    _render_lib().orc_camera(_p(a), float(min(max(fov, 0.1), 90.0)), _p(out))
+    return out
+
+
+def transc(op, a, b=None):
+    a = np.ascontiguousarray(a, np.float32)
+    out = np.empty_like(a)
+    bb = None if b is None else np.ascontiguousarray(b, np.float32)
+    _render_lib().orc_transc(op, _p(a), _p(bb), _p(out), a.size)
+    return out
+
+
+class OracleScene:
+    """The oracle's own flattening, BVH and tables for a SceneData; the Sobol
+    matrices are an input (checked against the reference table separately)."""
+
+    def __init__(self, data, sobol_matrices, params=None):
+        v, n, idx = data.flat()
+        self.v, self.n, self.idx = v, n, idx
+        self.bounds, self.hit, _ = bvh_build(v, idx)
+        self.mat_tex = np.ascontiguousarray(data.obj_mat_tex, np.int32)
+        self.materials = np.ascontiguousarray(data.materials, np.float32)
+        self.light_power, self.light_alias, self.light_prob, self.light_sum = light_tables(data)
+        self.sobol = np.ascontiguousarray(sobol_matrices, np.uint32)
+        W, H = data.film
+        self.noise = noise(W, H)
+        self.cam = camera(data.cam_angle, data.cam_fov)
+        s = OrcScene()
+        s.vertices, s.normals, s.indices, s.matTexIndex = _p(v), _p(n), _p(idx), _p(self.mat_tex)
+        s.nTriangles = idx.size // 3
+        s.objPrimCount = data.obj_indices.size // 3
+        s.bounds, s.hitTable, s.bvhSize = _p(self.bounds), _p(self.hit), self.bounds.shape[0]
+        s.materials = _p(self.materials)
+        s.nLightTriangles = data.light_indices.size // 3
+        s.lightPower, s.lightAlias, s.lightProb = _p(self.light_power), _p(self.light_alias), _p(self.light_prob)
+        s.lightSum = float(self.light_sum)
+        if data.env_rgb is not None:
+            rgb = np.ascontiguousarray(data.env_rgb, np.float32)
+            self.env_texels = rgb.astype(np.float16).astype(np.float32).reshape(-1)
+            self.env_alias, self.env_prob, esum = env_tables(rgb)
+            s.envTexels, s.envAlias, s.envProb = _p(self.env_texels), _p(self.env_alias), _p(self.env_prob)
+            s.envHeight, s.envWidth = rgb.shape[0], rgb.shape[1]
+            s.envSum = float(np.float32(int(esum)))
+        else:
+            s.envTexels = None
+            s.envSum = 0.0
+        s.envRotation = data.env_rotation
+        s.sobolMatrices, s.noise, s.sampler = _p(self.sobol), _p(self.noise), data.sampler
+        c = self.cam
+        s.camF = (C.c_float * 3)(*c[0:3])
+        s.camR = (C.c_float * 3)(*c[3:6])
+        s.camU = (C.c_float * 3)(*c[6:9])
+        s.camMatInv = (C.c_float * 9)(*c[9:18])
+        s.tanFOV = float(c[18])
+        s.camPos = (C.c_float * 3)(*data.cam_pos)
+        s.lensRadius, s.focalDist = data.cam_lens_radius, data.cam_focal_dist
+        s.filmW, s.filmH = W, H
+        s.camAsp = float(np.float32(W) / np.float32(H))
+        p = params or {}
+        s.maxDepth = p.get("max_depth", 4)
+        s.russianRoulette = p.get("russian_roulette", 0)
+        s.sampleLight = p.get("sample_light", 1)
+        s.lightEnvUniformSample = p.get("light_env_uniform_sample", 0)
+        s.lightPortion = p.get("light_portion", 0.5)
+        s.rrStartDepth = p.get("rr_start_depth", 1)
+        self.s = s
+
+    def render_pt(self, pixels, passes, spp0=0, fc0=1, nthreads=None):
+        """Sum of `passes` progressive passes for the pixel indices (y * W + x)."""
+        pix = np.ascontiguousarray(pixels, np.int32)
+        out = np.zeros((pix.size, 3), np.float32)
+        _render_lib().orc_render_pt(C.byref(self.s), spp0, passes, fc0, _p(pix), pix.size, _p(out),
+                                    nthreads or threads())
+        return out

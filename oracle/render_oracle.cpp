@@ -1,0 +1,1040 @@
+// render_oracle.cpp — CPU oracle of the ZillumGL MIS path tracer and the
+// sampling tables it reads.
+//
+// TEST INFRASTRUCTURE ONLY: the checker of the CUDA integrators.  Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
+//
+// Parity: the shaders restated here (src/shader/{math,random,microfacet,
+// material,material_loader,intersection,light,camera,path_integ_naive}.glsl)
+// need OpenGL 4.5, unavailable on this machine, so the oracle is a line-by-line
+// float32 restatement — PARITY UNPINNED at the shader level.  The host tables
+// follow src/core/{Scene,EnvironmentMap,Sampler,Camera}.cpp; the light alias
+// table is pinned against src/math/AliasTable.h compiled from the reference
+// tree (tests), the Sobol matrices against src/math/SobolMatrices256x32.h.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <utility>
+#include <vector>
+
+#include "oracle_math.h"
+#include "oracle_transc.h"
+
+using namespace orc;
+
+extern "C" {
+
+// Flattened scene in the reference's buffer layout (Scene.cpp:245-263).
+struct OrcScene {
+    // geometry: objects first, then light triangles (Scene.cpp:148-195)
+    const float* vertices;      // nv*3
+    const float* normals;       // nv*3
+    const uint32_t* indices;    // ntri*3
+    const int32_t* matTexIndex; // objPrimCount: (tex << 16) | mat
+    int64_t nTriangles;
+    int32_t objPrimCount;
+    // BVH in PackedBVH layout
+    const float* bounds;        // M*6
+    const int32_t* hitTable;    // 6*M*3
+    int64_t bvhSize;
+    // materials: 16 floats each (Material.h:32-53), slot 13 = type (int bits)
+    const float* materials;
+    // lights
+    int32_t nLightTriangles;
+    const float* lightPower;    // nL*3
+    const int32_t* lightAlias;
+    const float* lightProb;
+    float lightSum;
+    // environment map (texels already RGB16F-quantized, row-major, 3 floats)
+    const float* envTexels;     // may be NULL (black environment)
+    int32_t envWidth, envHeight;
+    const int32_t* envAlias;    // (W+1)*H
+    const float* envProb;       // (W+1)*H
+    float envSum;               // int-truncated (EnvironmentMap.h:22)
+    float envRotation;
+    // sampler
+    const uint32_t* sobolMatrices;  // 256*32
+    const float* noise;             // filmW*filmH*2
+    int32_t sampler;                // 0 independent, 1 sobol
+    // camera uniforms (NaivePath.cpp:49-60)
+    float camF[3], camR[3], camU[3], camPos[3];
+    float camMatInv[9];  // column-major mat3
+    float tanFOV, lensRadius, focalDist, camAsp;
+    int32_t filmW, filmH;
+    // integrator parameters (PathIntegParam, Integrator.h:56-66)
+    int32_t maxDepth;
+    int32_t russianRoulette;
+    int32_t sampleLight;
+    int32_t lightEnvUniformSample;
+    float lightPortion;
+    int32_t rrStartDepth;  // Russian roulette from this bounce on (1 = the reference)
+};
+
+}  // extern "C"
+
+namespace {
+
+const float Pi = 3.14159265358979323846f;
+const float PiInv = 1.0f / Pi;
+
+inline float satDot(vec3 a, vec3 b) { return fmax_(dot(a, b), 0.0f); }
+inline float absDot(vec3 a, vec3 b) { return std::fabs(dot(a, b)); }
+inline float square(float x) { return x * x; }
+inline float distSquare(vec3 x, vec3 y) { return dot(x - y, x - y); }
+inline float luminance(vec3 c) { return dot(c, vec3(0.299f, 0.587f, 0.114f)); }
+inline bool isBlack(vec3 c) { return luminance(c) < 1e-5f; }
+inline bool hasNan(vec3 c) { return std::isnan(c.x) || std::isnan(c.y) || std::isnan(c.z); }
+inline float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+inline vec3 mix3(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }
+inline vec3 mix3(vec3 x, vec3 y, vec3 a) { return x * (vec3(1.0f) - a) + y * a; }
+inline float maxComponent(vec3 v) { return fmax_(v.x, fmax_(v.y, v.z)); }
+inline float pow5(float x) {
+    float x2 = x * x;
+    return x2 * x2 * x;
+}
+inline vec3 reflect(vec3 I, vec3 N) { return I - (2.0f * dot(N, I)) * N; }
+
+// ---------------------------------------------------------------- random.glsl
+struct Rng {
+    uint32_t randSeed;
+    uint32_t sampleSeed;
+    int sampleOffset;
+};
+
+inline uint32_t hash(uint32_t seed) {  // random.glsl:5-13
+    seed = (seed ^ 61u) ^ (seed >> 16u);
+    seed *= 9u;
+    seed = seed ^ (seed >> 4u);
+    seed *= 0x27d4eb2du;
+    seed = seed ^ (seed >> 15u);
+    return seed;
+}
+
+inline float rand01(Rng& g) {  // random.glsl:15-19
+    g.randSeed = hash(g.randSeed);
+    return (float)g.randSeed * (1.0f / 4294967296.0f);
+}
+
+// Sampler::sobolSample (Sampler.cpp:19-28): XOR of the generator-matrix
+// columns selected by the bits of the sample index.
+inline uint32_t sobolSample(const uint32_t* m, uint32_t index, int dim) {
+    uint32_t r = 0;
+    for (int i = dim * 32; index != 0; index >>= 1, i++)
+        if (index & 1u) r ^= m[i];
+    return r;
+}
+
+struct SamplerCtx {
+    const OrcScene* sc;
+};
+
+inline float sample1D(const OrcScene& sc, Rng& g, int& s) {  // random.glsl:61-70
+    if (sc.sampler == 0) return rand01(g);
+    // texelFetch(uSobolSeq, sampleOffset + s): row = index / 256, dim = index % 256
+    uint32_t idx = (uint32_t)g.sampleOffset + (uint32_t)s;
+    uint32_t r = sobolSample(sc.sobolMatrices, idx / 256u, (int)(idx % 256u));
+    r ^= g.sampleSeed;
+    g.sampleSeed = hash(g.sampleSeed);
+    s++;
+    return (float)r / 4294967296.0f;
+}
+
+// --------------------------------------------------------------- math.glsl
+inline vec2 toConcentricDisk(vec2 v) {  // math.glsl:25-41
+    if (v.x == 0.0f && v.y == 0.0f) return vec2(0.0f, 0.0f);
+    v = v * 2.0f - 1.0f;
+    float phi, r;
+    if (v.x * v.x > v.y * v.y) {
+        r = v.x;
+        phi = Pi * v.y / v.x * 0.25f;
+    } else {
+        r = v.y;
+        phi = Pi * 0.5f - Pi * v.x / v.y * 0.25f;
+    }
+    return vec2(r * zcos(phi), r * zsin(phi));
+}
+
+struct mat3 {
+    vec3 c0, c1, c2;  // columns
+};
+inline vec3 mul(const mat3& m, vec3 v) {
+    return vec3(m.c0.x * v.x + m.c1.x * v.y + m.c2.x * v.z, m.c0.y * v.x + m.c1.y * v.y + m.c2.y * v.z,
+                m.c0.z * v.x + m.c1.z * v.y + m.c2.z * v.z);
+}
+// inverse(mat3) by cofactors: inv = adj(m) / det(m), det expanded along the
+// first column.
+inline mat3 inverse(const mat3& m) {
+    float a00 = m.c0.x, a01 = m.c1.x, a02 = m.c2.x;  // row 0
+    float a10 = m.c0.y, a11 = m.c1.y, a12 = m.c2.y;  // row 1
+    float a20 = m.c0.z, a21 = m.c1.z, a22 = m.c2.z;  // row 2
+    float C00 = a11 * a22 - a12 * a21;
+    float C10 = a02 * a21 - a01 * a22;
+    float C20 = a01 * a12 - a02 * a11;
+    float det = a00 * C00 + a10 * C10 + a20 * C20;
+    float id = 1.0f / det;
+    // rows of the inverse
+    float i00 = C00 * id, i01 = C10 * id, i02 = C20 * id;
+    float i10 = (a12 * a20 - a10 * a22) * id, i11 = (a00 * a22 - a02 * a20) * id, i12 = (a02 * a10 - a00 * a12) * id;
+    float i20 = (a10 * a21 - a11 * a20) * id, i21 = (a01 * a20 - a00 * a21) * id, i22 = (a00 * a11 - a01 * a10) * id;
+    return mat3{vec3(i00, i10, i20), vec3(i01, i11, i21), vec3(i02, i12, i22)};
+}
+
+inline vec3 getTangent(vec3 n) { return (std::fabs(n.z) > 0.999f) ? vec3(0.0f, 1.0f, 0.0f) : vec3(0.0f, 0.0f, 1.0f); }
+inline mat3 tbnMatrix(vec3 n) {  // math.glsl:78-84
+    vec3 t = getTangent(n);
+    vec3 b = normalize(cross(n, t));
+    t = cross(b, n);
+    return mat3{t, b, n};
+}
+inline vec3 normalToWorld(vec3 n, vec3 v) { return normalize(mul(tbnMatrix(n), v)); }
+
+struct vec4r {
+    vec3 v;
+    float w;
+};
+inline vec4r sampleCosineWeighted(vec3 n, vec2 u) {  // math.glsl:99-105
+    vec2 uv = toConcentricDisk(u);
+    float z = std::sqrt(1.0f - dot(uv, uv));
+    vec3 v = normalToWorld(n, vec3(uv.x, uv.y, z));
+    return vec4r{v, PiInv * z};
+}
+inline bool sameHemisphere(vec3 n, vec3 a, vec3 b) { return dot(n, a) * dot(n, b) > 0.0f; }
+
+inline vec3 sampleTriangleUniform(vec3 va, vec3 vb, vec3 vc, vec2 uv) {  // math.glsl:139-145
+    float r = std::sqrt(uv.y);
+    float u = 1.0f - r;
+    float v = uv.x * r;
+    return va * (1.0f - u - v) + vb * u + vc * v;
+}
+inline float triangleArea(vec3 va, vec3 vb, vec3 vc) { return 0.5f * length(cross(vc - va, vb - va)); }
+inline vec3 rotateZ(vec3 v, float angle) {
+    float c = zcos(angle), s = zsin(angle);
+    return vec3(v.x * c - v.y * s, v.x * s + v.y * c, v.z);
+}
+inline vec2 sphereToPlane(vec3 uv) {  // math.glsl:58-64
+    float theta = zatan2(uv.y, uv.x);
+    if (theta < 0.0f) theta += Pi * 2.0f;
+    float phi = zatan2(length(vec2(uv.x, uv.y)), uv.z);
+    return vec2(theta * PiInv * 0.5f, phi * PiInv);
+}
+inline vec3 planeToSphere(vec2 uv) {  // math.glsl:66-71
+    float theta = uv.x * Pi * 2.0f;
+    float phi = uv.y * Pi;
+    return vec3(zcos(theta) * zsin(phi), zsin(theta) * zsin(phi), zcos(phi));
+}
+inline float biHeuristic(float f, float g) { return f * f / (f * f + g * g); }
+
+// --------------------------------------------------------- microfacet.glsl
+inline float schlickW(float c) { return pow5(1.0f - c); }
+inline vec3 schlickF(float c, vec3 F0) { return F0 + (vec3(1.0f) - F0) * pow5(1.0f - c); }
+inline float schlickG(float c, float alpha) {
+    float k = alpha * 0.5f;
+    return c / (c * (1.0f - k) + k);
+}
+inline float smithG(vec3 n, vec3 wo, vec3 wi, float alpha) {
+    return schlickG(absDot(n, wo), alpha) * schlickG(absDot(n, wi), alpha);
+}
+inline float ggx(float c, float alpha) {  // microfacet.glsl:30-40
+    if (c < 1e-6f) return 0.0f;
+    float a2 = alpha * alpha;
+    float nom = a2;
+    float denom = c * c * (a2 - 1.0f) + 1.0f;
+    denom = denom * denom * Pi;
+    return nom / denom;
+}
+inline float ggxD(vec3 n, vec3 m, float alpha) { return ggx(dot(n, m), alpha); }
+inline float ggxPdfVisibleWm(vec3 n, vec3 m, vec3 wo, float alpha) {
+    return ggx(dot(n, m), alpha) * schlickG(dot(n, wo), alpha) * absDot(m, wo) / absDot(n, wo);
+}
+inline vec3 ggxSampleVisibleWm(vec3 n, vec3 wo, float alpha, vec2 u) {  // microfacet.glsl:74-92
+    mat3 tbn = tbnMatrix(n);
+    mat3 tbnInv = inverse(tbn);
+    vec3 vh = normalize(mul(tbnInv, wo) * vec3(alpha, alpha, 1.0f));
+    float lensq = vh.x * vh.x + vh.y * vh.y;
+    vec3 t1 = lensq > 0.0f ? vec3(-vh.y, vh.x, 0.0f) / std::sqrt(lensq) : vec3(1.0f, 0.0f, 0.0f);
+    vec3 t2 = cross(vh, t1);
+    vec2 xi = toConcentricDisk(u);
+    float s = 0.5f * (1.0f + vh.z);
+    xi.y = (1.0f - s) * std::sqrt(1.0f - xi.x * xi.x) + s * xi.y;
+    vec3 h = t1 * xi.x + t2 * xi.y + vh * std::sqrt(fmax_(0.0f, 1.0f - xi.x * xi.x - xi.y * xi.y));
+    h = normalize(vec3(h.x * alpha, h.y * alpha, fmax_(0.0f, h.z)));
+    return normalToWorld(n, h);
+}
+inline float gtr1(float c, float alpha) {  // microfacet.glsl:94-98
+    float a2 = alpha * alpha;
+    return (a2 - 1.0f) / (2.0f * Pi * zlog(alpha) * (1.0f + (a2 - 1.0f) * c * c));
+}
+inline float gtr1D(vec3 n, vec3 m, float alpha) { return gtr1(satDot(n, m), alpha); }
+inline vec3 gtr1SampleWm(vec3 n, vec3 wo, float alpha, vec2 u) {  // microfacet.glsl:105-115
+    float cosTheta = std::sqrt(fmax_(0.0f, (1.0f - zpow(alpha, 1.0f - u.x)) / (1.0f - alpha)));
+    float sinTheta = std::sqrt(fmax_(0.0f, 1.0f - cosTheta * cosTheta));
+    float phi = 2.0f * u.y * Pi;
+    vec3 m = normalize(vec3(zcos(phi) * sinTheta, zsin(phi) * sinTheta, cosTheta));
+    if (!sameHemisphere(n, wo, m)) m = -m;
+    return normalize(normalToWorld(n, m));
+}
+inline float gtr1PdfWm(vec3 n, vec3 m, vec3 wo, float alpha) { return gtr1D(n, m, alpha) * absDot(n, m); }
+
+// ----------------------------------------------------------- material.glsl
+enum : uint32_t { Diffuse = 1u << 0, GlosRefl = 1u << 1, GlosTrans = 1u << 2, SpecRefl = 1u << 3,
+                  SpecTrans = 1u << 4, Invalid = 1u << 16 };
+enum : uint32_t { Lambertian = 0, PrincipledBRDF = 1, MetalWorkflow = 2, Dielectric = 3, ThinDielectric = 4 };
+
+struct BSDFParam {
+    vec3 baseColor;
+    float subsurface = 0, metallic = 0, roughness = 0, specular = 0, specularTint = 0;
+    float sheen = 0, sheenTint = 0, clearcoat = 0, clearcoatGloss = 0, ior = 0;
+};
+struct BSDFSample {
+    vec3 wi;
+    float pdf;
+    vec3 bsdf;
+    float eta;
+    uint32_t flag;
+};
+inline BSDFSample invalidSample() { return BSDFSample{vec3(0.0f), 0.0f, vec3(0.0f), 0.0f, Invalid}; }
+
+inline vec3 lambertian(const BSDFParam& p) { return p.baseColor * PiInv; }
+inline float lambertianPdf(vec3 wi, vec3 n) { return satDot(wi, n) * PiInv; }
+inline BSDFSample lambertianSample(vec3 n, const BSDFParam& p, vec3 u) {  // material.glsl:78-83
+    vec3 wi = sampleCosineWeighted(n, vec2(u.y, u.z)).v;
+    float pdf = satDot(n, wi) * PiInv;
+    return BSDFSample{wi, pdf, p.baseColor * PiInv, 1.0f, Diffuse};
+}
+
+inline vec3 principledMetal(vec3 wo, vec3 wi, vec3 n, vec3 fm0, float alpha) {  // :357-373
+    float cosWo = satDot(n, wo);
+    float cosWi = satDot(n, wi);
+    vec3 h = normalize(wo + wi);
+    if (cosWo < 1e-10f || cosWi < 1e-10f) return vec3(0.0f);
+    vec3 fm = schlickF(absDot(h, wo), fm0);
+    float dm = ggxD(n, h, alpha);
+    float gm = smithG(n, wo, wi, alpha);
+    float denom = 4.0f * cosWi * cosWo;
+    if (denom < 1e-7f) return vec3(0.0f);
+    return fm * dm * gm / denom;
+}
+inline float principledMetalPdf(vec3 wo, vec3 wi, vec3 n, float alpha) {
+    vec3 h = normalize(wo + wi);
+    return ggxPdfVisibleWm(n, h, wo, alpha) / (4.0f * absDot(h, wo));
+}
+inline vec3 principledClearcoat(vec3 wo, vec3 wi, vec3 n, vec3 baseColor, float alpha) {  // :393-409
+    float cosWo = satDot(n, wo);
+    float cosWi = satDot(n, wi);
+    vec3 h = normalize(wo + wi);
+    if (cosWo < 1e-6f || cosWi < 1e-6f) return vec3(0.0f);
+    vec3 fc = schlickF(absDot(h, wo), baseColor);
+    float dc = gtr1D(n, h, alpha);
+    float gc = smithG(n, wo, wi, 0.25f);
+    float denom = 4.0f * cosWi * cosWo;
+    if (denom < 1e-7f) return vec3(0.0f);
+    return fc * dc * gc / denom;
+}
+inline float principledClearcoatPdf(vec3 wo, vec3 wi, vec3 n, float alpha) {
+    vec3 h = normalize(wo + wi);
+    return gtr1PdfWm(n, h, wo, alpha) / (4.0f * absDot(h, wo));
+}
+inline vec3 principledDiffuse(vec3 wo, vec3 wi, vec3 n, vec3 baseColor, float subsurface, float roughness) {
+    float cosWo = satDot(n, wo);  // :429-452
+    float cosWi = satDot(n, wi);
+    if (cosWo < 1e-10f || cosWi < 1e-10f) return vec3(0.0f);
+    vec3 h = normalize(wo + wi);
+    float hCosWi = dot(h, wi);
+    float hCosWi2 = hCosWi * hCosWi;
+    float fi = schlickW(cosWi);
+    float fo = schlickW(cosWo);
+    vec3 fd90 = vec3(0.5f + 2.0f * roughness * hCosWi2);
+    vec3 fd = mix3(vec3(1.0f), fd90, fi) * mix3(vec3(1.0f), fd90, fo);
+    vec3 baseDiffuse = baseColor * fd * PiInv;
+    vec3 fss90 = vec3(roughness * hCosWi2);
+    vec3 fss = mix3(vec3(1.0f), fss90, fi) * mix3(vec3(1.0f), fss90, fo);
+    vec3 ss = baseColor * PiInv * 1.25f * (fss * (1.0f / (cosWi + cosWo) - 0.5f) + vec3(0.5f));
+    return mix3(baseDiffuse, ss, subsurface);
+}
+
+inline void principledCommon(const BSDFParam& p, float& alpha, float& clearcoatAlpha, vec3& tintColor, vec3& fm0) {
+    alpha = square(p.roughness);
+    clearcoatAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
+    float lum = luminance(p.baseColor);
+    tintColor = lum > 0.0f ? p.baseColor / lum : vec3(1.0f);
+    fm0 = mix3(0.08f * p.specular * mix3(vec3(1.0f), tintColor, p.specularTint), p.baseColor, p.metallic);
+}
+
+inline vec3 principledBRDF(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p) {  // :462-490
+    vec3 res(0.0f);
+    float alpha, ccAlpha;
+    vec3 tint, fm0;
+    principledCommon(p, alpha, ccAlpha, tint, fm0);
+    float hCosWi = dot(normalize(wo + wi), wi);
+    res = res + principledDiffuse(wo, wi, n, p.baseColor, p.subsurface, p.roughness) * (1.0f - p.metallic);
+    res = res + principledMetal(wo, wi, n, fm0, alpha);
+    res = res + principledClearcoat(wo, wi, n, p.baseColor, ccAlpha) * p.clearcoat * 0.25f;
+    res = res + mix3(vec3(1.0f), tint, p.sheenTint) * schlickW(hCosWi) * p.sheen * (dot(n, wi) < 0.0f ? 0.0f : 1.0f);
+    return res;
+}
+inline float principledBRDFPdf(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p) {  // :492-514
+    float pdf = 0.0f;
+    float alpha = square(p.roughness);
+    float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
+    float spec = 1.0f / (2.0f - p.metallic);
+    float cosinePdf = absDot(n, wi) * PiInv;
+    pdf += cosinePdf * (1.0f - spec);
+    pdf += principledMetalPdf(wo, wi, n, alpha) * spec;
+    pdf += principledClearcoatPdf(wo, wi, n, ccAlpha) * 0.25f * p.clearcoat;
+    return pdf / (1.0f + 0.25f * p.clearcoat);
+}
+inline BSDFSample principledBRDFSample(vec3 n, vec3 wo, const BSDFParam& p, vec3 u, Rng& g) {  // :516-555
+    float alpha = square(p.roughness);
+    float spec = 1.0f / (2.0f - p.metallic);
+    float cdf0 = 1.0f - spec, cdf1 = 1.0f, cdf2 = 1.0f + p.clearcoat * 0.25f;
+    vec3 wi;
+    float s = rand01(g) * cdf2;
+    if (s <= cdf0) {
+        wi = sampleCosineWeighted(n, vec2(u.y, u.z)).v;  // principledDiffuseSample: .wi only
+    } else if (s <= cdf1) {
+        float lum = luminance(p.baseColor);
+        vec3 tint = lum > 0.0f ? p.baseColor / lum : vec3(1.0f);
+        vec3 fm0 = mix3(0.08f * p.specular * mix3(vec3(1.0f), tint, p.specularTint), p.baseColor, p.metallic);
+        (void)fm0;
+        // principledMetalSample(...).wi: InvalidBSDFSample has wi = 0
+        vec3 h = ggxSampleVisibleWm(n, wo, alpha, vec2(u.y, u.z));
+        vec3 w = reflect(-wo, h);
+        wi = (dot(n, w) < 0.0f) ? vec3(0.0f) : w;
+    } else {
+        vec3 h = gtr1SampleWm(n, wo, alpha, vec2(u.y, u.z));  // base alpha, as the reference does
+        vec3 w = reflect(-wo, h);
+        wi = (dot(n, w) < 0.0f) ? vec3(0.0f) : w;
+    }
+    vec3 bsdf = principledBRDF(wo, wi, n, p);
+    float pdf = principledBRDFPdf(wo, wi, n, p);
+    return BSDFSample{wi, pdf, bsdf, 1.0f, Diffuse};
+}
+
+// ---------------------------------------------------- material_loader.glsl
+inline uint32_t loadMaterialType(const OrcScene& sc, int matId) {
+    int32_t t;
+    std::memcpy(&t, &sc.materials[16 * matId + 13], 4);
+    return (uint32_t)t;
+}
+inline BSDFParam loadMaterial(const OrcScene& sc, uint32_t type, int matId) {  // :81-97
+    const float* m = sc.materials + 16 * matId;
+    BSDFParam p;
+    p.baseColor = vec3(m[0], m[1], m[2]);
+    if (type == PrincipledBRDF) {
+        p.roughness = mixf(0.0134f, 1.0f, m[3]);
+        p.subsurface = m[4];
+        p.metallic = m[5];
+        p.specular = m[6];
+        p.specularTint = m[7];
+        p.sheen = m[8];
+        p.sheenTint = m[9];
+        p.clearcoat = m[10];
+        p.clearcoatGloss = m[11];
+    }
+    return p;
+}
+inline vec3 materialBSDF(uint32_t type, const BSDFParam& p, vec3 wo, vec3 wi, vec3 n) {
+    if (type == PrincipledBRDF) return principledBRDF(wo, wi, n, p);
+    return lambertian(p);
+}
+inline float materialPdf(uint32_t type, const BSDFParam& p, vec3 wo, vec3 wi, vec3 n) {
+    if (type == PrincipledBRDF) return principledBRDFPdf(wo, wi, n, p);
+    return lambertianPdf(wi, n);
+}
+inline BSDFSample materialSample(uint32_t type, const BSDFParam& p, vec3 n, vec3 wo, vec3 u, Rng& g) {
+    if (type == PrincipledBRDF) return principledBRDFSample(n, wo, p, u, g);
+    return lambertianSample(n, p, u);
+}
+
+// -------------------------------------------------------- intersection.glsl
+struct Ray {
+    vec3 ori, dir;
+};
+inline Ray rayOffseted(vec3 o, vec3 d) { return Ray{o + d * 1e-4f, d}; }
+inline vec3 rayPoint(const Ray& r, float t) { return r.ori + r.dir * t; }
+
+inline vec3 V(const OrcScene& sc, uint32_t i) { return vec3(sc.vertices[3 * i], sc.vertices[3 * i + 1], sc.vertices[3 * i + 2]); }
+inline vec3 N(const OrcScene& sc, uint32_t i) { return vec3(sc.normals[3 * i], sc.normals[3 * i + 1], sc.normals[3 * i + 2]); }
+
+struct SurfaceInfo {
+    vec3 ns, ng;
+};
+inline SurfaceInfo triangleSurfaceInfo(const OrcScene& sc, int id, vec3 p) {  // :188-224 (uv unused)
+    uint32_t ia = sc.indices[3 * id], ib = sc.indices[3 * id + 1], ic = sc.indices[3 * id + 2];
+    vec3 a = V(sc, ia), b = V(sc, ib), c = V(sc, ic);
+    vec3 na = N(sc, ia), nb = N(sc, ib), nc = N(sc, ic);
+    vec3 pa = a - p, pb = b - p, pc = c - p;
+    float areaInv = 1.0f / length(cross(b - a, c - a));
+    float la = length(cross(pb, pc)) * areaInv;
+    float lb = length(cross(pc, pa)) * areaInv;
+    float lc = 1.0f - la - lb;
+    SurfaceInfo s;
+    s.ns = normalize(na * la + nb * lb + nc * lc);
+    s.ng = normalize(cross(pa, pb));
+    if (dot(s.ns, s.ng) < 0.0f) s.ng = -s.ng;
+    return s;
+}
+inline float triangleArea(const OrcScene& sc, int id) {
+    return triangleArea(V(sc, sc.indices[3 * id]), V(sc, sc.indices[3 * id + 1]), V(sc, sc.indices[3 * id + 2]));
+}
+inline vec3 triangleSampleUniform(const OrcScene& sc, int id, vec2 u) {
+    return sampleTriangleUniform(V(sc, sc.indices[3 * id]), V(sc, sc.indices[3 * id + 1]), V(sc, sc.indices[3 * id + 2]), u);
+}
+
+}  // namespace
+
+// traversal from bvh_oracle.cpp
+extern "C" void orc_trace(const float*, const int32_t*, int64_t, const float*, const uint32_t*, const float*,
+                          const float*, const float*, int64_t, int32_t, int32_t*, float*, int32_t*, int32_t*, int32_t);
+
+namespace {
+
+inline int bvhHit(const OrcScene& sc, const Ray& r, float& dist) {
+    float o[3] = {r.ori.x, r.ori.y, r.ori.z}, d[3] = {r.dir.x, r.dir.y, r.dir.z};
+    int32_t id;
+    float t;
+    orc_trace(sc.bounds, sc.hitTable, sc.bvhSize, sc.vertices, sc.indices, o, d, nullptr, 1, 0, &id, &t, nullptr,
+              nullptr, 1);
+    dist = t;
+    return id;
+}
+inline bool bvhTest(const OrcScene& sc, const Ray& r, float dist) {
+    float o[3] = {r.ori.x, r.ori.y, r.ori.z}, d[3] = {r.dir.x, r.dir.y, r.dir.z};
+    int32_t occ;
+    orc_trace(sc.bounds, sc.hitTable, sc.bvhSize, sc.vertices, sc.indices, o, d, &dist, 1, 1, &occ, nullptr, nullptr,
+              nullptr, 1);
+    return occ != 0;
+}
+
+// ---------------------------------------------------------------- light.glsl
+struct LightLiSample {
+    vec3 wi, coef;
+    float pdf;
+};
+inline LightLiSample invalidLi() { return LightLiSample{vec3(0.0f), vec3(0.0f), 0.0f}; }
+
+inline vec3 lightPowerOf(const OrcScene& sc, int id) {
+    return vec3(sc.lightPower[3 * id], sc.lightPower[3 * id + 1], sc.lightPower[3 * id + 2]);
+}
+inline int lightSampleOne(const OrcScene& sc, vec2 u) {  // light.glsl:68-72
+    // u.x can round to exactly 1.0 (random.glsl:69); the reference then reads
+    // one entry past the table, the build clamps to the last entry.
+    int cx = std::min(f2i((float)sc.nLightTriangles * u.x), sc.nLightTriangles - 1);
+    return (u.y < sc.lightProb[cx]) ? cx : sc.lightAlias[cx];
+}
+inline float lightPdfSampleOne(const OrcScene& sc, int id) { return luminance(lightPowerOf(sc, id)) / sc.lightSum; }
+inline vec3 lightLe(const OrcScene& sc, int id, vec3 x, vec3 wo) {  // :79-86
+    int triId = id + sc.objPrimCount;
+    SurfaceInfo s = triangleSurfaceInfo(sc, triId, x);
+    if (dot(wo, s.ng) <= 0.0f) return vec3(0.0f);
+    return lightPowerOf(sc, id) / triangleArea(sc, triId) * 0.5f * PiInv;
+}
+inline float lightPdfLi(const OrcScene& sc, int id, vec3 x, vec3 y) {  // :88-98
+    int triId = id + sc.objPrimCount;
+    vec3 norm = triangleSurfaceInfo(sc, triId, y).ng;
+    vec3 yx = normalize(x - y);
+    float cosTheta = absDot(norm, yx);
+    if (cosTheta < 1e-8f) return -1.0f;
+    return distSquare(x, y) / (triangleArea(sc, triId) * cosTheta);
+}
+inline LightLiSample lightSampleLi(const OrcScene& sc, int id, vec3 x, vec2 u) {  // :122-155
+    int triId = id + sc.objPrimCount;
+    vec3 a = V(sc, sc.indices[3 * triId]), b = V(sc, sc.indices[3 * triId + 1]), c = V(sc, sc.indices[3 * triId + 2]);
+    vec3 y = sampleTriangleUniform(a, b, c, u);
+    vec3 wi = normalize(y - x);
+    vec3 norm = triangleSurfaceInfo(sc, triId, y).ng;
+    float cosTheta = dot(norm, -wi);
+    if (cosTheta < 1e-6f) return invalidLi();
+    Ray lightRay = rayOffseted(x, wi);
+    float dist = distance(x, y);
+    float pdf = dist * dist / (triangleArea(a, b, c) * cosTheta);
+    float testDist = dist - 1e-4f - 1e-6f;
+    if (bvhTest(sc, lightRay, testDist) || pdf < 1e-8f) return invalidLi();
+    vec3 weight = lightLe(sc, id, y, -wi);
+    float pdfSample = luminance(lightPowerOf(sc, id)) / sc.lightSum;
+    pdf *= pdfSample;
+    return LightLiSample{wi, weight / pdf, pdf};
+}
+
+// Env texture: RGB16F texels, bilinear with repeat wrap at GL texel centres.
+inline vec3 envTexel(const OrcScene& sc, int x, int y) {
+    int W = sc.envWidth, H = sc.envHeight;
+    x %= W;
+    if (x < 0) x += W;
+    y %= H;
+    if (y < 0) y += H;
+    const float* t = sc.envTexels + 3 * ((size_t)y * W + x);
+    return vec3(t[0], t[1], t[2]);
+}
+inline vec3 envTexture(const OrcScene& sc, vec2 st) {
+    float u = st.x * (float)sc.envWidth - 0.5f;
+    float v = st.y * (float)sc.envHeight - 0.5f;
+    float fu = std::floor(u), fv = std::floor(v);
+    float au = u - fu, av = v - fv;
+    int x0 = f2i(fu), y0 = f2i(fv);
+    vec3 t00 = envTexel(sc, x0, y0), t10 = envTexel(sc, x0 + 1, y0);
+    vec3 t01 = envTexel(sc, x0, y0 + 1), t11 = envTexel(sc, x0 + 1, y0 + 1);
+    return mix3(mix3(t00, t10, au), mix3(t01, t11, au), av);
+}
+inline vec3 envLe(const OrcScene& sc, vec3 wi) {  // light.glsl:163-167
+    if (!sc.envTexels) return vec3(0.0f);
+    wi = rotateZ(wi, -sc.envRotation);
+    return envTexture(sc, sphereToPlane(wi));
+}
+inline float envGetPortion(const OrcScene& sc, vec3 wi) { return luminance(envLe(sc, wi)) / sc.envSum; }
+inline float envPdfLi(const OrcScene& sc, vec3 wi) {  // :174-179
+    if (sc.envSum == 0.0f) return 0.0f;
+    return envGetPortion(sc, wi) * (float)sc.envWidth * (float)sc.envHeight * 0.5f * square(PiInv);
+}
+struct EnvWi {
+    vec3 wi;
+    float pdf;
+};
+inline EnvWi envSampleWi(const OrcScene& sc, float ux, float uy, float uz, float uw) {  // :181-205
+    int w = sc.envWidth, h = sc.envHeight;
+    int rx = std::min(f2i((float)h * ux), h - 1);  // clamped like lightSampleOne
+    int rIdx = rx * (w + 1) + w;
+    int row = (uy < sc.envProb[rIdx]) ? rx : sc.envAlias[rIdx];
+    int cx = std::min(f2i((float)w * uz), w - 1);
+    int cIdx = row * (w + 1) + cx;
+    int col = (uw < sc.envProb[cIdx]) ? cx : sc.envAlias[cIdx];
+    vec2 uv = vec2((float)col + 0.5f, (float)row + 0.5f) / vec2((float)w, (float)h);
+    vec3 wi = planeToSphere(uv);
+    wi = rotateZ(wi, sc.envRotation);
+    float pdf = envGetPortion(sc, wi) * (float)w * (float)h * 0.5f * square(PiInv);
+    return EnvWi{wi, pdf};
+}
+inline LightLiSample envSampleLi(const OrcScene& sc, vec3 x, float ux, float uy, float uz, float uw) {
+    if (!sc.envTexels) return invalidLi();  // black environment: nothing to sample
+    EnvWi sp = envSampleWi(sc, ux, uy, uz, uw);
+    Ray ray = rayOffseted(x, sp.wi);
+    if (bvhTest(sc, ray, 1e8f) || sp.pdf == 0.0f) return invalidLi();
+    return LightLiSample{sp.wi, envLe(sc, sp.wi) / sp.pdf, sp.pdf};
+}
+inline LightLiSample sampleLightAndEnv(const OrcScene& sc, vec3 x, float ud, float u0, float u1, float u2, float u3) {
+    float pdfSampleLight = 0.0f;  // light.glsl:221-235
+    if (sc.nLightTriangles > 0)
+        pdfSampleLight = sc.lightEnvUniformSample ? sc.lightPortion : sc.lightSum / (sc.lightSum + sc.envSum);
+    bool sampleLight = ud < pdfSampleLight;
+    float pdfSelect = sampleLight ? pdfSampleLight : 1.0f - pdfSampleLight;
+    LightLiSample s;
+    if (sampleLight) {
+        int id = lightSampleOne(sc, vec2(u0, u1));
+        s = lightSampleLi(sc, id, x, vec2(u2, u3));
+    } else {
+        s = envSampleLi(sc, x, u0, u1, u2, u3);
+    }
+    s.coef = s.coef / pdfSelect;
+    s.pdf *= pdfSelect;
+    return s;
+}
+inline float pdfSelectLight(const OrcScene& sc, int id) {
+    float fst = luminance(lightPowerOf(sc, id)) / sc.lightSum;
+    float snd = sc.lightEnvUniformSample ? sc.lightPortion : sc.lightSum / (sc.lightSum + sc.envSum);
+    return fst * snd;
+}
+inline float pdfSelectEnv(const OrcScene& sc) {
+    return sc.lightEnvUniformSample ? (1.0f - sc.lightPortion) : sc.envSum / (sc.lightSum + sc.envSum);
+}
+
+// --------------------------------------------------------------- camera.glsl
+inline vec3 cv(const float* p) { return vec3(p[0], p[1], p[2]); }
+inline Ray thinLensCameraSampleRay(const OrcScene& sc, vec2 uv, float u0, float u1, float u2, float u3) {
+    vec2 texelSize = vec2(1.0f) / vec2((float)sc.filmW, (float)sc.filmH);  // camera.glsl:62-77
+    vec2 biased = uv + texelSize * vec2(u0, u1);
+    vec2 ndc = biased * 2.0f - 1.0f;
+    vec2 lens = toConcentricDisk(vec2(u2, u3)) * sc.lensRadius;
+    vec3 pLens(lens.x, lens.y, 0.0f);
+    vec2 fp = ndc * vec2(sc.camAsp, 1.0f) * sc.focalDist * sc.tanFOV;
+    vec3 pFocus(fp.x, fp.y, sc.focalDist);
+    vec3 dir = pFocus - pLens;
+    dir = normalize(cv(sc.camR) * dir.x + cv(sc.camU) * dir.y + cv(sc.camF) * dir.z);
+    return Ray{cv(sc.camPos) + cv(sc.camR) * pLens.x + cv(sc.camU) * pLens.y, dir};
+}
+
+// ------------------------------------------------------ path_integ_naive.glsl
+vec3 pathIntegTrace(const OrcScene& sc, Ray ray, int& s, Rng& g) {  // :35-143
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    vec3 pos = rayPoint(ray, primDist);
+    if (id == -1) return envLe(sc, ray.dir);
+    if (id - sc.objPrimCount >= 0) return lightLe(sc, id - sc.objPrimCount, pos, -ray.dir);
+    vec3 wo = -ray.dir;
+    vec3 result(0.0f), throughput(1.0f);
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        SurfaceInfo surf = triangleSurfaceInfo(sc, id, pos);
+        int matTexId = sc.matTexIndex[id];
+        int matId = matTexId & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != Dielectric && matType != ThinDielectric) {
+            if (dot(surf.ns, wo) < 0.0f) {
+                surf.ns = -surf.ns;
+                surf.ng = -surf.ng;
+            }
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        if (sc.sampleLight) {
+            float ud = sample1D(sc, g, s);
+            float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
+            LightLiSample ls = sampleLightAndEnv(sc, pos, ud, u0, u1, u2, u3);
+            if (ls.pdf > 0.0f) {
+                vec3 f = materialBSDF(matType, mp, wo, ls.wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                float weight = biHeuristic(ls.pdf, fpdf);
+                result = result + f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+            }
+        }
+        float b0 = sample1D(sc, g, s), b1 = sample1D(sc, g, s), b2 = sample1D(sc, g, s);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        vec3 bsdf = bs.bsdf;
+        uint32_t flag = bs.flag;
+        bool deltaBsdf = (flag == SpecRefl || flag == SpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        throughput = throughput * (bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        ray = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, ray, dist);
+        int lightId = nextId - sc.objPrimCount;
+        vec3 nextPos = rayPoint(ray, dist);
+        if (nextId == -1) {
+            vec3 radiance = envLe(sc, wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float envPdf = envPdfLi(sc, wi) * pdfSelectEnv(sc);
+                weight = (envPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, envPdf);
+            }
+            result = result + radiance * throughput * weight;
+            break;
+        } else if (lightId >= 0) {
+            vec3 radiance = lightLe(sc, lightId, nextPos, -wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, lightId);
+                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
+            }
+            result = result + radiance * throughput * weight;
+            break;
+        }
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bsdf / bsdfPdf), 0.95f);
+            if (sample1D(sc, g, s) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        id = nextId;
+        pos = nextPos;
+        wo = -wi;
+    }
+    return result;
+}
+
+// Per-pixel seeds: noise = tex(noise, tex(noise, coord / size)) with bilinear
+// filtering and repeat wrap at GL texel centres (path_integ_naive.glsl:156-160).
+inline vec2 noiseTexel(const OrcScene& sc, int x, int y) {
+    int W = sc.filmW, H = sc.filmH;
+    x %= W;
+    if (x < 0) x += W;
+    y %= H;
+    if (y < 0) y += H;
+    const float* t = sc.noise + 2 * ((size_t)y * W + x);
+    return vec2(t[0], t[1]);
+}
+inline vec2 mix2(vec2 a, vec2 b, float t) { return vec2(a.x * (1.0f - t) + b.x * t, a.y * (1.0f - t) + b.y * t); }
+inline vec2 noiseTexture(const OrcScene& sc, vec2 st) {
+    float u = st.x * (float)sc.filmW - 0.5f;
+    float v = st.y * (float)sc.filmH - 0.5f;
+    float fu = std::floor(u), fv = std::floor(v);
+    float au = u - fu, av = v - fv;
+    int x0 = f2i(fu), y0 = f2i(fv);
+    vec2 t00 = noiseTexel(sc, x0, y0), t10 = noiseTexel(sc, x0 + 1, y0);
+    vec2 t01 = noiseTexel(sc, x0, y0 + 1), t11 = noiseTexel(sc, x0 + 1, y0 + 1);
+    return mix2(mix2(t00, t10, au), mix2(t01, t11, au), av);
+}
+
+// main() of path_integ_naive.glsl:145-174 for one pixel and one pass.
+vec3 renderPixel(const OrcScene& sc, int px, int py, int spp, int freeCounter, bool& valid) {
+    vec2 texSize((float)sc.filmW, (float)sc.filmH);
+    vec2 scr = vec2((float)px, (float)py) / texSize;
+    vec2 nc = noiseTexture(sc, scr);
+    nc = noiseTexture(sc, nc);
+    vec2 tc = texSize * nc;
+    Rng g;
+    g.randSeed = f2u(tc.x) * (uint32_t)freeCounter + f2u(tc.y);
+    g.sampleSeed = f2u(tc.x) * f2u(tc.y);
+    const int sampleNum = 131072, sampleDim = 256;
+    int off = (int)((uint32_t)spp * (uint32_t)sampleDim);
+    if (off > sampleNum * sampleDim) off -= sampleNum * sampleDim;
+    g.sampleOffset = off;
+    int s = 0;
+    float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    vec3 r = pathIntegTrace(sc, ray, s, g);
+    valid = !hasNan(r);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Renders `passes` consecutive progressive passes (spp = spp0 + p,
+// freeCounter = fc0 + p) of the MIS path tracer for the listed pixels and
+// accumulates into out_rgb[npix*3] like imageStore(lastRes + result) does,
+// skipping NaN samples.
+void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, const int32_t* pixels, int64_t npix,
+                   float* out_rgb, int32_t nthreads) {
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            int64_t i = next.fetch_add(16);
+            if (i >= npix) break;
+            int64_t e = std::min<int64_t>(npix, i + 16);
+            for (; i < e; i++) {
+                int p = pixels[i];
+                int px = p % sc->filmW, py = p / sc->filmW;
+                vec3 acc(out_rgb[3 * i], out_rgb[3 * i + 1], out_rgb[3 * i + 2]);
+                for (int k = 0; k < passes; k++) {
+                    bool ok;
+                    vec3 r = renderPixel(*sc, px, py, spp0 + k, fc0 + k, ok);
+                    if (ok) acc = acc + r;
+                }
+                out_rgb[3 * i] = acc.x;
+                out_rgb[3 * i + 1] = acc.y;
+                out_rgb[3 * i + 2] = acc.z;
+            }
+        }
+    };
+    if (nthreads <= 1) {
+        work();
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; t++) th.emplace_back(work);
+    for (auto& t : th) t.join();
+}
+
+// ----------------------------------------------------------- host tables
+
+// Light power split and alias table (Scene.cpp:200-243, AliasTable.h:12-54).
+// vertices are world-space light vertices, indices local to them; each
+// instance k owns triangles [first[k], first[k+1]) and total power power[k].
+float orc_light_tables(const float* vertices, const uint32_t* indices, const uint32_t* first, const float* power,
+                       int32_t ninst, float* lightPower, int32_t* alias, float* prob) {
+    std::vector<float> pdf;
+    float lightSum = 0.0f;
+    int out = 0;
+    for (int k = 0; k < ninst; k++) {
+        vec3 P(power[3 * k], power[3 * k + 1], power[3 * k + 2]);
+        auto tri = [&](uint32_t t, vec3& a, vec3& b, vec3& c) {
+            a = vec3(vertices[3 * indices[3 * t]], vertices[3 * indices[3 * t] + 1], vertices[3 * indices[3 * t] + 2]);
+            b = vec3(vertices[3 * indices[3 * t + 1]], vertices[3 * indices[3 * t + 1] + 1], vertices[3 * indices[3 * t + 1] + 2]);
+            c = vec3(vertices[3 * indices[3 * t + 2]], vertices[3 * indices[3 * t + 2] + 1], vertices[3 * indices[3 * t + 2] + 2]);
+        };
+        float sumArea = 0.0f;
+        for (uint32_t t = first[k]; t < first[k + 1]; t++) {
+            vec3 a, b, c;
+            tri(t, a, b, c);
+            sumArea += length(cross(c - a, b - a));
+        }
+        for (uint32_t t = first[k]; t < first[k + 1]; t++) {
+            vec3 a, b, c;
+            tri(t, a, b, c);
+            float area = length(cross(c - a, b - a));
+            vec3 pw = P * area / sumArea;
+            lightPower[3 * out] = pw.x;
+            lightPower[3 * out + 1] = pw.y;
+            lightPower[3 * out + 2] = pw.z;
+            out++;
+            float l = dot(pw, vec3(0.299f, 0.587f, 0.114f));
+            pdf.push_back(l);
+            lightSum += l;
+        }
+    }
+    // AliasTable::build
+    int n = (int)pdf.size();
+    std::vector<float> pr = pdf;
+    float sumPdf = 0.0f;
+    for (int i = 0; i < n; i++) sumPdf += pr[i];
+    float sumInv = (float)n / sumPdf;
+    std::vector<std::pair<int, float>> greater, lesser;
+    for (int i = 0; i < n; i++) {
+        pr[i] *= sumInv;
+        (pr[i] < 1.0f ? lesser : greater).push_back({i, pr[i]});
+    }
+    std::vector<int> al(n, 0);
+    while (!greater.empty() && !lesser.empty()) {
+        auto [l, pl] = lesser.back();
+        lesser.pop_back();
+        auto [g, pg] = greater.back();
+        greater.pop_back();
+        al[l] = g;
+        pr[l] = pl;
+        pg += pl - 1.0f;
+        (pg < 1.0f ? lesser : greater).push_back({g, pg});
+    }
+    while (!greater.empty()) {
+        auto [g, pg] = greater.back();
+        greater.pop_back();
+        al[g] = g;
+        pr[g] = pg;
+    }
+    while (!lesser.empty()) {
+        auto [l, pl] = lesser.back();
+        lesser.pop_back();
+        al[l] = l;
+        pr[l] = pl;
+    }
+    for (int i = 0; i < n; i++) {
+        alias[i] = al[i];
+        prob[i] = pr[i];
+    }
+    return lightSum;
+}
+
+// AliasTable::build alone, through the light-table routine: one instance per
+// pdf entry would change the pdf, so the construction is repeated here.
+void orc_alias_build(const float* pdf, int32_t n, int32_t* alias, float* prob) {
+    std::vector<float> pr(pdf, pdf + n);
+    float sumPdf = 0.0f;
+    for (int i = 0; i < n; i++) sumPdf += pr[i];
+    float sumInv = (float)n / sumPdf;
+    std::vector<std::pair<int, float>> greater, lesser;
+    for (int i = 0; i < n; i++) {
+        pr[i] *= sumInv;
+        (pr[i] < 1.0f ? lesser : greater).push_back({i, pr[i]});
+    }
+    std::vector<int> al(n, 0);
+    while (!greater.empty() && !lesser.empty()) {
+        auto [l, pl] = lesser.back();
+        lesser.pop_back();
+        auto [g, pg] = greater.back();
+        greater.pop_back();
+        al[l] = g;
+        pr[l] = pl;
+        pg += pl - 1.0f;
+        (pg < 1.0f ? lesser : greater).push_back({g, pg});
+    }
+    while (!greater.empty()) {
+        auto [g, pg] = greater.back();
+        greater.pop_back();
+        al[g] = g;
+        pr[g] = pg;
+    }
+    while (!lesser.empty()) {
+        auto [l, pl] = lesser.back();
+        lesser.pop_back();
+        al[l] = l;
+        pr[l] = pl;
+    }
+    for (int i = 0; i < n; i++) {
+        alias[i] = al[i];
+        prob[i] = pr[i];
+    }
+}
+
+// Env-map sampling tables (EnvironmentMap.cpp:8-59, setupAliasTable :66-114).
+// rgb: float image W*H*3 (before the RGB16F upload).  alias/prob: (W+1)*H.
+// Returns the pdf sum; the shader receives int(sum) (EnvironmentMap.h:22).
+float orc_env_tables(const float* rgb, int32_t W, int32_t H, int32_t* alias, float* prob) {
+    auto off = [W](int i, int j) { return (size_t)i * (W + 1) + j; };
+    for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+            const float* p = rgb + 3 * ((size_t)i * W + j);
+            float lum = 0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2];
+            prob[off(i, j)] = lum * std::sin((float)(i + 0.5f) / (float)H * 3.141592653589793f);
+        }
+    auto setup = [](int32_t* al, float* pdf, int n, int stride) -> float {
+        float sum = 0.0f;
+        for (int i = 0, o = 0; i < n; i++, o += stride) sum += pdf[o];
+        float sumInv = (float)n / sum;
+        std::vector<std::pair<int, float>> greater, lesser;
+        for (int i = 0, o = 0; i < n; i++, o += stride) {
+            pdf[o] *= sumInv;
+            (pdf[o] < 1.0f ? lesser : greater).push_back({i, pdf[o]});
+        }
+        while (!greater.empty() && !lesser.empty()) {
+            auto [l, pl] = lesser.back();
+            lesser.pop_back();
+            auto [g, pg] = greater.back();
+            greater.pop_back();
+            al[l * stride] = g;
+            pdf[l * stride] = pl;
+            pg += pl - 1.0f;
+            (pg < 1.0f ? lesser : greater).push_back({g, pg});
+        }
+        while (!greater.empty()) {
+            auto [g, pg] = greater.back();
+            (void)pg;
+            greater.pop_back();
+            al[g * stride] = g;
+            pdf[g * stride] = 1.0f;
+        }
+        while (!lesser.empty()) {
+            auto [l, pl] = lesser.back();
+            (void)pl;
+            lesser.pop_back();
+            al[l * stride] = l;
+            pdf[l * stride] = 1.0f;
+        }
+        return sum;
+    };
+    for (int i = 0; i < H; i++) prob[off(i, W)] = setup(alias + off(i, 0), prob + off(i, 0), W, 1);
+    return setup(alias + W, prob + W, H, W + 1);
+}
+
+// Noise texture of Sampler::genNoiseTexture (Sampler.cpp:66-80) with the
+// libstdc++ engines: std::default_random_engine = minstd_rand0 (seed 1) and
+// uniform_real_distribution<float>(0, 1) = generate_canonical<float, 24>.
+void orc_noise(int32_t W, int32_t H, float* out) {
+    uint64_t x = 1;
+    size_t n = (size_t)W * H * 2;
+    for (size_t i = 0; i < n; i++) {
+        x = (x * 16807u) % 2147483647u;
+        float v = (float)(x - 1) / 2147483646.0f;
+        if (v >= 1.0f) v = std::nextafter(1.0f, 0.0f);
+        out[i] = v * (1.0f - 0.0f) + 0.0f;
+    }
+}
+
+// glm::normalize: x * inversesqrt(dot(x, x))
+static vec3 glmNormalize(vec3 v) { return v * (1.0f / std::sqrt(dot(v, v))); }
+
+// Camera::update (Camera.cpp:149-162) and the uniforms of NaivePath.cpp:49-60.
+// out: F[3], R[3], U[3], camMatInv[9] (column-major), tanFOV
+void orc_camera(const float* angle, float fov, float* out) {
+    const float rad = 0.01745329251994329576923690768489f;
+    float ax = angle[0] * rad, ay = angle[1] * rad;
+    float x = std::sin(ax) * std::cos(ay);
+    float y = std::cos(ax) * std::cos(ay);
+    float z = std::sin(ay);
+    vec3 front = glmNormalize(vec3(x, y, z));
+    vec3 right = glmNormalize(cross(front, vec3(0.0f, 0.0f, 1.0f)));
+    // glm::rotate(mat4(1), angle.z (radians), front) applied to (right, 1)
+    float c = std::cos(angle[2]), s = std::sin(angle[2]);
+    vec3 axis = glmNormalize(front);
+    vec3 temp = axis * (1.0f - c);
+    float R00 = c + temp.x * axis.x, R01 = temp.x * axis.y + s * axis.z, R02 = temp.x * axis.z - s * axis.y;
+    float R10 = temp.y * axis.x - s * axis.z, R11 = c + temp.y * axis.y, R12 = temp.y * axis.z + s * axis.x;
+    float R20 = temp.z * axis.x + s * axis.y, R21 = temp.z * axis.y - s * axis.x, R22 = c + temp.z * axis.z;
+    // rotMatrix columns: col j = Rotate[j] (m = identity); result = M * (right, 1)
+    vec3 rr((R00 * right.x + R10 * right.y) + R20 * right.z, (R01 * right.x + R11 * right.y) + R21 * right.z,
+            (R02 * right.x + R12 * right.y) + R22 * right.z);
+    right = glmNormalize(rr);
+    vec3 up = glmNormalize(cross(right, front));
+    mat3 m{right, up, front};
+    mat3 inv = inverse(m);
+    float* o = out;
+    o[0] = front.x; o[1] = front.y; o[2] = front.z;
+    o[3] = right.x; o[4] = right.y; o[5] = right.z;
+    o[6] = up.x; o[7] = up.y; o[8] = up.z;
+    o[9] = inv.c0.x; o[10] = inv.c0.y; o[11] = inv.c0.z;
+    o[12] = inv.c1.x; o[13] = inv.c1.y; o[14] = inv.c1.z;
+    o[15] = inv.c2.x; o[16] = inv.c2.y; o[17] = inv.c2.z;
+    o[18] = std::tan(fov * 0.5f * rad);
+}
+
+}  // extern "C"

@@ -327,6 +327,60 @@ int host_threads() {
     return n == 0 ? 1 : (int)n;
 }
 
+// Builds the MTBVH on the host and uploads node records and triangles to the
+// current device.  Throws zgl::Error.
+zgl_accel* accel_create(const float* vertices, const uint32_t* indices, int64_t ntri) {
+    auto* a = new zgl_accel();
+    try {
+        ZGL_CUDA(cudaGetDevice(&a->device));
+        ZGL_CUDA(cudaMalloc(&a->d_counter, 256));
+        a->ntri = ntri;
+        build_bvh(vertices, indices, a->ntri, a->host, host_threads());
+        a->M = a->host.M;
+        if (a->M > 0) {
+            size_t nb = sizeof(float) * a->M * 6, nh = sizeof(int32_t) * a->M * 18;
+            float* d_bounds = nullptr;
+            int32_t* d_hit = nullptr;
+            ZGL_CUDA(cudaMalloc(&a->d_nodes, sizeof(float4) * 12 * a->M));
+            ZGL_CUDA(cudaMalloc(&a->d_tris, sizeof(float4) * 3 * a->ntri));
+            ZGL_CUDA(cudaMalloc(&d_bounds, nb));
+            ZGL_CUDA(cudaMalloc(&d_hit, nh));
+            ZGL_CUDA(cudaMemcpy(d_bounds, a->host.bounds.data(), nb, cudaMemcpyHostToDevice));
+            ZGL_CUDA(cudaMemcpy(d_hit, a->host.hitTable.data(), nh, cudaMemcpyHostToDevice));
+            ZGL_CUDA(launch_pack_nodes(d_bounds, d_hit, a->M, a->d_nodes, 0));
+            // triangles: a, ab = b - a, ac = c - a (float32, as intersection.glsl:68-69)
+            std::vector<float4> tris((size_t)a->ntri * 3);
+            for (int64_t t = 0; t < a->ntri; t++) {
+                const float* A = vertices + 3 * (size_t)indices[3 * t];
+                const float* B = vertices + 3 * (size_t)indices[3 * t + 1];
+                const float* C = vertices + 3 * (size_t)indices[3 * t + 2];
+                float abx = B[0] - A[0], aby = B[1] - A[1], abz = B[2] - A[2];
+                float acx = C[0] - A[0], acy = C[1] - A[1], acz = C[2] - A[2];
+                tris[3 * t + 0] = make_float4(A[0], A[1], A[2], abx);
+                tris[3 * t + 1] = make_float4(aby, abz, acx, acy);
+                tris[3 * t + 2] = make_float4(acz, 0.0f, 0.0f, 0.0f);
+            }
+            ZGL_CUDA(cudaMemcpy(a->d_tris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice));
+            ZGL_CUDA(cudaDeviceSynchronize());
+            ZGL_CUDA(cudaFree(d_bounds));
+            ZGL_CUDA(cudaFree(d_hit));
+        }
+    } catch (...) {
+        accel_free(a);
+        throw;
+    }
+    return a;
+}
+
+void accel_free(zgl_accel* a) {
+    if (!a) return;
+    if (a->d_counter) cudaFree(a->d_counter);
+    if (a->d_nodes) cudaFree(a->d_nodes);
+    if (a->d_tris) cudaFree(a->d_tris);
+    if (a->d_stage) cudaFree(a->d_stage);
+    delete a;
+}
+
 }  // namespace zgl
 
 using namespace zgl;
@@ -368,50 +422,7 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint3
     if (!out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build: out is NULL");
     *out = nullptr;
     validate_mesh("zgl_accel_build", vertices, n_vertices, indices, n_triangles);
-
-    auto* a = new zgl_accel();
-    try {
-        ZGL_CUDA(cudaGetDevice(&a->device));
-        ZGL_CUDA(cudaMalloc(&a->d_counter, 256));
-        a->ntri = (int64_t)n_triangles;
-        build_bvh(vertices, indices, a->ntri, a->host, host_threads());
-        a->M = a->host.M;
-        if (a->M > 0) {
-            size_t nb = sizeof(float) * a->M * 6, nh = sizeof(int32_t) * a->M * 18;
-            float* d_bounds = nullptr;
-            int32_t* d_hit = nullptr;
-            ZGL_CUDA(cudaMalloc(&a->d_nodes, sizeof(float4) * 12 * a->M));
-            ZGL_CUDA(cudaMalloc(&a->d_tris, sizeof(float4) * 3 * a->ntri));
-            ZGL_CUDA(cudaMalloc(&d_bounds, nb));
-            ZGL_CUDA(cudaMalloc(&d_hit, nh));
-            ZGL_CUDA(cudaMemcpy(d_bounds, a->host.bounds.data(), nb, cudaMemcpyHostToDevice));
-            ZGL_CUDA(cudaMemcpy(d_hit, a->host.hitTable.data(), nh, cudaMemcpyHostToDevice));
-            ZGL_CUDA(launch_pack_nodes(d_bounds, d_hit, a->M, a->d_nodes, 0));
-            // triangles: a, ab = b - a, ac = c - a (float32, as intersection.glsl:68-69)
-            std::vector<float4> tris((size_t)a->ntri * 3);
-            for (int64_t t = 0; t < a->ntri; t++) {
-                const float* A = vertices + 3 * (size_t)indices[3 * t];
-                const float* B = vertices + 3 * (size_t)indices[3 * t + 1];
-                const float* C = vertices + 3 * (size_t)indices[3 * t + 2];
-                float abx = B[0] - A[0], aby = B[1] - A[1], abz = B[2] - A[2];
-                float acx = C[0] - A[0], acy = C[1] - A[1], acz = C[2] - A[2];
-                tris[3 * t + 0] = make_float4(A[0], A[1], A[2], abx);
-                tris[3 * t + 1] = make_float4(aby, abz, acx, acy);
-                tris[3 * t + 2] = make_float4(acz, 0.0f, 0.0f, 0.0f);
-            }
-            ZGL_CUDA(cudaMemcpy(a->d_tris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice));
-            ZGL_CUDA(cudaDeviceSynchronize());
-            ZGL_CUDA(cudaFree(d_bounds));
-            ZGL_CUDA(cudaFree(d_hit));
-        }
-    } catch (...) {
-        if (a->d_counter) cudaFree(a->d_counter);
-        if (a->d_nodes) cudaFree(a->d_nodes);
-        if (a->d_tris) cudaFree(a->d_tris);
-        delete a;
-        throw;
-    }
-    *out = a;
+    *out = accel_create(vertices, indices, (int64_t)n_triangles);
     ZGL_API_END
 }
 
@@ -436,12 +447,7 @@ zgl_status zgl_accel_export(const zgl_accel* accel, float* bounds, int32_t* hit_
 
 zgl_status zgl_accel_destroy(zgl_accel* accel) {
     ZGL_API_BEGIN
-    if (!accel) return ZGL_OK;
-    if (accel->d_nodes) cudaFree(accel->d_nodes);
-    if (accel->d_tris) cudaFree(accel->d_tris);
-    if (accel->d_stage) cudaFree(accel->d_stage);
-    if (accel->d_counter) cudaFree(accel->d_counter);
-    delete accel;
+    accel_free(accel);
     ZGL_API_END
 }
 

@@ -62,4 +62,9 @@ cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir
                                int64_t n, int any_hit, int32_t* visits, int32_t* tests,
                                cudaStream_t s);
 
+// Host build + upload (throws zgl::Error) and release of an accelerator.
+zgl_accel* accel_create(const float* vertices, const uint32_t* indices, int64_t ntri);
+void accel_free(zgl_accel* a);
+int host_threads();
+
 }  // namespace zgl

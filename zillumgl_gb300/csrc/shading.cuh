@@ -1,0 +1,513 @@
+// shading.cuh — device side of the render hot path: samplers, BSDFs, area
+// and environment lights, thin-lens camera.  Each function follows the GLSL
+// function it names (src/shader/*.glsl) operation for operation in float32.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "accel.h"
+#include "device_scene.h"
+#include "traverse.cuh"
+#include "zmath.cuh"
+
+namespace zgl {
+
+enum : uint32_t { kDiffuse = 1u, kGlosRefl = 2u, kGlosTrans = 4u, kSpecRefl = 8u, kSpecTrans = 16u, kInvalid = 1u << 16 };
+enum : uint32_t { kLambertian = 0, kPrincipled = 1, kMetalWorkflow = 2, kDielectric = 3, kThinDielectric = 4 };
+
+__device__ __forceinline__ v3 f3(float3 a) { return v3{a.x, a.y, a.z}; }
+
+// ------------------------------------------------------------- random.glsl
+__device__ __forceinline__ uint32_t zhash(uint32_t seed) {  // random.glsl:5-13
+    seed = (seed ^ 61u) ^ (seed >> 16u);
+    seed *= 9u;
+    seed = seed ^ (seed >> 4u);
+    seed *= 0x27d4eb2du;
+    seed = seed ^ (seed >> 15u);
+    return seed;
+}
+
+struct Sampler {
+    uint32_t randSeed;
+    uint32_t sampleSeed;
+    uint32_t sampleOffset;  // spp * 256, wrapped like path_integ_naive.glsl:163-164
+    int32_t dim;            // the Sampler counter `s`
+    int32_t mode;           // 0 independent, 1 sobol
+    const uint32_t* rowCache;  // shared-memory copy of the 256 values of row sampleOffset/256
+    const uint32_t* mats;      // 256*32 generator matrices
+};
+
+__device__ __forceinline__ float rand01(Sampler& g) {  // random.glsl:15-19
+    g.randSeed = zhash(g.randSeed);
+    return (float)g.randSeed * (1.0f / 4294967296.0f);
+}
+
+__device__ __forceinline__ uint32_t sobol_value(const uint32_t* mats, uint32_t index, uint32_t dim) {
+    uint32_t r = 0;
+    const uint32_t* col = mats + dim * 32u;
+    for (int i = 0; index != 0u; index >>= 1, i++)
+        if (index & 1u) r ^= __ldg(col + i);
+    return r;
+}
+
+__device__ __forceinline__ float sample1D(Sampler& g) {  // random.glsl:61-70
+    if (g.mode == 0) return rand01(g);
+    uint32_t r;
+    if (g.dim < 256) {
+        r = g.rowCache[g.dim];
+    } else {
+        uint32_t idx = g.sampleOffset + (uint32_t)g.dim;
+        r = sobol_value(g.mats, idx >> 8, idx & 255u);
+    }
+    r ^= g.sampleSeed;
+    g.sampleSeed = zhash(g.sampleSeed);
+    g.dim++;
+    return (float)r / 4294967296.0f;
+}
+
+// --------------------------------------------------------------- math.glsl
+__device__ __forceinline__ v2 toConcentricDisk(v2 v) {  // math.glsl:25-41
+    if (v.x == 0.0f && v.y == 0.0f) return mk2(0.0f, 0.0f);
+    v = mk2(v.x * 2.0f - 1.0f, v.y * 2.0f - 1.0f);
+    float phi, r;
+    if (v.x * v.x > v.y * v.y) {
+        r = v.x;
+        phi = kPi * v.y / v.x * 0.25f;
+    } else {
+        r = v.y;
+        phi = kPi * 0.5f - kPi * v.x / v.y * 0.25f;
+    }
+    return mk2(r * zcos(phi), r * zsin(phi));
+}
+__device__ __forceinline__ m3 tbnMatrix(v3 n) {  // math.glsl:78-84
+    v3 t = (fabsf(n.z) > 0.999f) ? mk3(0.0f, 1.0f, 0.0f) : mk3(0.0f, 0.0f, 1.0f);
+    v3 b = normalize(cross(n, t));
+    t = cross(b, n);
+    return m3{t, b, n};
+}
+__device__ __forceinline__ v3 normalToWorld(v3 n, v3 v) { return normalize(mul(tbnMatrix(n), v)); }
+__device__ __forceinline__ v3 sampleCosineWeighted(v3 n, v2 u, float& pdf) {  // math.glsl:99-105
+    v2 uv = toConcentricDisk(u);
+    float z = zsqrt(1.0f - dot(uv, uv));
+    pdf = kPiInv * z;
+    return normalToWorld(n, mk3(uv.x, uv.y, z));
+}
+__device__ __forceinline__ bool sameHemisphere(v3 n, v3 a, v3 b) { return dot(n, a) * dot(n, b) > 0.0f; }
+__device__ __forceinline__ v3 sampleTriangleUniform(v3 va, v3 vb, v3 vc, v2 uv) {  // math.glsl:139-145
+    float r = zsqrt(uv.y);
+    float u = 1.0f - r;
+    float v = uv.x * r;
+    return va * (1.0f - u - v) + vb * u + vc * v;
+}
+__device__ __forceinline__ float triangleArea(v3 va, v3 vb, v3 vc) {
+    return 0.5f * length(cross(vc - va, vb - va));
+}
+__device__ __forceinline__ v3 rotateZ(v3 v, float angle) {  // math.glsl:180-185
+    float c = zcos(angle), s = zsin(angle);
+    return mk3(v.x * c - v.y * s, v.x * s + v.y * c, v.z);
+}
+__device__ __forceinline__ v2 sphereToPlane(v3 uv) {  // math.glsl:58-64
+    float theta = zatan2(uv.y, uv.x);
+    if (theta < 0.0f) theta += kPi * 2.0f;
+    float phi = zatan2(length(mk2(uv.x, uv.y)), uv.z);
+    return mk2(theta * kPiInv * 0.5f, phi * kPiInv);
+}
+__device__ __forceinline__ v3 planeToSphere(v2 uv) {  // math.glsl:66-71
+    float theta = uv.x * kPi * 2.0f;
+    float phi = uv.y * kPi;
+    return mk3(zcos(theta) * zsin(phi), zsin(theta) * zsin(phi), zcos(phi));
+}
+__device__ __forceinline__ float biHeuristic(float f, float g) { return f * f / (f * f + g * g); }
+
+// ---------------------------------------------------------- microfacet.glsl
+__device__ __forceinline__ float schlickW(float c) { return pow5(1.0f - c); }
+__device__ __forceinline__ v3 schlickF(float c, v3 F0) { return F0 + (mk3(1.0f) - F0) * pow5(1.0f - c); }
+__device__ __forceinline__ float schlickG(float c, float alpha) {
+    float k = alpha * 0.5f;
+    return c / (c * (1.0f - k) + k);
+}
+__device__ __forceinline__ float smithG(v3 n, v3 wo, v3 wi, float alpha) {
+    return schlickG(absDot(n, wo), alpha) * schlickG(absDot(n, wi), alpha);
+}
+__device__ __forceinline__ float ggx(float c, float alpha) {  // microfacet.glsl:30-40
+    if (c < 1e-6f) return 0.0f;
+    float a2 = alpha * alpha;
+    float denom = c * c * (a2 - 1.0f) + 1.0f;
+    denom = denom * denom * kPi;
+    return a2 / denom;
+}
+__device__ __forceinline__ float ggxPdfVisibleWm(v3 n, v3 m, v3 wo, float alpha) {
+    return ggx(dot(n, m), alpha) * schlickG(dot(n, wo), alpha) * absDot(m, wo) / absDot(n, wo);
+}
+__device__ __forceinline__ v3 ggxSampleVisibleWm(v3 n, v3 wo, float alpha, v2 u) {  // microfacet.glsl:74-92
+    m3 tbn = tbnMatrix(n);
+    m3 tbnInv = inverse(tbn);
+    v3 vh = normalize(mul(tbnInv, wo) * mk3(alpha, alpha, 1.0f));
+    float lensq = vh.x * vh.x + vh.y * vh.y;
+    v3 t1 = lensq > 0.0f ? mk3(-vh.y, vh.x, 0.0f) / zsqrt(lensq) : mk3(1.0f, 0.0f, 0.0f);
+    v3 t2 = cross(vh, t1);
+    v2 xi = toConcentricDisk(u);
+    float s = 0.5f * (1.0f + vh.z);
+    xi.y = (1.0f - s) * zsqrt(1.0f - xi.x * xi.x) + s * xi.y;
+    v3 h = t1 * xi.x + t2 * xi.y + vh * zsqrt(zmax(0.0f, 1.0f - xi.x * xi.x - xi.y * xi.y));
+    h = normalize(mk3(h.x * alpha, h.y * alpha, zmax(0.0f, h.z)));
+    return normalToWorld(n, h);
+}
+__device__ __forceinline__ float gtr1(float c, float alpha) {  // microfacet.glsl:94-98
+    float a2 = alpha * alpha;
+    return (a2 - 1.0f) / (2.0f * kPi * zlog(alpha) * (1.0f + (a2 - 1.0f) * c * c));
+}
+__device__ __forceinline__ v3 gtr1SampleWm(v3 n, v3 wo, float alpha, v2 u) {  // microfacet.glsl:105-115
+    float cosTheta = zsqrt(zmax(0.0f, (1.0f - zpow(alpha, 1.0f - u.x)) / (1.0f - alpha)));
+    float sinTheta = zsqrt(zmax(0.0f, 1.0f - cosTheta * cosTheta));
+    float phi = 2.0f * u.y * kPi;
+    v3 m = normalize(mk3(zcos(phi) * sinTheta, zsin(phi) * sinTheta, cosTheta));
+    if (!sameHemisphere(n, wo, m)) m = -m;
+    return normalize(normalToWorld(n, m));
+}
+
+// ------------------------------------------------------------ material.glsl
+struct BSDFParam {
+    v3 baseColor;
+    float subsurface, metallic, roughness, specular, specularTint;
+    float sheen, sheenTint, clearcoat, clearcoatGloss;
+};
+struct BSDFSample {
+    v3 wi;
+    float pdf;
+    v3 bsdf;
+    uint32_t flag;
+};
+
+__device__ __forceinline__ v3 principledMetal(v3 wo, v3 wi, v3 n, v3 fm0, float alpha) {  // material.glsl:357-373
+    float cosWo = satDot(n, wo);
+    float cosWi = satDot(n, wi);
+    v3 h = normalize(wo + wi);
+    if (cosWo < 1e-10f || cosWi < 1e-10f) return mk3(0.0f);
+    v3 fm = schlickF(absDot(h, wo), fm0);
+    float dm = ggx(dot(n, h), alpha);
+    float gm = smithG(n, wo, wi, alpha);
+    float denom = 4.0f * cosWi * cosWo;
+    if (denom < 1e-7f) return mk3(0.0f);
+    return fm * dm * gm / denom;
+}
+__device__ __forceinline__ float principledMetalPdf(v3 wo, v3 wi, v3 n, float alpha) {
+    v3 h = normalize(wo + wi);
+    return ggxPdfVisibleWm(n, h, wo, alpha) / (4.0f * absDot(h, wo));
+}
+__device__ __forceinline__ v3 principledClearcoat(v3 wo, v3 wi, v3 n, v3 baseColor, float alpha) {  // :393-409
+    float cosWo = satDot(n, wo);
+    float cosWi = satDot(n, wi);
+    v3 h = normalize(wo + wi);
+    if (cosWo < 1e-6f || cosWi < 1e-6f) return mk3(0.0f);
+    v3 fc = schlickF(absDot(h, wo), baseColor);
+    float dc = gtr1(satDot(n, h), alpha);
+    float gc = smithG(n, wo, wi, 0.25f);
+    float denom = 4.0f * cosWi * cosWo;
+    if (denom < 1e-7f) return mk3(0.0f);
+    return fc * dc * gc / denom;
+}
+__device__ __forceinline__ float principledClearcoatPdf(v3 wo, v3 wi, v3 n, float alpha) {
+    v3 h = normalize(wo + wi);
+    return gtr1(satDot(n, h), alpha) * absDot(n, h) / (4.0f * absDot(h, wo));
+}
+__device__ __forceinline__ v3 principledDiffuse(v3 wo, v3 wi, v3 n, v3 baseColor, float subsurface,
+                                                float roughness) {  // :429-452
+    float cosWo = satDot(n, wo);
+    float cosWi = satDot(n, wi);
+    if (cosWo < 1e-10f || cosWi < 1e-10f) return mk3(0.0f);
+    v3 h = normalize(wo + wi);
+    float hCosWi = dot(h, wi);
+    float hCosWi2 = hCosWi * hCosWi;
+    float fi = schlickW(cosWi);
+    float fo = schlickW(cosWo);
+    v3 fd90 = mk3(0.5f + 2.0f * roughness * hCosWi2);
+    v3 fd = mix3(mk3(1.0f), fd90, fi) * mix3(mk3(1.0f), fd90, fo);
+    v3 baseDiffuse = baseColor * fd * kPiInv;
+    v3 fss90 = mk3(roughness * hCosWi2);
+    v3 fss = mix3(mk3(1.0f), fss90, fi) * mix3(mk3(1.0f), fss90, fo);
+    v3 ss = baseColor * kPiInv * 1.25f * (fss * (1.0f / (cosWi + cosWo) - 0.5f) + mk3(0.5f));
+    return mix3(baseDiffuse, ss, subsurface);
+}
+__device__ __forceinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :462-490
+    float alpha = sq(p.roughness);
+    float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
+    float lum = luminance(p.baseColor);
+    v3 tint = lum > 0.0f ? p.baseColor / lum : mk3(1.0f);
+    v3 fm0 = mix3(0.08f * p.specular * mix3(mk3(1.0f), tint, p.specularTint), p.baseColor, p.metallic);
+    float hCosWi = dot(normalize(wo + wi), wi);
+    v3 res = mk3(0.0f);
+    res = res + principledDiffuse(wo, wi, n, p.baseColor, p.subsurface, p.roughness) * (1.0f - p.metallic);
+    res = res + principledMetal(wo, wi, n, fm0, alpha);
+    res = res + principledClearcoat(wo, wi, n, p.baseColor, ccAlpha) * p.clearcoat * 0.25f;
+    res = res + mix3(mk3(1.0f), tint, p.sheenTint) * schlickW(hCosWi) * p.sheen * (dot(n, wi) < 0.0f ? 0.0f : 1.0f);
+    return res;
+}
+__device__ __forceinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :492-514
+    float pdf = 0.0f;
+    float alpha = sq(p.roughness);
+    float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
+    float spec = 1.0f / (2.0f - p.metallic);
+    float cosinePdf = absDot(n, wi) * kPiInv;
+    pdf += cosinePdf * (1.0f - spec);
+    pdf += principledMetalPdf(wo, wi, n, alpha) * spec;
+    pdf += principledClearcoatPdf(wo, wi, n, ccAlpha) * 0.25f * p.clearcoat;
+    return pdf / (1.0f + 0.25f * p.clearcoat);
+}
+__device__ __forceinline__ BSDFSample principledBRDFSample(v3 n, v3 wo, const BSDFParam& p, v3 u, Sampler& g) {
+    float alpha = sq(p.roughness);  // material.glsl:516-555
+    float spec = 1.0f / (2.0f - p.metallic);
+    float cdf0 = 1.0f - spec, cdf1 = 1.0f, cdf2 = 1.0f + p.clearcoat * 0.25f;
+    float s = rand01(g) * cdf2;  // the lobe pick draws from the rand() stream
+    v3 wi;
+    if (s <= cdf0) {
+        float pdf;
+        wi = sampleCosineWeighted(n, mk2(u.y, u.z), pdf);
+    } else if (s <= cdf1) {
+        v3 h = ggxSampleVisibleWm(n, wo, alpha, mk2(u.y, u.z));
+        v3 w = reflect(-wo, h);
+        wi = (dot(n, w) < 0.0f) ? mk3(0.0f) : w;
+    } else {
+        v3 h = gtr1SampleWm(n, wo, alpha, mk2(u.y, u.z));  // base alpha, as the reference
+        v3 w = reflect(-wo, h);
+        wi = (dot(n, w) < 0.0f) ? mk3(0.0f) : w;
+    }
+    BSDFSample r;
+    r.wi = wi;
+    r.bsdf = principledBRDF(wo, wi, n, p);
+    r.pdf = principledBRDFPdf(wo, wi, n, p);
+    r.flag = kDiffuse;
+    return r;
+}
+
+// ----------------------------------------------------- material_loader.glsl
+__device__ __forceinline__ uint32_t loadMaterialType(const DeviceScene& sc, int matId) {
+    return (uint32_t)__float_as_int(__ldg(&sc.materials[4 * matId + 3]).y);
+}
+__device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_t type, int matId) {
+    const float4 m0 = __ldg(&sc.materials[4 * matId + 0]);
+    BSDFParam p;
+    p.baseColor = mk3(m0.x, m0.y, m0.z);
+    p.subsurface = p.metallic = p.roughness = p.specular = p.specularTint = 0.0f;
+    p.sheen = p.sheenTint = p.clearcoat = p.clearcoatGloss = 0.0f;
+    if (type == kPrincipled) {  // loadPrincipledBRDF (material_loader.glsl:37-58)
+        const float4 m1 = __ldg(&sc.materials[4 * matId + 1]);
+        const float4 m2 = __ldg(&sc.materials[4 * matId + 2]);
+        p.roughness = mixf(0.0134f, 1.0f, m0.w);
+        p.subsurface = m1.x;
+        p.metallic = m1.y;
+        p.specular = m1.z;
+        p.specularTint = m1.w;
+        p.sheen = m2.x;
+        p.sheenTint = m2.y;
+        p.clearcoat = m2.z;
+        p.clearcoatGloss = m2.w;
+    }
+    return p;
+}
+__device__ __forceinline__ v3 materialBSDF(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n) {
+    if (type == kPrincipled) return principledBRDF(wo, wi, n, p);
+    return p.baseColor * kPiInv;
+}
+__device__ __forceinline__ float materialPdf(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n) {
+    if (type == kPrincipled) return principledBRDFPdf(wo, wi, n, p);
+    return satDot(wi, n) * kPiInv;
+}
+__device__ __forceinline__ BSDFSample materialSample(uint32_t type, const BSDFParam& p, v3 n, v3 wo, v3 u,
+                                                     Sampler& g) {
+    if (type == kPrincipled) return principledBRDFSample(n, wo, p, u, g);
+    BSDFSample r;  // lambertianSample (material.glsl:78-83)
+    float pdf;
+    r.wi = sampleCosineWeighted(n, mk2(u.y, u.z), pdf);
+    r.pdf = satDot(n, r.wi) * kPiInv;
+    r.bsdf = p.baseColor * kPiInv;
+    r.flag = kDiffuse;
+    return r;
+}
+
+// ------------------------------------------------------- intersection.glsl
+struct TriShade {
+    v3 a, b, c, na, nb, nc;
+    int32_t matTex;
+};
+__device__ __forceinline__ TriShade loadTri(const DeviceScene& sc, int id) {
+    const float4* p = sc.shade + 5 * (size_t)id;
+    float4 s0 = __ldg(p), s1 = __ldg(p + 1), s2 = __ldg(p + 2), s3 = __ldg(p + 3), s4 = __ldg(p + 4);
+    TriShade t;
+    t.a = mk3(s0.x, s0.y, s0.z);
+    t.b = mk3(s0.w, s1.x, s1.y);
+    t.c = mk3(s1.z, s1.w, s2.x);
+    t.na = mk3(s2.y, s2.z, s2.w);
+    t.nb = mk3(s3.x, s3.y, s3.z);
+    t.nc = mk3(s3.w, s4.x, s4.y);
+    t.matTex = __float_as_int(s4.z);
+    return t;
+}
+struct Surface {
+    v3 ns, ng;
+};
+__device__ __forceinline__ Surface surfaceInfo(const TriShade& t, v3 p) {  // intersection.glsl:188-224
+    v3 pa = t.a - p, pb = t.b - p, pc = t.c - p;
+    float areaInv = 1.0f / length(cross(t.b - t.a, t.c - t.a));
+    float la = length(cross(pb, pc)) * areaInv;
+    float lb = length(cross(pc, pa)) * areaInv;
+    float lc = 1.0f - la - lb;
+    Surface s;
+    s.ns = normalize(t.na * la + t.nb * lb + t.nc * lc);
+    s.ng = normalize(cross(pa, pb));
+    if (dot(s.ns, s.ng) < 0.0f) s.ng = -s.ng;
+    return s;
+}
+__device__ __forceinline__ v3 geomNormal(const DeviceScene& sc, int triId, v3 p) {
+    return surfaceInfo(loadTri(sc, triId), p).ng;
+}
+
+struct Ray {
+    v3 ori, dir;
+};
+__device__ __forceinline__ Ray rayOffseted(v3 o, v3 d) { return Ray{o + d * 1e-4f, d}; }
+__device__ __forceinline__ v3 rayPoint(const Ray& r, float t) { return r.ori + r.dir * t; }
+
+__device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float& dist) {
+    TraceRay tr = make_trace_ray(make_float3(r.ori.x, r.ori.y, r.ori.z), make_float3(r.dir.x, r.dir.y, r.dir.z));
+    dist = 1e8f;
+    int v = 0, t = 0;
+    return traverse<false, false>(sc.accel, tr, dist, v, t);
+}
+__device__ __forceinline__ bool bvhTest(const DeviceScene& sc, const Ray& r, float dist) {
+    TraceRay tr = make_trace_ray(make_float3(r.ori.x, r.ori.y, r.ori.z), make_float3(r.dir.x, r.dir.y, r.dir.z));
+    int v = 0, t = 0;
+    return traverse<true, false>(sc.accel, tr, dist, v, t) != 0;
+}
+__device__ __forceinline__ bool visible(const DeviceScene& sc, v3 x, v3 y) {  // intersection.glsl:429-433
+    float dist = distance(x, y) - 2e-5f;
+    v3 wi = normalize(y - x);
+    return !bvhTest(sc, Ray{x + wi * 1e-5f, wi}, dist);
+}
+
+// ----------------------------------------------------------------- light.glsl
+struct LiSample {
+    v3 wi, coef;
+    float pdf;
+};
+__device__ __forceinline__ LiSample invalidLi() { return LiSample{mk3(0.0f), mk3(0.0f), 0.0f}; }
+
+__device__ __forceinline__ int lightSampleOne(const DeviceScene& sc, v2 u) {  // light.glsl:68-72
+    int cx = min(zf2i((float)sc.nLight * u.x), sc.nLight - 1);  // u.x == 1.0 would read past the table
+    return (u.y < __ldg(&sc.lightProb[cx])) ? cx : __ldg(&sc.lightAlias[cx]);
+}
+__device__ __forceinline__ v3 lightPowerOf(const DeviceScene& sc, int id, float& area) {
+    float4 p = __ldg(&sc.lightPower[id]);
+    area = p.w;
+    return mk3(p.x, p.y, p.z);
+}
+__device__ __forceinline__ float lightPdfSampleOne(const DeviceScene& sc, int id) {
+    float a;
+    return luminance(lightPowerOf(sc, id, a)) / sc.lightSum;
+}
+__device__ __forceinline__ v3 lightLe(const DeviceScene& sc, int id, v3 x, v3 wo) {  // light.glsl:79-86
+    int triId = id + sc.objPrimCount;
+    v3 ng = geomNormal(sc, triId, x);
+    if (dot(wo, ng) <= 0.0f) return mk3(0.0f);
+    float area;
+    v3 pw = lightPowerOf(sc, id, area);
+    return pw / area * 0.5f * kPiInv;
+}
+__device__ __forceinline__ float lightPdfLi(const DeviceScene& sc, int id, v3 x, v3 y) {  // light.glsl:88-98
+    int triId = id + sc.objPrimCount;
+    v3 norm = geomNormal(sc, triId, y);
+    v3 yx = normalize(x - y);
+    float cosTheta = absDot(norm, yx);
+    if (cosTheta < 1e-8f) return -1.0f;
+    float area;
+    lightPowerOf(sc, id, area);
+    return distSquare(x, y) / (area * cosTheta);
+}
+__device__ __forceinline__ LiSample lightSampleLi(const DeviceScene& sc, int id, v3 x, v2 u) {  // light.glsl:122-155
+    int triId = id + sc.objPrimCount;
+    TriShade t = loadTri(sc, triId);
+    v3 y = sampleTriangleUniform(t.a, t.b, t.c, u);
+    v3 wi = normalize(y - x);
+    v3 norm = surfaceInfo(t, y).ng;
+    float cosTheta = dot(norm, -wi);
+    if (cosTheta < 1e-6f) return invalidLi();
+    Ray lightRay = rayOffseted(x, wi);
+    float dist = distance(x, y);
+    float area;
+    v3 pw = lightPowerOf(sc, id, area);
+    float pdf = dist * dist / (area * cosTheta);
+    float testDist = dist - 1e-4f - 1e-6f;
+    if (bvhTest(sc, lightRay, testDist) || pdf < 1e-8f) return invalidLi();
+    v3 weight = lightLe(sc, id, y, -wi);
+    float pdfSample = luminance(pw) / sc.lightSum;
+    pdf *= pdfSample;
+    return LiSample{wi, weight / pdf, pdf};
+}
+
+__device__ __forceinline__ v3 envTexel(const DeviceScene& sc, int x, int y) {
+    int W = sc.envW, H = sc.envH;
+    x %= W;
+    if (x < 0) x += W;
+    y %= H;
+    if (y < 0) y += H;
+    float4 t = __ldg(&sc.envTexels[(size_t)y * W + x]);
+    return mk3(t.x, t.y, t.z);
+}
+__device__ __forceinline__ v3 envTexture(const DeviceScene& sc, v2 st) {  // bilinear, repeat, texel centres
+    float u = st.x * (float)sc.envW - 0.5f;
+    float v = st.y * (float)sc.envH - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float au = u - fu, av = v - fv;
+    int x0 = zf2i(fu), y0 = zf2i(fv);
+    v3 t00 = envTexel(sc, x0, y0), t10 = envTexel(sc, x0 + 1, y0);
+    v3 t01 = envTexel(sc, x0, y0 + 1), t11 = envTexel(sc, x0 + 1, y0 + 1);
+    return mix3(mix3(t00, t10, au), mix3(t01, t11, au), av);
+}
+__device__ __forceinline__ v3 envLe(const DeviceScene& sc, v3 wi) {  // light.glsl:163-167
+    if (sc.envTexels == nullptr) return mk3(0.0f);
+    wi = rotateZ(wi, -sc.envRotation);
+    return envTexture(sc, sphereToPlane(wi));
+}
+__device__ __forceinline__ float envGetPortion(const DeviceScene& sc, v3 wi) { return luminance(envLe(sc, wi)) / sc.envSum; }
+__device__ __forceinline__ float envPdfLi(const DeviceScene& sc, v3 wi) {  // light.glsl:174-179
+    if (sc.envSum == 0.0f) return 0.0f;
+    return envGetPortion(sc, wi) * (float)sc.envW * (float)sc.envH * 0.5f * sq(kPiInv);
+}
+__device__ __forceinline__ LiSample envSampleLi(const DeviceScene& sc, v3 x, float ux, float uy, float uz, float uw) {
+    if (sc.envTexels == nullptr) return invalidLi();  // light.glsl:181-219
+    int w = sc.envW, h = sc.envH;
+    int rx = min(zf2i((float)h * ux), h - 1);
+    int rIdx = rx * (w + 1) + w;
+    int row = (uy < __ldg(&sc.envProb[rIdx])) ? rx : __ldg(&sc.envAlias[rIdx]);
+    int cx = min(zf2i((float)w * uz), w - 1);
+    int cIdx = row * (w + 1) + cx;
+    int col = (uw < __ldg(&sc.envProb[cIdx])) ? cx : __ldg(&sc.envAlias[cIdx]);
+    v2 uv = mk2((float)col + 0.5f, (float)row + 0.5f) / mk2((float)w, (float)h);
+    v3 wi = planeToSphere(uv);
+    wi = rotateZ(wi, sc.envRotation);
+    float pdf = envGetPortion(sc, wi) * (float)w * (float)h * 0.5f * sq(kPiInv);
+    Ray ray = rayOffseted(x, wi);
+    if (bvhTest(sc, ray, 1e8f) || pdf == 0.0f) return invalidLi();
+    return LiSample{wi, envLe(sc, wi) / pdf, pdf};
+}
+__device__ __forceinline__ float pdfSampleLightSel(const DeviceScene& sc, int uniform, float portion) {
+    return uniform ? portion : sc.lightSum / (sc.lightSum + sc.envSum);
+}
+
+// ---------------------------------------------------------------- camera.glsl
+__device__ __forceinline__ Ray thinLensCameraSampleRay(const DeviceScene& sc, v2 uv, float u0, float u1, float u2,
+                                                       float u3) {  // camera.glsl:62-77
+    v2 texel = mk2(1.0f / (float)sc.filmW, 1.0f / (float)sc.filmH);
+    v2 biased = uv + texel * mk2(u0, u1);
+    v2 ndc = mk2(biased.x * 2.0f - 1.0f, biased.y * 2.0f - 1.0f);
+    v2 lens = toConcentricDisk(mk2(u2, u3)) * sc.lensRadius;
+    v2 fp = ndc * mk2(sc.camAsp, 1.0f) * sc.focalDist * sc.tanFOV;
+    v3 dir = mk3(fp.x, fp.y, sc.focalDist) - mk3(lens.x, lens.y, 0.0f);
+    v3 R = f3(sc.camR), U = f3(sc.camU), F = f3(sc.camF);
+    dir = normalize(R * dir.x + U * dir.y + F * dir.z);
+    return Ray{f3(sc.camPos) + R * lens.x + U * lens.y, dir};
+}
+
+}  // namespace zgl

@@ -1,0 +1,261 @@
+"""Scene and integrator interfaces.
+
+``Scene`` mirrors ``Scene::createGLContext`` (src/core/Scene.cpp:133-270): it
+takes world-space object and light meshes, materials in the 64-byte
+``Material`` layout (src/core/Material.h:32-53), an optional environment image
+and the camera, and builds the sampling tables and device buffers through the
+C ABI.  ``PathIntegrator`` mirrors ``NaivePathIntegrator``
+(src/core/Integrator.h:68-91): ``render_one_pass``, ``reset``, ``get_frame``
+and ``result_scale``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import call
+
+LAMBERTIAN, PRINCIPLED, METAL_WORKFLOW, DIELECTRIC, THIN_DIELECTRIC = 0, 1, 2, 3, 4
+NO_TEXTURE = -1
+
+
+def material(type_: int = LAMBERTIAN, base_color=(1.0, 1.0, 1.0), roughness: float = 1.0, subsurface: float = 0.0,
+             metallic: float = 0.0, specular: float = 1.0, specular_tint: float = 1.0, sheen: float = 0.0,
+             sheen_tint: float = 1.0, clearcoat: float = 0.0, clearcoat_gloss: float = 0.0,
+             ior: float = 1.5) -> np.ndarray:
+    """One material record: 16 float32 in the layout of struct Material, with
+    the defaults of src/core/Material.h:32-53 (type stored as int32 bits)."""
+    rec = np.zeros(16, np.float32)
+    rec[0:3] = base_color
+    rec[3] = roughness
+    rec[4:8] = (subsurface, metallic, specular, specular_tint)
+    rec[8:12] = (sheen, sheen_tint, clearcoat, clearcoat_gloss)
+    rec[12] = ior
+    rec[13:14] = np.array([type_], np.int32).view(np.float32)
+    return rec
+
+
+def mat_tex(mat_index: int, tex_index: int = NO_TEXTURE) -> int:
+    """(texIndex << 16) | matIndex as stored per triangle (Scene.cpp:168)."""
+    return int(np.array([(tex_index << 16) | mat_index], np.int64).astype(np.int32)[0])
+
+
+def alias_table(pdf) -> tuple[np.ndarray, np.ndarray]:
+    """AliasTable::build<int32_t>(pdf) (src/math/AliasTable.h:12-54)."""
+    pdf = np.ascontiguousarray(pdf, np.float32)
+    alias = np.zeros(pdf.size, np.int32)
+    prob = np.zeros(pdf.size, np.float32)
+    call("zgl_alias_table_build", pdf.ctypes.data, pdf.size, alias.ctypes.data, prob.ctypes.data)
+    return alias, prob
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("obj_vertices", C.c_void_p), ("obj_n_vertices", C.c_size_t), ("obj_normals", C.c_void_p),
+        ("obj_indices", C.c_void_p), ("obj_n_triangles", C.c_size_t), ("obj_mat_tex", C.c_void_p),
+        ("materials", C.c_void_p), ("n_materials", C.c_size_t),
+        ("light_vertices", C.c_void_p), ("light_n_vertices", C.c_size_t), ("light_normals", C.c_void_p),
+        ("light_indices", C.c_void_p), ("light_n_triangles", C.c_size_t), ("light_first", C.c_void_p),
+        ("light_power", C.c_void_p), ("n_light_instances", C.c_size_t),
+        ("env_rgb", C.c_void_p), ("env_width", C.c_int32), ("env_height", C.c_int32), ("env_rotation", C.c_float),
+        ("cam_pos", C.c_float * 3), ("cam_angle", C.c_float * 3), ("cam_fov", C.c_float),
+        ("cam_lens_radius", C.c_float), ("cam_focal_dist", C.c_float),
+        ("film_width", C.c_int32), ("film_height", C.c_int32), ("sampler", C.c_int32),
+    ]
+
+
+class IntegratorParams(C.Structure):
+    _fields_ = [
+        ("max_depth", C.c_int32), ("russian_roulette", C.c_int32), ("rr_start_depth", C.c_int32),
+        ("sample_light", C.c_int32), ("light_env_uniform_sample", C.c_int32), ("light_portion", C.c_float),
+        ("finite_sample", C.c_int32), ("max_sample", C.c_int32),
+    ]
+
+
+def _f32(a, cols=3):
+    return np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1, cols))
+
+
+@dataclass
+class SceneData:
+    """World-space scene arrays (objects first, then lights), as flattened by
+    Scene::createGLContext."""
+
+    obj_vertices: np.ndarray
+    obj_normals: np.ndarray
+    obj_indices: np.ndarray
+    obj_mat_tex: np.ndarray
+    materials: np.ndarray            # (n, 16) float32
+    light_vertices: np.ndarray
+    light_normals: np.ndarray
+    light_indices: np.ndarray
+    light_first: np.ndarray          # uint32 offsets, n_instances + 1
+    light_power: np.ndarray          # (n_instances, 3)
+    film: tuple[int, int] = (256, 256)
+    cam_pos: tuple = (0.0, 0.0, 0.0)
+    cam_angle: tuple = (0.0, 0.0, 0.0)
+    cam_fov: float = 45.0
+    cam_lens_radius: float = 0.0
+    cam_focal_dist: float = 1.0
+    sampler: int = 1
+    env_rgb: np.ndarray | None = None  # (H, W, 3) float32
+    env_rotation: float = 0.0
+    _keep: list = field(default_factory=list, repr=False)
+
+    def normalized(self) -> "SceneData":
+        self.obj_vertices = _f32(self.obj_vertices)
+        self.obj_normals = _f32(self.obj_normals)
+        self.obj_indices = np.ascontiguousarray(np.asarray(self.obj_indices, np.uint32).reshape(-1))
+        self.obj_mat_tex = np.ascontiguousarray(np.asarray(self.obj_mat_tex, np.int32).reshape(-1))
+        self.materials = _f32(self.materials, 16)
+        self.light_vertices = _f32(self.light_vertices)
+        self.light_normals = _f32(self.light_normals)
+        self.light_indices = np.ascontiguousarray(np.asarray(self.light_indices, np.uint32).reshape(-1))
+        self.light_first = np.ascontiguousarray(np.asarray(self.light_first, np.uint32).reshape(-1))
+        self.light_power = _f32(self.light_power)
+        if self.env_rgb is not None:
+            self.env_rgb = np.ascontiguousarray(np.asarray(self.env_rgb, np.float32))
+        return self
+
+    def desc(self) -> SceneDesc:
+        self.normalized()
+        d = SceneDesc()
+        p = lambda a: a.ctypes.data if a is not None and a.size else None  # noqa: E731
+        d.obj_vertices, d.obj_n_vertices = p(self.obj_vertices), self.obj_vertices.shape[0]
+        d.obj_normals = p(self.obj_normals)
+        d.obj_indices, d.obj_n_triangles = p(self.obj_indices), self.obj_indices.size // 3
+        d.obj_mat_tex = p(self.obj_mat_tex)
+        d.materials, d.n_materials = p(self.materials), self.materials.shape[0]
+        d.light_vertices, d.light_n_vertices = p(self.light_vertices), self.light_vertices.shape[0]
+        d.light_normals = p(self.light_normals)
+        d.light_indices, d.light_n_triangles = p(self.light_indices), self.light_indices.size // 3
+        d.light_first = p(self.light_first)
+        d.light_power, d.n_light_instances = p(self.light_power), self.light_power.shape[0]
+        if self.env_rgb is not None:
+            d.env_rgb = self.env_rgb.ctypes.data
+            d.env_height, d.env_width = self.env_rgb.shape[0], self.env_rgb.shape[1]
+        d.env_rotation = self.env_rotation
+        d.cam_pos = (C.c_float * 3)(*self.cam_pos)
+        d.cam_angle = (C.c_float * 3)(*self.cam_angle)
+        d.cam_fov, d.cam_lens_radius, d.cam_focal_dist = self.cam_fov, self.cam_lens_radius, self.cam_focal_dist
+        d.film_width, d.film_height = self.film
+        d.sampler = self.sampler
+        return d
+
+    # flattened arrays (objects then lights), for checkers
+    def flat(self):
+        self.normalized()
+        nvo = self.obj_vertices.shape[0]
+        v = np.concatenate([self.obj_vertices, self.light_vertices]).astype(np.float32)
+        n = np.concatenate([self.obj_normals, self.light_normals]).astype(np.float32)
+        idx = np.concatenate([self.obj_indices, self.light_indices + np.uint32(nvo)]).astype(np.uint32)
+        return v, n, idx
+
+
+class Scene:
+    """Device-resident scene (owner of a ``zgl_scene`` handle)."""
+
+    TABLES = {
+        "light_power": np.float32, "light_alias": np.int32, "light_prob": np.float32, "env_alias": np.int32,
+        "env_prob": np.float32, "env_texels": np.float32, "sobol": np.uint32, "noise": np.float32,
+        "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32,
+    }
+
+    def __init__(self, data: SceneData, host_only: bool = False):
+        self.data = data
+        desc = data.desc()
+        h = C.c_void_p()
+        call("zgl_scene_create", C.byref(desc), 1 if host_only else 0, C.byref(h))
+        self._h = h
+        self.film = tuple(data.film)
+
+    def table_size(self, name: str) -> int:
+        d = self.data
+        nl = d.light_indices.size // 3
+        W, H = self.film
+        ew, eh = (d.env_rgb.shape[1], d.env_rgb.shape[0]) if d.env_rgb is not None else (0, 0)
+        return {
+            "light_power": nl * 3, "light_alias": nl, "light_prob": nl,
+            "env_alias": (ew + 1) * eh if ew else 0, "env_prob": (ew + 1) * eh if ew else 0,
+            "env_texels": ew * eh * 3, "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2,
+            "camera": 19, "scalars": 4,
+        }[name]
+
+    def export(self, name: str) -> np.ndarray:
+        out = np.empty(self.table_size(name), self.TABLES[name])
+        call("zgl_scene_export", self._h, name.encode(), out.ctypes.data if out.size else C.c_void_p(1),
+             out.nbytes)
+        return out
+
+    def close(self):
+        if self._h:
+            call("zgl_scene_destroy", self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+
+def default_params(**kw) -> IntegratorParams:
+    p = IntegratorParams()
+    call("zgl_integrator_params_default", C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class PathIntegrator:
+    """NaivePathIntegrator (src/core/Integrator.h:68-91) on the GPU."""
+
+    KIND = 0
+
+    def __init__(self, scene: Scene, params: IntegratorParams | None = None, **kw):
+        self.scene = scene
+        self.params = params or default_params(**kw)
+        h = C.c_void_p()
+        call("zgl_integrator_create", scene.handle, self.KIND, C.byref(self.params), C.byref(h))
+        self._h = h
+
+    def render_one_pass(self, stream=None) -> None:
+        from .accel import _stream_handle
+
+        call("zgl_integrator_render_pass", self._h, _stream_handle(stream))
+
+    def reset(self) -> None:
+        call("zgl_integrator_reset", self._h)
+
+    def get_frame(self, out=None, stream=None):
+        """(RGBA sum image (H, W, 4), samples)."""
+        from .accel import _ptr, _stream_handle
+
+        W, H = self.scene.film
+        if out is None:
+            out = np.empty((H, W, 4), np.float32)
+        spp = C.c_int32()
+        call("zgl_integrator_frame", self._h, _ptr(out), C.byref(spp), _stream_handle(stream))
+        return out, spp.value
+
+    def result_scale(self) -> float:
+        v = C.c_float()
+        call("zgl_integrator_result_scale", self._h, C.byref(v))
+        return v.value
+
+    def close(self):
+        if self._h:
+            call("zgl_integrator_destroy", self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

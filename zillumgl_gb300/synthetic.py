@@ -119,3 +119,121 @@ def incoherent_rays(vertices, indices, origins, dirs, hit_id, hit_t, seed: int):
 
 def shadow_tmax(n: int, seed: int) -> np.ndarray:
     return _rng(seed).random(n).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Cornell-style path-tracing scene
+# ---------------------------------------------------------------------------
+def _quad(p0, p1, p2, p3, n):
+    v = np.array([p0, p1, p2, p3], np.float64)
+    nn = np.tile(np.asarray(n, np.float64), (4, 1))
+    return v, nn, np.array([0, 1, 2, 0, 2, 3], np.int64)
+
+
+def _box(lo, hi):
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    faces = [
+        ((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1), (0, -1, 0)),
+        ((x1, y1, z0), (x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (0, 1, 0)),
+        ((x0, y1, z0), (x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (-1, 0, 0)),
+        ((x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1), (1, 0, 0)),
+        ((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1), (0, 0, 1)),
+        ((x0, y1, z0), (x1, y1, z0), (x1, y0, z0), (x0, y0, z0), (0, 0, -1)),
+    ]
+    return [_quad(*f) for f in faces]
+
+
+def _uv_sphere(center, radius, segments=32, rings=16):
+    c = np.asarray(center, np.float64)
+    verts, idx = [], []
+    for i in range(rings + 1):
+        th = np.pi * i / rings
+        for j in range(segments + 1):
+            ph = 2 * np.pi * j / segments
+            verts.append((np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)))
+    verts = np.array(verts)
+    row = segments + 1
+    for i in range(rings):
+        for j in range(segments):
+            a, b, cc, d = i * row + j, (i + 1) * row + j, (i + 1) * row + j + 1, i * row + j + 1
+            if i != 0:
+                idx += [a, b, d]
+            if i != rings - 1:
+                idx += [b, cc, d]
+    return c + radius * verts, verts.copy(), np.array(idx, np.int64)
+
+
+def cornell_scene(seed: int = 1, width: int = 256, height: int = 256, sampler: int = 1):
+    """Seeded Cornell-style box: 5 Lambertian walls with albedo U(0.2, 0.8)^3,
+    one area-light quad of power 15 under the ceiling, two axis-aligned boxes
+    and two 32x16 UV spheres (about 2k triangles); one sphere carries the only
+    principled material (roughness U(0.1, 0.9), metallic in {0, 1}).  Z is up,
+    the camera looks along +y into the open side of the box."""
+    from .scene import LAMBERTIAN, PRINCIPLED, SceneData, mat_tex, material
+
+    rng = np.random.default_rng(seed)
+    mats, parts = [], []  # parts: (verts, normals, idx, material index)
+
+    def add(mesh_list, mat_rec):
+        mats.append(mat_rec)
+        m = len(mats) - 1
+        for v, n, i in mesh_list:
+            parts.append((v, n, i, m))
+
+    walls = [
+        ((-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0), (0, 0, 1)),      # floor
+        ((-1, 1, 2), (1, 1, 2), (1, -1, 2), (-1, -1, 2), (0, 0, -1)),     # ceiling
+        ((-1, 1, 0), (1, 1, 0), (1, 1, 2), (-1, 1, 2), (0, -1, 0)),       # back
+        ((-1, -1, 0), (-1, 1, 0), (-1, 1, 2), (-1, -1, 2), (1, 0, 0)),    # left
+        ((1, 1, 0), (1, -1, 0), (1, -1, 2), (1, 1, 2), (-1, 0, 0)),       # right
+    ]
+    for w in walls:
+        add([_quad(*w)], material(LAMBERTIAN, base_color=rng.uniform(0.2, 0.8, 3)))
+    add(_box((-0.65, 0.15, 0.0), (-0.15, 0.65, 1.2)), material(LAMBERTIAN, base_color=rng.uniform(0.2, 0.8, 3)))
+    add(_box((0.125, -0.575, 0.0), (0.575, -0.125, 0.45)), material(LAMBERTIAN, base_color=rng.uniform(0.2, 0.8, 3)))
+    add([_uv_sphere((-0.45, -0.45, 0.3), 0.3)],
+        material(PRINCIPLED, base_color=rng.uniform(0.2, 0.8, 3), roughness=rng.uniform(0.1, 0.9),
+                 metallic=float(rng.integers(0, 2))))
+    add([_uv_sphere((0.5, 0.5, 0.25), 0.25)], material(LAMBERTIAN, base_color=rng.uniform(0.2, 0.8, 3)))
+
+    ov, on, oi, om = [], [], [], []
+    base = 0
+    for v, n, i, m in parts:
+        ov.append(v)
+        on.append(n)
+        oi.append(i + base)
+        om += [mat_tex(m)] * (i.size // 3)
+        base += v.shape[0]
+    lv, ln, li = _quad((-0.3, -0.3, 1.98), (0.3, -0.3, 1.98), (0.3, 0.3, 1.98), (-0.3, 0.3, 1.98), (0, 0, -1))
+    return SceneData(
+        obj_vertices=np.concatenate(ov), obj_normals=np.concatenate(on), obj_indices=np.concatenate(oi),
+        obj_mat_tex=np.array(om, np.int32), materials=np.stack(mats),
+        light_vertices=lv, light_normals=ln, light_indices=li, light_first=np.array([0, 2], np.uint32),
+        light_power=np.array([[15.0, 15.0, 15.0]]), film=(width, height), cam_pos=(0.0, -3.4, 1.0),
+        cam_angle=(0.0, 0.0, 0.0), cam_fov=40.0, cam_lens_radius=0.0, cam_focal_dist=1.0, sampler=sampler,
+    ).normalized()
+
+
+def sky_environment(width: int, height: int, seed: int = 2, sun_dir=(0.4, -0.3, 0.866), peak_over_mean=1e3):
+    """Procedural equirectangular environment (rows = polar angle from +z):
+    a sky gradient plus a Gaussian sun lobe scaled so that peak/mean is about
+    `peak_over_mean`.  Returns float32 (height, width, 3)."""
+    rng = np.random.default_rng(seed)
+    v = (np.arange(height) + 0.5) / height
+    u = (np.arange(width) + 0.5) / width
+    phi = np.pi * v[:, None]
+    theta = 2 * np.pi * u[None, :]
+    d = np.stack([np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi) * np.ones_like(theta)], -1)
+    up = np.clip(d[..., 2], -1, 1)
+    sky = np.stack([0.3 + 0.2 * up, 0.45 + 0.25 * up, 0.7 + 0.3 * up], -1)
+    sky = np.clip(sky, 0.02, None) * (1.0 + 0.02 * rng.standard_normal(sky.shape[:2]))[..., None]
+    s = np.asarray(sun_dir, np.float64)
+    s = s / np.linalg.norm(s)
+    lobe = np.exp((d @ s - 1.0) / 0.0004)
+    sky_mean = sky.mean()
+    img = sky + lobe[..., None] * np.array([1.0, 0.95, 0.85])
+    peak = img.max()
+    scale = (peak_over_mean * img.mean() - sky_mean) if peak > 0 else 0.0
+    img = sky + lobe[..., None] * np.array([1.0, 0.95, 0.85]) * max(scale, 1.0)
+    return np.clip(img, 0.0, None).astype(np.float32)
