@@ -112,6 +112,22 @@ zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const f
                            const float* tmax, size_t n, int32_t any_hit,
                            int32_t* visits, int32_t* tests, void* stream);
 
+/* Allocation-free variant of zgl_trace_closest, for callers that must not
+ * let the library allocate device memory (a frame loop under a fixed memory
+ * budget, or an application whose own pool allocator owns the device).  No
+ * counterpart in the reference.  The kernel's scratch (the persistent work
+ * counter) and the staging area for host arrays live in one static device
+ * array of 8 MiB + 256 B that every GPU loading the library holds until the
+ * process exits; the call makes no cudaMalloc or cudaFree.  n is limited to
+ * 262144 rays per call (larger n returns ZGL_ERR_INVALID_ARG); arrays may be
+ * host or device memory, as for zgl_trace_closest.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make that first call before any stream capture.  All calls
+ * share the array: calls whose GPU work overlaps (other streams, other host
+ * threads) race on it and must be serialised by the caller. */
+zgl_status zgl_trace_closest_noalloc(const zgl_accel* accel, const float* origins, const float* dirs,
+                                     size_t n, int32_t* hit_id, float* hit_t, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Scene: flattened geometry, materials, lights, environment, camera         */
 /* ------------------------------------------------------------------------ */

@@ -56,6 +56,8 @@ SIGNATURES: dict[str, tuple] = {
                                   C.c_void_p]),
     "zgl_trace_count": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int32,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_trace_closest_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                              C.c_void_p, C.c_void_p]),
     "zgl_scene_create": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "zgl_scene_export": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_size_t]),
     "zgl_scene_destroy": (C.c_int32, [C.c_void_p]),

@@ -134,6 +134,18 @@ class Accelerator:
              _stream_handle(stream))
         return hit_id, hit_t
 
+    def trace_closest_noalloc(self, origins, dirs, hit_id=None, hit_t=None, stream=None):
+        """bvhHit through the allocation-free entry point (at most 262144 rays;
+        the library allocates no device memory for the call)."""
+        n = _check_rays(origins, dirs)
+        if hit_id is None:
+            hit_id = _like(origins, (n,), np.int32, torch.int32 if torch else None)
+        if hit_t is None:
+            hit_t = _like(origins, (n,), np.float32, torch.float32 if torch else None)
+        call("zgl_trace_closest_noalloc", self._h, _ptr(origins), _ptr(dirs), n, _ptr(hit_id), _ptr(hit_t),
+             _stream_handle(stream))
+        return hit_id, hit_t
+
     def trace_any(self, origins, dirs, tmax, occluded=None, stream=None):
         """bvhTest: 1 where some triangle lies at 0 < t < tmax."""
         n = _check_rays(origins, dirs)

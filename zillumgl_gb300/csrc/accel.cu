@@ -2,6 +2,7 @@
 // the zgl_accel_* and zgl_trace_* entry points.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -515,6 +516,93 @@ zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const f
                                 (const float*)st.ptr(sm), (int64_t)n, any_hit, (int32_t*)st.ptr(sv),
                                 (int32_t*)st.ptr(sx), s));
     st.finish();
+    ZGL_API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free closest-hit tracing.
+//
+// Some callers cannot let a library call cudaMalloc: a renderer that runs a
+// frame loop under a fixed device-memory budget, or that hands all device
+// memory to its own pool allocator, cannot afford an allocation that may fail
+// mid-frame or that synchronises the whole device.  zgl_trace_closest_noalloc
+// serves them: the persistent trace kernel's scratch (its work counter) and
+// the staging area for host arrays live in one file-scope device array that
+// the library holds from the moment it is loaded until the process exits, on
+// every GPU that loads it.
+// ---------------------------------------------------------------------------
+namespace zgl {
+namespace {
+
+constexpr size_t kNoAllocMaxRays = size_t(1) << 18;  // 262144 rays per call
+constexpr size_t kNoAllocHeader = 256;               // work counter
+constexpr size_t kNoAllocOrigins = kNoAllocHeader;
+constexpr size_t kNoAllocDirs = kNoAllocOrigins + 12 * kNoAllocMaxRays;
+constexpr size_t kNoAllocIds = kNoAllocDirs + 12 * kNoAllocMaxRays;
+constexpr size_t kNoAllocDist = kNoAllocIds + 4 * kNoAllocMaxRays;
+constexpr size_t kNoAllocBytes = kNoAllocDist + 4 * kNoAllocMaxRays;  // 8 MiB + 256 B
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// The array's name in host code is only a host-side handle, not a device
+// address: the device address is looked up once per device, with that device
+// current, and cached.
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+unsigned char* noalloc_scratch(int device) {
+    if (device < 0 || device >= 256) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest_noalloc: device %d", device);
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            fail(ZGL_ERR_CUDA, "zgl_trace_closest_noalloc: cudaGetSymbolAddress failed: %s",
+                 cudaGetErrorString(e));
+        }
+        g_noalloc_addr[device] = p;
+    }
+    return static_cast<unsigned char*>(g_noalloc_addr[device]);
+}
+
+}  // namespace
+}  // namespace zgl
+
+extern "C" {
+
+zgl_status zgl_trace_closest_noalloc(const zgl_accel* accel, const float* origins, const float* dirs, size_t n,
+                                     int32_t* hit_id, float* hit_t, void* stream) {
+    ZGL_API_BEGIN
+    if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest_noalloc: NULL accel");
+    if (n == 0) return ZGL_OK;
+    if (!origins || !dirs || !hit_id || !hit_t) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest_noalloc: NULL array");
+    if (n > kNoAllocMaxRays)
+        fail(ZGL_ERR_INVALID_ARG,
+             "zgl_trace_closest_noalloc: %zu rays exceed the allocation-free limit of %zu rays per call", n,
+             kNoAllocMaxRays);
+    DeviceGuard dg(accel->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char* base = noalloc_scratch(accel->device);
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(base);
+    const bool ho = !is_device_ptr(origins), hd = !is_device_ptr(dirs);
+    const bool hi = !is_device_ptr(hit_id), ht = !is_device_ptr(hit_t);
+    const float* d_org = ho ? reinterpret_cast<const float*>(base + kNoAllocOrigins) : origins;
+    const float* d_dir = hd ? reinterpret_cast<const float*>(base + kNoAllocDirs) : dirs;
+    int32_t* d_id = hi ? reinterpret_cast<int32_t*>(base + kNoAllocIds) : hit_id;
+    float* d_t = ht ? reinterpret_cast<float*>(base + kNoAllocDist) : hit_t;
+    if (ho) ZGL_CUDA(cudaMemcpyAsync(base + kNoAllocOrigins, origins, 12 * n, cudaMemcpyHostToDevice, s));
+    if (hd) ZGL_CUDA(cudaMemcpyAsync(base + kNoAllocDirs, dirs, 12 * n, cudaMemcpyHostToDevice, s));
+    // the persistent schedule with its counter in the static array (reset here:
+    // the array keeps the previous call's contents); an empty accelerator
+    // takes the counter-free kernel
+    ZGL_CUDA(launch_trace_closest(device_view(accel), d_org, d_dir, (int64_t)n, d_id, d_t,
+                                  accel->M > 0 ? counter : nullptr, s));
+    if (hi) ZGL_CUDA(cudaMemcpyAsync(hit_id, d_id, 4 * n, cudaMemcpyDeviceToHost, s));
+    if (ht) ZGL_CUDA(cudaMemcpyAsync(hit_t, d_t, 4 * n, cudaMemcpyDeviceToHost, s));
+    if (ho || hd || hi || ht) ZGL_CUDA(cudaStreamSynchronize(s));
     ZGL_API_END
 }
 
