@@ -208,11 +208,21 @@ zgl_status zgl_alias_table_build(const float* pdf, size_t n, int32_t* alias, flo
 
 typedef struct zgl_integrator zgl_integrator;
 
-enum { ZGL_INTEGRATOR_PATH = 0 };
+/* ZGL_INTEGRATOR_PATH: NaivePathIntegrator (path_integ_naive.glsl);
+ * ZGL_INTEGRATOR_LIGHT: LightPathIntegrator, the particle tracer
+ * (light_path_integ.glsl, LightPath.cpp); ZGL_INTEGRATOR_TRIPLE:
+ * TriplePathIntegrator, the MIS-weighted (s=0)+(s=1)+(t=1) integrator
+ * (triple_path_pass_{pt,lpt}.glsl, TriplePath.cpp).  The light and triple
+ * integrators need at least one light triangle. */
+enum { ZGL_INTEGRATOR_PATH = 0, ZGL_INTEGRATOR_LIGHT = 1, ZGL_INTEGRATOR_TRIPLE = 2 };
 
-/* Parameters of PathIntegParam (src/core/Integrator.h:56-66) plus
- * rr_start_depth: Russian roulette runs from this bounce on (1 = every
- * bounce, the reference's behaviour). */
+/* Parameters of PathIntegParam / LightPathIntegParam / TriplePathIntegParam
+ * (src/core/Integrator.h:56-143) plus rr_start_depth: Russian roulette runs
+ * from this bounce on (1 = every bounce, the reference's behaviour).
+ * blocks_per_pass: light paths per pass are blocks_per_pass x 1536 (0 = the
+ * reference default, 32 for the light tracer and 64 for the triple
+ * integrator); loops_per_pass: light paths per thread of the triple
+ * integrator (LPTLoopsPerPass, 1). */
 typedef struct zgl_integrator_params {
     int32_t max_depth;                /* 4 */
     int32_t russian_roulette;         /* 0 */
@@ -222,6 +232,8 @@ typedef struct zgl_integrator_params {
     float light_portion;              /* 0.5 */
     int32_t finite_sample;            /* 0 */
     int32_t max_sample;               /* 64 */
+    int32_t blocks_per_pass;          /* 0 = kind default */
+    int32_t loops_per_pass;           /* 1 */
 } zgl_integrator_params;
 
 /* Fill the reference defaults. */
@@ -246,8 +258,10 @@ zgl_status zgl_integrator_reset(zgl_integrator* integ);
  * Synchronous for host memory. */
 zgl_status zgl_integrator_frame(zgl_integrator* integ, float* out, int32_t* spp, void* stream);
 
-/* Integrator::resultScale (Integrator.h:79): 1 / (samples + 1) for the path
- * tracer (the reference's display scale; divide the sum by spp for the mean). */
+/* Integrator::resultScale: 1 / (samples + 1) for the path tracer
+ * (Integrator.h:79) and 1 / samplePerPixel for the light and triple
+ * integrators (Integrator.h:114, :156), with the reference's bookkeeping of
+ * samplePerPixel (LightPath.cpp:113-134, TriplePath.cpp:303-322). */
 zgl_status zgl_integrator_result_scale(const zgl_integrator* integ, float* out);
 
 zgl_status zgl_integrator_destroy(zgl_integrator* integ);

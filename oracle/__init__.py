@@ -137,6 +137,11 @@ def _render_lib():
         L.orc_render_pt.restype = None
         L.orc_render_pt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                     C.c_void_p, C.c_int32]
+        L.orc_render_lt.restype = None
+        L.orc_render_lt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
+        L.orc_render_triple.restype = None
+        L.orc_render_triple.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_void_p]
         L.orc_alias_build.restype = None
         L.orc_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.orc_transc.restype = None
@@ -272,3 +277,17 @@ class OracleScene:
         _render_lib().orc_render_pt(C.byref(self.s), spp0, passes, fc0, _p(pix), pix.size, _p(out),
                                     nthreads or threads())
         return out
+
+    def render_lt(self, passes, blocks=32, spp0=0, fc0=1):
+        """Film sum (H, W, 3) of `passes` light-tracer passes."""
+        W, H = self.s.filmW, self.s.filmH
+        film = np.zeros((H, W, 3), np.float32)
+        _render_lib().orc_render_lt(C.byref(self.s), spp0, passes, fc0, blocks, _p(film))
+        return film
+
+    def render_triple(self, passes, blocks=64, loops=1, spp0=0, fc0=1):
+        """Film sum (H, W, 3) of `passes` triple-integrator passes."""
+        W, H = self.s.filmW, self.s.filmH
+        film = np.zeros((H, W, 3), np.float32)
+        _render_lib().orc_render_triple(C.byref(self.s), spp0, passes, fc0, blocks, loops, _p(film))
+        return film

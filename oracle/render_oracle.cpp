@@ -732,6 +732,383 @@ vec3 pathIntegTrace(const OrcScene& sc, Ray ray, int& s, Rng& g) {  // :35-143
     return result;
 }
 
+// ---------------------------------------------- camera importance (camera.glsl)
+inline bool inFilmBound(vec2 uv) { return uv.x >= 0.0f && uv.x <= 1.0f && uv.y >= 0.0f && uv.y <= 1.0f; }
+inline bool thinLensCameraDelta(const OrcScene& sc) { return sc.lensRadius <= 1e-6f; }
+inline vec2 thinLensCameraRasterPos(const OrcScene& sc, const Ray& ray) {  // camera.glsl:79-91
+    float cosTheta = dot(ray.dir, cv(sc.camF));
+    float dFocus = sc.focalDist / cosTheta;
+    mat3 inv{vec3(sc.camMatInv[0], sc.camMatInv[1], sc.camMatInv[2]),
+             vec3(sc.camMatInv[3], sc.camMatInv[4], sc.camMatInv[5]),
+             vec3(sc.camMatInv[6], sc.camMatInv[7], sc.camMatInv[8])};
+    vec3 pFocus = mul(inv, rayPoint(ray, dFocus) - cv(sc.camPos));
+    vec2 filmSize((float)sc.filmW, (float)sc.filmH);
+    float aspect = filmSize.x / filmSize.y;
+    vec3 div = vec3(aspect * sc.tanFOV * sc.focalDist, 1.0f * sc.tanFOV * sc.focalDist, 1.0f * sc.focalDist);
+    pFocus = pFocus / div;
+    return vec2((pFocus.x + 1.0f) * 0.5f, (pFocus.y + 1.0f) * 0.5f);
+}
+inline vec3 thinLensCameraIe(const OrcScene& sc, const Ray& ray) {  // camera.glsl:93-107
+    float cosTheta = dot(ray.dir, cv(sc.camF));
+    if (cosTheta < 1e-6f) return vec3(0.0f);
+    vec2 pRaster = thinLensCameraRasterPos(sc, ray);
+    if (!inFilmBound(pRaster)) return vec3(0.0f);
+    float tanFOVInv = 1.0f / sc.tanFOV;
+    float cos2Theta = cosTheta * cosTheta;
+    float lensArea = thinLensCameraDelta(sc) ? 1.0f : Pi * sc.lensRadius * sc.lensRadius;
+    return vec3(0.25f) * square(tanFOVInv / cos2Theta) / (lensArea * sc.camAsp);
+}
+struct CameraIiSample {
+    vec3 wi, Ii;
+    float dist;
+    vec2 uv;
+    float pdf;
+};
+inline CameraIiSample thinLensCameraSampleIi(const OrcScene& sc, vec3 ref, vec2 u) {  // camera.glsl:109-127
+    vec2 l = toConcentricDisk(u) * sc.lensRadius;
+    vec3 pLens(l.x, l.y, 0.0f);
+    vec3 y = cv(sc.camPos) + cv(sc.camR) * pLens.x + cv(sc.camU) * pLens.y + cv(sc.camF) * pLens.z;
+    float dist = distance(ref, y);
+    vec3 wi = normalize(y - ref);
+    float cosTheta = satDot(cv(sc.camF), -wi);
+    if (cosTheta < 1e-6f) return CameraIiSample{vec3(0.0f), vec3(0.0f), 0.0f, vec2(0.0f), 0.0f};
+    Ray ray{y, -wi};
+    vec3 Ie = thinLensCameraIe(sc, ray);
+    vec2 uv = thinLensCameraRasterPos(sc, ray);
+    float lensArea = thinLensCameraDelta(sc) ? 1.0f : Pi * sc.lensRadius * sc.lensRadius;
+    float pdf = dist * dist / (cosTheta * lensArea);
+    return CameraIiSample{wi, Ie, dist, uv, pdf};
+}
+struct CamPdf {
+    float pdfPos, pdfDir;
+};
+inline CamPdf thinLensCameraPdfIe(const OrcScene& sc, const Ray& ray) {  // camera.glsl:129-141
+    float cosTheta = dot(cv(sc.camF), ray.dir);
+    if (cosTheta < 1e-6f) return CamPdf{0.0f, 0.0f};
+    vec2 pRaster = thinLensCameraRasterPos(sc, ray);
+    if (!inFilmBound(pRaster)) return CamPdf{0.0f, 0.0f};
+    float pdfPos = thinLensCameraDelta(sc) ? 1.0f : 1.0f / (Pi * sc.lensRadius * sc.lensRadius);
+    float pdfDir = 1.0f / (cosTheta * cosTheta * cosTheta);
+    return CamPdf{pdfPos, pdfDir};
+}
+
+// ------------------------------------------------------- light emission (light.glsl)
+struct LightLeSample {
+    Ray ray;
+    vec3 Le;
+    float pdfPos, pdfDir;
+};
+inline LightLeSample lightSampleOneLe(const OrcScene& sc, int id, float u0, float u1, float u2, float u3) {
+    int triId = id + sc.objPrimCount;  // light.glsl:111-120
+    vec3 ori = triangleSampleUniform(sc, triId, vec2(u0, u1));
+    vec3 norm = triangleSurfaceInfo(sc, triId, ori).ng;
+    vec4r samp = sampleCosineWeighted(norm, vec2(u2, u3));
+    return LightLeSample{rayOffseted(ori, samp.v), lightLe(sc, id, ori, samp.v), 1.0f / triangleArea(sc, triId), samp.w};
+}
+inline CamPdf lightPdfLe(const OrcScene& sc, int id, const Ray& ray) {  // light.glsl:100-109
+    int triId = id + sc.objPrimCount;
+    vec3 norm = triangleSurfaceInfo(sc, triId, ray.ori).ng;
+    CamPdf r;
+    r.pdfPos = 1.0f / triangleArea(sc, triId);
+    r.pdfDir = (dot(norm, ray.dir) <= 0.0f) ? 0.0f : 0.5f * PiInv;
+    return r;
+}
+inline vec3 triangleNormalShad(const OrcScene& sc, int id, vec3 p) {  // intersection.glsl:149-173
+    uint32_t ia = sc.indices[3 * id], ib = sc.indices[3 * id + 1], ic = sc.indices[3 * id + 2];
+    vec3 a = V(sc, ia), b = V(sc, ib), c = V(sc, ic);
+    vec3 pa = a - p, pb = b - p, pc = c - p;
+    float areaInv = 1.0f / length(cross(b - a, c - a));
+    float la = length(cross(pb, pc)) * areaInv;
+    float lb = length(cross(pc, pa)) * areaInv;
+    float lc = 1.0f - la - lb;
+    return normalize(N(sc, ia) * la + N(sc, ib) * lb + N(sc, ic) * lc);
+}
+inline bool visibleOrc(const OrcScene& sc, vec3 x, vec3 y) {  // intersection.glsl:429-433
+    float dist = distance(x, y) - 2e-5f;
+    vec3 wi = normalize(y - x);
+    return !bvhTest(sc, Ray{x + wi * 1e-5f, wi}, dist);
+}
+inline float remap(float p) { return p < 1e-8f ? 1.0f : p * p; }
+
+// Film of the light-tracing passes: float[H][W][3]; samples outside the film
+// (or on its far edge, where int(uv * size) == size) are dropped like an
+// out-of-range imageAtomicAdd.
+inline void accumulateFilm(const OrcScene& sc, float* film, vec2 uv, vec3 res) {
+    if (!inFilmBound(uv)) return;
+    int x = f2i(uv.x * (float)sc.filmW), y = f2i(uv.y * (float)sc.filmH);
+    if (x >= sc.filmW || y >= sc.filmH) return;
+    float* p = film + 3 * ((size_t)y * sc.filmW + x);
+    p[0] += res.x;
+    p[1] += res.y;
+    p[2] += res.z;
+}
+
+inline void loadSurface(const OrcScene& sc, int id, vec3 pos, vec3 wo, SurfaceInfo& surf, uint32_t& matType,
+                        BSDFParam& mp) {
+    surf = triangleSurfaceInfo(sc, id, pos);
+    int matId = sc.matTexIndex[id] & 0x0000ffff;
+    matType = loadMaterialType(sc, matId);
+    if (matType != Dielectric && matType != ThinDielectric && dot(surf.ns, wo) < 0.0f) {
+        surf.ns = -surf.ns;
+        surf.ng = -surf.ng;
+    }
+    mp = loadMaterial(sc, matType, matId);
+}
+
+// lightIntegTrace (light_path_integ.glsl:45-146); rand() stream only.
+void lightIntegTrace(const OrcScene& sc, Rng& g, float* film) {
+    float a0 = rand01(g), a1 = rand01(g);
+    int light = lightSampleOne(sc, vec2(a0, a1));
+    float pdfSource = lightPdfSampleOne(sc, light);
+    Ray ray;
+    vec3 wo, throughput;
+    {
+        int triId = light + sc.objPrimCount;
+        float b0 = rand01(g), b1 = rand01(g);
+        vec3 pLit = triangleSampleUniform(sc, triId, vec2(b0, b1));
+        float c0 = rand01(g), c1 = rand01(g);
+        CameraIiSample ci = thinLensCameraSampleIi(sc, pLit, vec2(c0, c1));
+        if (ci.pdf > 0.0f) {
+            vec3 pCam = pLit + ci.wi * ci.dist;
+            float pdfPos = 1.0f / triangleArea(sc, triId);
+            if (visibleOrc(sc, pLit, pCam)) {
+                vec3 Le = lightLe(sc, light, pLit, ci.wi);
+                vec3 contrib = Le * ci.Ii / (ci.pdf * pdfPos * pdfSource);
+                if (!isBlack(contrib)) accumulateFilm(sc, film, ci.uv, contrib);
+            }
+        }
+        float d0 = rand01(g), d1 = rand01(g), d2 = rand01(g), d3 = rand01(g);
+        LightLeSample le = lightSampleOneLe(sc, light, d0, d1, d2, d3);
+        vec3 nl = triangleSurfaceInfo(sc, triId, le.ray.ori).ng;
+        wo = -le.ray.dir;
+        ray = rayOffseted(le.ray.ori, le.ray.dir);
+        throughput = le.Le * absDot(nl, -wo) / (pdfSource * le.pdfPos * le.pdfDir);
+    }
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        float dist;
+        int id = bvhHit(sc, ray, dist);
+        if (id == -1) break;
+        if (id - sc.objPrimCount >= 0) break;
+        vec3 pos = rayPoint(ray, dist);
+        SurfaceInfo surf;
+        uint32_t matType;
+        BSDFParam mp;
+        loadSurface(sc, id, pos, wo, surf, matType, mp);
+        {
+            float c0 = rand01(g), c1 = rand01(g);
+            CameraIiSample ci = thinLensCameraSampleIi(sc, pos, vec2(c0, c1));
+            if (ci.pdf > 0.0f) {
+                vec3 pCam = pos + ci.wi * ci.dist;
+                if (visibleOrc(sc, pos, pCam)) {
+                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    float cosWi = satDot(surf.ng, ci.wi) * std::fabs(dot(surf.ns, wo) / dot(surf.ng, wo));
+                    vec3 res = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
+                    if (!hasNan(res) && !std::isnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
+                        accumulateFilm(sc, film, ci.uv, res);
+                }
+            }
+        }
+        float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
+        if (bsdfPdf < 1e-8f || std::isnan(bsdfPdf)) break;
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bs.bsdf / bsdfPdf), 1.0f);
+            if (rand01(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float cosWi = deltaBsdf ? 1.0f : std::fabs(dot(surf.ng, wi) * dot(surf.ns, wo) / dot(surf.ng, wo));
+        throughput = throughput * (bs.bsdf * cosWi / bsdfPdf);
+        ray = rayOffseted(pos, wi);
+        wo = -wi;
+    }
+}
+
+inline float weightS0(float s1s0, float t1s0) { return 1.0f / (1.0f + s1s0 + t1s0); }
+inline float weightS1(float s1s0, float t1s1) { return s1s0 / (1.0f + s1s0 + s1s0 * t1s1); }
+inline float weightT1(float s0t1, float s1t1) { return 1.0f / (s0t1 + s1t1 + 1.0f); }
+
+// traceCameraPath (triple_path_pass_pt.glsl:59-195)
+vec3 traceCameraPath(const OrcScene& sc, Ray ray, Rng& g, int& s) {
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    vec3 pos = rayPoint(ray, primDist);
+    if (id == -1) return envLe(sc, ray.dir);
+    if (id - sc.objPrimCount >= 0) return lightLe(sc, id - sc.objPrimCount, pos, -ray.dir);
+    SurfaceInfo surf = triangleSurfaceInfo(sc, id, pos);
+    vec3 wo = -ray.dir;
+    vec3 prevNorm = cv(sc.camF);
+    vec3 result(0.0f), throughput(1.0f);
+    CamPdf camPdf = thinLensCameraPdfIe(sc, ray);
+    float primaryPdf = remap(camPdf.pdfPos) / remap(camPdf.pdfDir * absDot(surf.ns, ray.dir) / square(primDist));
+    float t1s0 = primaryPdf, t1s1 = primaryPdf;
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        if (bounce > 1) surf = triangleSurfaceInfo(sc, id, pos);
+        int matId = sc.matTexIndex[id] & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != Dielectric && matType != ThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        {
+            float a0 = sample1D(sc, g, s), a1 = sample1D(sc, g, s);
+            int light = lightSampleOne(sc, vec2(a0, a1));
+            int triId = light + sc.objPrimCount;
+            float pdfSource = lightPdfSampleOne(sc, light);
+            float b0 = sample1D(sc, g, s), b1 = sample1D(sc, g, s);
+            vec3 pLit = triangleSampleUniform(sc, triId, vec2(b0, b1));
+            vec3 wi = normalize(pLit - pos);
+            vec3 Le = lightLe(sc, light, pLit, -wi);
+            if (!isBlack(Le) && visibleOrc(sc, pos, pLit)) {
+                vec3 nLit = triangleSurfaceInfo(sc, triId, pLit).ng;
+                float pA = pdfSource / triangleArea(sc, triId);
+                float dist2 = distSquare(pos, pLit);
+                float pS = pA * dist2 / absDot(nLit, wi);
+                vec3 f = materialBSDF(matType, mp, wo, wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, wi, surf.ns);
+                float pdfRev = materialPdf(matType, mp, wi, wo, surf.ns);
+                float pdfPLit = remap(pA);
+                float coefToSurf = remap(0.5f * PiInv * absDot(surf.ns, wi));
+                float coefToLight = remap(fpdf * satDot(nLit, -wi));
+                float coefToPrev = (bounce == 1) ? 1.0f : remap(pdfRev * absDot(prevNorm, wo));
+                float coefDist = remap(dist2);
+                float weight = weightS1(pdfPLit * coefDist / coefToLight, t1s1 * coefToSurf * coefToPrev / coefDist);
+                result = result + Le * f * throughput * absDot(surf.ns, wi) / pS * weight;
+            }
+        }
+        float b0 = sample1D(sc, g, s), b1 = sample1D(sc, g, s), b2 = sample1D(sc, g, s);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        Ray nextRay = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, nextRay, dist);
+        int lightId = nextId - sc.objPrimCount;
+        vec3 nextPos = rayPoint(nextRay, dist);
+        float pdfDirToNext = materialPdf(matType, mp, wo, wi, surf.ns);
+        float pdfDirToPrev = materialPdf(matType, mp, wi, wo, surf.ns);
+        if (nextId == -1) break;
+        if (lightId >= 0) {
+            vec3 nLit = triangleSurfaceInfo(sc, nextId, nextPos).ng;
+            CamPdf pdfLit = lightPdfLe(sc, lightId, Ray{nextPos, -wi});
+            float pdfPLit = remap(pdfLit.pdfPos * lightPdfSampleOne(sc, lightId));
+            float coefToLight = remap(pdfDirToNext * satDot(nLit, -wi));
+            float coefToSurf = remap(pdfLit.pdfDir * absDot(surf.ns, wi));
+            float coefToPrev = (bounce == 1) ? 1.0f : remap(pdfDirToPrev * absDot(prevNorm, wo));
+            float coefDist = remap(dist * dist);
+            float weight = std::isnan(t1s0) ? 0.0f
+                                            : weightS0(pdfPLit * coefDist / coefToLight,
+                                                       t1s0 * coefToSurf * pdfPLit * coefToPrev / coefToLight);
+            result = result + lightLe(sc, lightId, nextPos, -wi) * throughput * weight;
+            break;
+        }
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+            if (sample1D(sc, g, s) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float coef = ((bounce == 1) ? 1.0f : remap(pdfDirToPrev * absDot(prevNorm, wo))) /
+                     remap(pdfDirToNext * absDot(triangleNormalShad(sc, nextId, nextPos), wi));
+        t1s0 *= coef;
+        t1s1 *= coef;
+        prevNorm = surf.ns;
+        pos = nextPos;
+        wo = -wi;
+        id = nextId;
+    }
+    return result;
+}
+
+// traceLightPath (triple_path_pass_lpt.glsl:58-182); contributions scaled by uScale.
+void traceLightPath(const OrcScene& sc, Rng& g, float* film, float uScale) {
+    float a0 = rand01(g), a1 = rand01(g);
+    int light = lightSampleOne(sc, vec2(a0, a1));
+    float pdfSource = lightPdfSampleOne(sc, light);
+    Ray ray;
+    vec3 wo, throughput, prevNorm;
+    float prevPdfDir, s0t1, s1t1;
+    {
+        int triId = light + sc.objPrimCount;
+        float b0 = rand01(g), b1 = rand01(g);
+        (void)triangleSampleUniform(sc, triId, vec2(b0, b1));  // computed and unused by the reference
+        float d0 = rand01(g), d1 = rand01(g), d2 = rand01(g), d3 = rand01(g);
+        LightLeSample le = lightSampleOneLe(sc, light, d0, d1, d2, d3);
+        vec3 nl = triangleSurfaceInfo(sc, triId, le.ray.ori).ng;
+        wo = -le.ray.dir;
+        ray = rayOffseted(le.ray.ori, le.ray.dir);
+        throughput = le.Le * absDot(nl, -wo) / (pdfSource * le.pdfPos * le.pdfDir);
+        prevNorm = nl;
+        prevPdfDir = le.pdfDir;
+        s0t1 = 1.0f / remap(le.pdfPos * pdfSource);
+        s1t1 = 1.0f;
+    }
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        float dist;
+        int id = bvhHit(sc, ray, dist);
+        if (id == -1) break;
+        if (id - sc.objPrimCount >= 0) break;
+        vec3 pos = rayPoint(ray, dist);
+        SurfaceInfo surf = triangleSurfaceInfo(sc, id, pos);
+        int matId = sc.matTexIndex[id] & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != Dielectric && matType != ThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        float coefToPos = remap(prevPdfDir * absDot(surf.ns, wo));
+        s0t1 /= coefToPos;
+        s1t1 /= coefToPos / (bounce == 1 ? remap(dist * dist) : 1.0f);
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        {
+            float c0 = rand01(g), c1 = rand01(g);
+            CameraIiSample ci = thinLensCameraSampleIi(sc, pos, vec2(c0, c1));
+            if (ci.pdf > 0.0f) {
+                vec3 pCam = pos + ci.wi * ci.dist;
+                if (visibleOrc(sc, pos, pCam)) {
+                    float cosWi = satDot(surf.ng, ci.wi) * std::fabs(dot(surf.ns, wo) / dot(surf.ng, wo));
+                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    vec3 contrib = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
+                    float coefToSurf = remap(thinLensCameraPdfIe(sc, Ray{pCam, -ci.wi}).pdfDir * satDot(surf.ns, ci.wi));
+                    float coefToPrev = remap(materialPdf(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
+                    float coefDist = remap(ci.dist * ci.dist);
+                    float coef0 = coefToSurf * coefToPrev / coefDist;
+                    float coef1 = ((bounce == 1) ? 1.0f : coefToPrev) * coefToSurf / coefDist;
+                    float weight = weightT1(s0t1 * coef0, s1t1 * coef1);
+                    vec3 res = contrib * weight;
+                    if (!hasNan(res) && !std::isnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
+                        accumulateFilm(sc, film, ci.uv, res * uScale);
+                }
+            }
+        }
+        float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
+        if (bsdfPdf < 1e-8f || std::isnan(bsdfPdf)) break;
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bs.bsdf / bsdfPdf), 1.0f);
+            if (rand01(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float coefToPrev = remap(materialPdf(matType, mp, wi, wo, surf.ns) * absDot(prevNorm, wo));
+        s0t1 *= coefToPrev;
+        s1t1 *= (bounce == 1) ? 1.0f : coefToPrev;
+        prevPdfDir = materialPdf(matType, mp, wo, wi, surf.ns);
+        prevNorm = surf.ns;
+        float cosWi = deltaBsdf ? 1.0f : std::fabs(dot(surf.ng, wi) * dot(surf.ns, wo) / dot(surf.ng, wo));
+        throughput = throughput * (bs.bsdf * cosWi / bsdfPdf);
+        ray = rayOffseted(pos, wi);
+        wo = -wi;
+    }
+}
+
 // Per-pixel seeds: noise = tex(noise, tex(noise, coord / size)) with bilinear
 // filtering and repeat wrap at GL texel centres (path_integ_naive.glsl:156-160).
 inline vec2 noiseTexel(const OrcScene& sc, int x, int y) {
@@ -815,6 +1192,66 @@ void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; t++) th.emplace_back(work);
     for (auto& t : th) t.join();
+}
+
+// Light tracer passes (light_path_integ.glsl:148-158): `blocks` x 1536 light
+// paths per pass, seeded spp * (1536 * blocks) + gid + freeCounter; film is
+// float[H][W][3] and accumulates.
+void orc_render_lt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, int32_t blocks, float* film) {
+    const uint32_t group = 1536u * (uint32_t)blocks;
+    for (int k = 0; k < passes; k++) {
+        uint32_t spp = (uint32_t)(spp0 + k), fc = (uint32_t)(fc0 + k);
+        for (uint32_t gid = 0; gid < group; gid++) {
+            Rng g;
+            g.randSeed = spp * group + gid + fc;
+            g.sampleSeed = 0;
+            g.sampleOffset = 0;
+            lightIntegTrace(*sc, g, film);
+        }
+    }
+}
+
+// Triple-integrator passes (TriplePath.cpp:97-136): the camera pass of
+// triple_path_pass_pt.glsl for every pixel, then `blocks` x 1536 x `loops`
+// light paths of triple_path_pass_lpt.glsl scaled by W*H / (blocks*loops*1536).
+void orc_render_triple(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, int32_t blocks,
+                       int32_t loops, float* film) {
+    const uint32_t group = 1536u * (uint32_t)blocks * (uint32_t)loops;
+    const float uScale = (float)(sc->filmW * sc->filmH) / (float)(blocks * loops * 1536);
+    for (int k = 0; k < passes; k++) {
+        int spp = spp0 + k, fc = fc0 + k;
+        for (int py = 0; py < sc->filmH; py++)
+            for (int px = 0; px < sc->filmW; px++) {
+                vec2 texSize((float)sc->filmW, (float)sc->filmH);
+                vec2 scr = vec2((float)px, (float)py) / texSize;
+                vec2 nc = noiseTexture(*sc, scr);
+                nc = noiseTexture(*sc, nc);
+                vec2 tc = texSize * nc;
+                Rng g;
+                g.randSeed = f2u(tc.x) * (uint32_t)fc + f2u(tc.y);
+                g.sampleSeed = f2u(tc.x) * f2u(tc.y);
+                int off = (int)((uint32_t)spp * 256u);
+                if (off > 131072 * 256) off -= 131072 * 256;
+                g.sampleOffset = off;
+                int s = 0;
+                float u0 = sample1D(*sc, g, s), u1 = sample1D(*sc, g, s), u2 = sample1D(*sc, g, s), u3 = sample1D(*sc, g, s);
+                Ray ray = thinLensCameraSampleRay(*sc, scr, u0, u1, u2, u3);
+                vec3 r = traceCameraPath(*sc, ray, g, s);
+                if (!hasNan(r)) {
+                    float* p = film + 3 * ((size_t)py * sc->filmW + px);
+                    p[0] += r.x;
+                    p[1] += r.y;
+                    p[2] += r.z;
+                }
+            }
+        for (uint32_t gid = 0; gid < 1536u * (uint32_t)blocks; gid++) {
+            Rng g;
+            g.randSeed = (uint32_t)spp * group + gid + (uint32_t)fc;
+            g.sampleSeed = 0;
+            g.sampleOffset = 0;
+            for (int i = 0; i < loops; i++) traceLightPath(*sc, g, film, uScale);
+        }
+    }
 }
 
 // ----------------------------------------------------------- host tables

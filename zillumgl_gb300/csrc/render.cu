@@ -7,6 +7,7 @@
 // once per block into shared memory.
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "scene.h"
 #include "shading.cuh"
@@ -19,7 +20,10 @@ struct zgl_integrator {
     int32_t curSample = 0;    // mCurSample
     int32_t freeCounter = 0;  // mFreeCounter
     bool finished = false;
-    float4* d_frame = nullptr;  // RGBA sum, filmW * filmH
+    float4* d_frame = nullptr;  // path tracer: RGBA sum, filmW * filmH
+    float* d_film = nullptr;    // light / triple: RGB sum, filmW * filmH * 3 (the r32f 3W x H film)
+    float samplePerPixel = 0.0f;
+    int32_t blocks = 0, loops = 1;
 };
 
 namespace zgl {
@@ -180,6 +184,368 @@ path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uin
     }
 }
 
+// Film of the light-tracing passes, float[H][W][3].  int(uv * size) == size
+// (uv on the far edge) falls outside the image and is dropped, as an
+// out-of-range imageAtomicAdd is.
+__device__ __forceinline__ void accumulateFilm(const DeviceScene& sc, float* film, v2 uv, v3 res) {
+    if (!inFilmBound(uv)) return;
+    int x = zf2i(uv.x * (float)sc.filmW), y = zf2i(uv.y * (float)sc.filmH);
+    if (x >= sc.filmW || y >= sc.filmH) return;
+    float* p = film + 3 * ((size_t)y * sc.filmW + x);
+    atomicAdd(p, res.x);
+    atomicAdd(p + 1, res.y);
+    atomicAdd(p + 2, res.z);
+}
+
+__device__ __forceinline__ void shadeSurface(const DeviceScene& sc, int id, v3 pos, v3 wo, Surface& surf,
+                                             uint32_t& matType, BSDFParam& mp) {
+    TriShade tri = loadTri(sc, id);
+    surf = surfaceInfo(tri, pos);
+    int matId = tri.matTex & 0x0000ffff;
+    matType = loadMaterialType(sc, matId);
+    if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
+        surf.ns = -surf.ns;
+        surf.ng = -surf.ng;
+    }
+    mp = loadMaterial(sc, matType, matId);
+}
+
+// lightIntegTrace (light_path_integ.glsl:45-146); the light tracer forces the
+// independent sampler (LightPath.cpp:49), so every dimension is rand().
+__device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler& g, float* film) {
+    float a0 = rand01(g), a1 = rand01(g);
+    int light = lightSampleOne(sc, mk2(a0, a1));
+    float pdfSource = lightPdfSampleOne(sc, light);
+    Ray ray;
+    v3 wo, throughput;
+    {
+        int triId = light + sc.objPrimCount;
+        float b0 = rand01(g), b1 = rand01(g);
+        TriShade t = loadTri(sc, triId);
+        v3 pLit = sampleTriangleUniform(t.a, t.b, t.c, mk2(b0, b1));
+        float c0 = rand01(g), c1 = rand01(g);
+        CameraIiSample ci = thinLensCameraSampleIi(sc, pLit, mk2(c0, c1));
+        if (ci.pdf > 0.0f) {
+            v3 pCam = pLit + ci.wi * ci.dist;
+            float area;
+            lightPowerOf(sc, light, area);
+            float pdfPos = 1.0f / area;
+            if (visible(sc, pLit, pCam)) {
+                v3 Le = lightLe(sc, light, pLit, ci.wi);
+                v3 contrib = Le * ci.Ii / (ci.pdf * pdfPos * pdfSource);
+                if (!isBlack(contrib)) accumulateFilm(sc, film, ci.uv, contrib);
+            }
+        }
+        float d0 = rand01(g), d1 = rand01(g), d2 = rand01(g), d3 = rand01(g);
+        LightLeSample le = lightSampleOneLe(sc, light, d0, d1, d2, d3);
+        v3 nl = geomNormal(sc, triId, le.ray.ori);
+        wo = -le.ray.dir;
+        ray = rayOffseted(le.ray.ori, le.ray.dir);
+        throughput = le.Le * absDot(nl, -wo) / (pdfSource * le.pdfPos * le.pdfDir);
+    }
+    for (int bounce = 1; bounce <= pp.maxDepth; bounce++) {
+        float dist;
+        int id = bvhHit(sc, ray, dist);
+        if (id == -1) break;
+        if (id - sc.objPrimCount >= 0) break;
+        v3 pos = rayPoint(ray, dist);
+        Surface surf;
+        uint32_t matType;
+        BSDFParam mp;
+        shadeSurface(sc, id, pos, wo, surf, matType, mp);
+        {
+            float c0 = rand01(g), c1 = rand01(g);
+            CameraIiSample ci = thinLensCameraSampleIi(sc, pos, mk2(c0, c1));
+            if (ci.pdf > 0.0f) {
+                v3 pCam = pos + ci.wi * ci.dist;
+                if (visible(sc, pos, pCam)) {
+                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
+                    v3 res = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
+                    if (!hasNan(res) && !zisnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
+                        accumulateFilm(sc, film, ci.uv, res);
+                }
+            }
+        }
+        float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        v3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+        if (bsdfPdf < 1e-8f || zisnan(bsdfPdf)) break;
+        if (pp.rr && bounce >= pp.rrStart) {
+            float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 1.0f);
+            if (rand01(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float cosWi = deltaBsdf ? 1.0f : fabsf(dot(surf.ng, wi) * dot(surf.ns, wo) / dot(surf.ng, wo));
+        throughput = throughput * (bs.bsdf * cosWi / bsdfPdf);
+        ray = rayOffseted(pos, wi);
+        wo = -wi;
+    }
+}
+
+__device__ __forceinline__ float weightS0(float s1s0, float t1s0) { return 1.0f / (1.0f + s1s0 + t1s0); }
+__device__ __forceinline__ float weightS1(float s1s0, float t1s1) { return s1s0 / (1.0f + s1s0 + s1s0 * t1s1); }
+__device__ __forceinline__ float weightT1(float s0t1, float s1t1) { return 1.0f / (s0t1 + s1t1 + 1.0f); }
+
+// traceCameraPath (triple_path_pass_pt.glsl:59-195)
+__device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g) {
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    v3 pos = rayPoint(ray, primDist);
+    if (id == -1) return envLe(sc, ray.dir);
+    if (id - sc.objPrimCount >= 0) return lightLe(sc, id - sc.objPrimCount, pos, -ray.dir);
+    Surface surf = surfaceInfo(loadTri(sc, id), pos);
+    v3 wo = -ray.dir;
+    v3 prevNorm = f3(sc.camF);
+    v3 result = mk3(0.0f), throughput = mk3(1.0f);
+    PdfPair camPdf = thinLensCameraPdfIe(sc, ray);
+    float primaryPdf = remap(camPdf.pdfPos) / remap(camPdf.pdfDir * absDot(surf.ns, ray.dir) / sq(primDist));
+    float t1s0 = primaryPdf, t1s1 = primaryPdf;
+    for (int bounce = 1; bounce <= pp.maxDepth; bounce++) {
+        TriShade tri = loadTri(sc, id);
+        if (bounce > 1) surf = surfaceInfo(tri, pos);
+        int matId = tri.matTex & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        {
+            float a0 = sample1D(g), a1 = sample1D(g);
+            int light = lightSampleOne(sc, mk2(a0, a1));
+            int triId = light + sc.objPrimCount;
+            float pdfSource = lightPdfSampleOne(sc, light);
+            float b0 = sample1D(g), b1 = sample1D(g);
+            TriShade lt = loadTri(sc, triId);
+            v3 pLit = sampleTriangleUniform(lt.a, lt.b, lt.c, mk2(b0, b1));
+            v3 wi = normalize(pLit - pos);
+            v3 Le = lightLe(sc, light, pLit, -wi);
+            if (!isBlack(Le) && visible(sc, pos, pLit)) {
+                v3 nLit = surfaceInfo(lt, pLit).ng;
+                float area;
+                lightPowerOf(sc, light, area);
+                float pA = pdfSource / area;
+                float dist2 = distSquare(pos, pLit);
+                float pS = pA * dist2 / absDot(nLit, wi);
+                v3 f = materialBSDF(matType, mp, wo, wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, wi, surf.ns);
+                float pdfRev = materialPdf(matType, mp, wi, wo, surf.ns);
+                float pdfPLit = remap(pA);
+                float coefToSurf = remap(0.5f * kPiInv * absDot(surf.ns, wi));
+                float coefToLight = remap(fpdf * satDot(nLit, -wi));
+                float coefToPrev = (bounce == 1) ? 1.0f : remap(pdfRev * absDot(prevNorm, wo));
+                float coefDist = remap(dist2);
+                float weight = weightS1(pdfPLit * coefDist / coefToLight, t1s1 * coefToSurf * coefToPrev / coefDist);
+                result = result + Le * f * throughput * absDot(surf.ns, wi) / pS * weight;
+            }
+        }
+        float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        v3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        Ray nextRay = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, nextRay, dist);
+        int lightId = nextId - sc.objPrimCount;
+        v3 nextPos = rayPoint(nextRay, dist);
+        float pdfDirToNext = materialPdf(matType, mp, wo, wi, surf.ns);
+        float pdfDirToPrev = materialPdf(matType, mp, wi, wo, surf.ns);
+        if (nextId == -1) break;
+        if (lightId >= 0) {
+            v3 nLit = geomNormal(sc, nextId, nextPos);
+            PdfPair pdfLit = lightPdfLe(sc, lightId, Ray{nextPos, -wi});
+            float pdfPLit = remap(pdfLit.pdfPos * lightPdfSampleOne(sc, lightId));
+            float coefToLight = remap(pdfDirToNext * satDot(nLit, -wi));
+            float coefToSurf = remap(pdfLit.pdfDir * absDot(surf.ns, wi));
+            float coefToPrev = (bounce == 1) ? 1.0f : remap(pdfDirToPrev * absDot(prevNorm, wo));
+            float coefDist = remap(dist * dist);
+            float weight = zisnan(t1s0) ? 0.0f
+                                        : weightS0(pdfPLit * coefDist / coefToLight,
+                                                   t1s0 * coefToSurf * pdfPLit * coefToPrev / coefToLight);
+            result = result + lightLe(sc, lightId, nextPos, -wi) * throughput * weight;
+            break;
+        }
+        if (pp.rr && bounce >= pp.rrStart) {
+            float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+            if (sample1D(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float coef = ((bounce == 1) ? 1.0f : remap(pdfDirToPrev * absDot(prevNorm, wo))) /
+                     remap(pdfDirToNext * absDot(triangleNormalShad(sc, nextId, nextPos), wi));
+        t1s0 *= coef;
+        t1s1 *= coef;
+        prevNorm = surf.ns;
+        pos = nextPos;
+        wo = -wi;
+        id = nextId;
+    }
+    return result;
+}
+
+// traceLightPath (triple_path_pass_lpt.glsl:58-182)
+__device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sampler& g, float* film, float uScale) {
+    float a0 = rand01(g), a1 = rand01(g);
+    int light = lightSampleOne(sc, mk2(a0, a1));
+    float pdfSource = lightPdfSampleOne(sc, light);
+    Ray ray;
+    v3 wo, throughput, prevNorm;
+    float prevPdfDir, s0t1, s1t1;
+    {
+        int triId = light + sc.objPrimCount;
+        rand01(g);  // the reference samples a point here and never uses it
+        rand01(g);
+        float d0 = rand01(g), d1 = rand01(g), d2 = rand01(g), d3 = rand01(g);
+        LightLeSample le = lightSampleOneLe(sc, light, d0, d1, d2, d3);
+        v3 nl = geomNormal(sc, triId, le.ray.ori);
+        wo = -le.ray.dir;
+        ray = rayOffseted(le.ray.ori, le.ray.dir);
+        throughput = le.Le * absDot(nl, -wo) / (pdfSource * le.pdfPos * le.pdfDir);
+        prevNorm = nl;
+        prevPdfDir = le.pdfDir;
+        s0t1 = 1.0f / remap(le.pdfPos * pdfSource);
+        s1t1 = 1.0f;
+    }
+    for (int bounce = 1; bounce <= pp.maxDepth; bounce++) {
+        float dist;
+        int id = bvhHit(sc, ray, dist);
+        if (id == -1) break;
+        if (id - sc.objPrimCount >= 0) break;
+        v3 pos = rayPoint(ray, dist);
+        TriShade tri = loadTri(sc, id);
+        Surface surf = surfaceInfo(tri, pos);
+        int matId = tri.matTex & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        float coefToPos = remap(prevPdfDir * absDot(surf.ns, wo));
+        s0t1 /= coefToPos;
+        s1t1 /= coefToPos / (bounce == 1 ? remap(dist * dist) : 1.0f);
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        {
+            float c0 = rand01(g), c1 = rand01(g);
+            CameraIiSample ci = thinLensCameraSampleIi(sc, pos, mk2(c0, c1));
+            if (ci.pdf > 0.0f) {
+                v3 pCam = pos + ci.wi * ci.dist;
+                if (visible(sc, pos, pCam)) {
+                    float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
+                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    v3 contrib = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
+                    float coefToSurf = remap(thinLensCameraPdfIe(sc, Ray{pCam, -ci.wi}).pdfDir * satDot(surf.ns, ci.wi));
+                    float coefToPrev = remap(materialPdf(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
+                    float coefDist = remap(ci.dist * ci.dist);
+                    float coef0 = coefToSurf * coefToPrev / coefDist;
+                    float coef1 = ((bounce == 1) ? 1.0f : coefToPrev) * coefToSurf / coefDist;
+                    float weight = weightT1(s0t1 * coef0, s1t1 * coef1);
+                    v3 res = contrib * weight;
+                    if (!hasNan(res) && !zisnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
+                        accumulateFilm(sc, film, ci.uv, res * uScale);
+                }
+            }
+        }
+        float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        v3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+        if (bsdfPdf < 1e-8f || zisnan(bsdfPdf)) break;
+        if (pp.rr && bounce >= pp.rrStart) {
+            float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 1.0f);
+            if (rand01(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        float coefToPrev = remap(materialPdf(matType, mp, wi, wo, surf.ns) * absDot(prevNorm, wo));
+        s0t1 *= coefToPrev;
+        s1t1 *= (bounce == 1) ? 1.0f : coefToPrev;
+        prevPdfDir = materialPdf(matType, mp, wo, wi, surf.ns);
+        prevNorm = surf.ns;
+        float cosWi = deltaBsdf ? 1.0f : fabsf(dot(surf.ng, wi) * dot(surf.ns, wo) / dot(surf.ng, wo));
+        throughput = throughput * (bs.bsdf * cosWi / bsdfPdf);
+        ray = rayOffseted(pos, wi);
+        wo = -wi;
+    }
+}
+
+constexpr int kLightBlock = 256;
+
+// main() of light_path_integ.glsl:148-158: logical group 1536 x blocks
+__global__ void __launch_bounds__(kLightBlock)
+light_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCounter, uint32_t nPaths, float* film) {
+    uint32_t gid = blockIdx.x * kLightBlock + threadIdx.x;
+    if (gid >= nPaths) return;
+    Sampler g;
+    g.randSeed = spp * nPaths + gid + freeCounter;
+    g.sampleSeed = 0;
+    g.sampleOffset = 0;
+    g.dim = 0;
+    g.mode = 0;
+    g.rowCache = nullptr;
+    g.mats = sc.sobol;
+    lightTrace(sc, pp, g, film);
+}
+
+// main() of triple_path_pass_pt.glsl:197-224 (addFilm: one owner per pixel)
+__global__ void __launch_bounds__(kTileX* kTileY)
+triple_pt_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uint32_t sampleOffset,
+                 float* __restrict__ film) {
+    __shared__ uint32_t row[256];
+    load_sobol_row(sc, sampleOffset, row);
+    const int px = blockIdx.x * kTileX + threadIdx.x;
+    const int py = blockIdx.y * kTileY + threadIdx.y;
+    if (px >= sc.filmW || py >= sc.filmH) return;
+    const size_t pix = (size_t)py * sc.filmW + px;
+    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+    Sampler g;
+    g.randSeed = seed.x * (uint32_t)freeCounter + seed.y;
+    g.sampleSeed = seed.x * seed.y;
+    g.sampleOffset = sampleOffset;
+    g.dim = 0;
+    g.mode = sc.sampler;
+    g.rowCache = row;
+    g.mats = sc.sobol;
+    v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    v3 r = tripleCameraTrace(sc, pp, ray, g);
+    if (!hasNan(r)) {
+        float* p = film + 3 * pix;
+        p[0] = p[0] + r.x;
+        p[1] = p[1] + r.y;
+        p[2] = p[2] + r.z;
+    }
+}
+
+// main() of triple_path_pass_lpt.glsl:184-191
+__global__ void __launch_bounds__(kLightBlock)
+triple_lpt_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCounter, uint32_t nThreads,
+                  uint32_t loops, float uScale, float* film) {
+    uint32_t gid = blockIdx.x * kLightBlock + threadIdx.x;
+    if (gid >= nThreads) return;
+    Sampler g;
+    g.randSeed = spp * (nThreads * loops) + gid + freeCounter;
+    g.sampleSeed = 0;
+    g.sampleOffset = 0;
+    g.dim = 0;
+    g.mode = 0;
+    g.rowCache = nullptr;
+    g.mats = sc.sobol;
+    for (uint32_t i = 0; i < loops; i++) tripleLightTrace(sc, pp, g, film, uScale);
+}
+
+// img_copy_1x32f_4x32f.glsl: film (r, g, b) -> frame (r, g, b, 1)
+__global__ void film_to_frame_kernel(const float* __restrict__ film, float4* __restrict__ out, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = make_float4(film[3 * i], film[3 * i + 1], film[3 * i + 2], 1.0f);
+}
+
 // sampleOffset = uSpp * uSampleDim, minus the table size once when beyond it
 // (path_integ_naive.glsl:163-164), in 32-bit arithmetic.
 uint32_t sample_offset(int32_t spp) {
@@ -201,6 +567,37 @@ cudaError_t launch_path_pass(const zgl_scene* s, const zgl_integrator_params& p,
     return cudaGetLastError();
 }
 
+cudaError_t launch_light_pass(const zgl_scene* s, const zgl_integrator_params& p, int32_t blocks, int32_t spp,
+                              int32_t freeCounter, float* film, cudaStream_t st) {
+    PathParams pp{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
+                  p.light_portion};
+    uint32_t n = 1536u * (uint32_t)blocks;
+    light_kernel<<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(s->view(), pp, (uint32_t)spp,
+                                                                             (uint32_t)freeCounter, n, film);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_triple_pass(const zgl_scene* s, const zgl_integrator_params& p, int32_t blocks, int32_t loops,
+                               int32_t spp, int32_t freeCounter, float* film, cudaStream_t st) {
+    PathParams pp{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
+                  p.light_portion};
+    dim3 block(kTileX, kTileY);
+    dim3 grid((unsigned)((s->filmW + kTileX - 1) / kTileX), (unsigned)((s->filmH + kTileY - 1) / kTileY));
+    triple_pt_kernel<<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), film);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    uint32_t n = 1536u * (uint32_t)blocks;
+    float uScale = (float)(s->filmW * s->filmH) / (float)(blocks * loops * 1536);
+    triple_lpt_kernel<<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(
+        s->view(), pp, (uint32_t)spp, (uint32_t)freeCounter, n, (uint32_t)loops, uScale, film);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_film_to_frame(const float* film, float4* out, int64_t n, cudaStream_t st) {
+    film_to_frame_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(film, out, n);
+    return cudaGetLastError();
+}
+
 }  // namespace zgl
 
 using namespace zgl;
@@ -212,6 +609,10 @@ void check_params(const zgl_integrator_params& p) {
     if (p.rr_start_depth < 1) fail(ZGL_ERR_INVALID_ARG, "integrator: rr_start_depth must be >= 1");
     if (!(p.light_portion >= 0.0f && p.light_portion <= 1.0f))
         fail(ZGL_ERR_INVALID_ARG, "integrator: light_portion must lie in [0, 1]");
+    if (p.blocks_per_pass < 0 || p.blocks_per_pass > 65536)
+        fail(ZGL_ERR_INVALID_ARG, "integrator: blocks_per_pass %d out of range", p.blocks_per_pass);
+    if (p.loops_per_pass < 1 || p.loops_per_pass > 4096)
+        fail(ZGL_ERR_INVALID_ARG, "integrator: loops_per_pass %d out of range", p.loops_per_pass);
 }
 
 bool is_device_memory(const void* p) {
@@ -238,6 +639,8 @@ zgl_status zgl_integrator_params_default(zgl_integrator_params* p) {
     p->light_portion = 0.5f;
     p->finite_sample = 0;
     p->max_sample = 64;
+    p->blocks_per_pass = 0;
+    p->loops_per_pass = 1;
     ZGL_API_END
 }
 
@@ -247,7 +650,11 @@ zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integ
     if (!scene || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_create: NULL argument");
     *out = nullptr;
     if (scene->host_only) fail(ZGL_ERR_STATE, "zgl_integrator_create: scene was created host-only");
-    if (kind != ZGL_INTEGRATOR_PATH) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_create: unknown kind %d", kind);
+    if (kind < ZGL_INTEGRATOR_PATH || kind > ZGL_INTEGRATOR_TRIPLE)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_create: unknown kind %d", kind);
+    if (kind != ZGL_INTEGRATOR_PATH && scene->nLight == 0)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_create: the light and triple integrators sample light triangles "
+                                  "and the scene has none");
     zgl_integrator_params p;
     zgl_integrator_params_default(&p);
     if (params) p = *params;
@@ -256,10 +663,20 @@ zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integ
     it->scene = scene;
     it->kind = kind;
     it->params = p;
-    cudaError_t e = cudaMalloc(&it->d_frame, sizeof(float4) * (size_t)scene->filmW * scene->filmH);
-    if (e == cudaSuccess) e = cudaMemset(it->d_frame, 0, sizeof(float4) * (size_t)scene->filmW * scene->filmH);
+    it->blocks = p.blocks_per_pass ? p.blocks_per_pass : (kind == ZGL_INTEGRATOR_TRIPLE ? 64 : 32);
+    it->loops = p.loops_per_pass;
+    size_t npix = (size_t)scene->filmW * scene->filmH;
+    cudaError_t e;
+    if (kind == ZGL_INTEGRATOR_PATH) {
+        e = cudaMalloc(&it->d_frame, sizeof(float4) * npix);
+        if (e == cudaSuccess) e = cudaMemset(it->d_frame, 0, sizeof(float4) * npix);
+    } else {
+        e = cudaMalloc(&it->d_film, sizeof(float) * 3 * npix);
+        if (e == cudaSuccess) e = cudaMemset(it->d_film, 0, sizeof(float) * 3 * npix);
+    }
     if (e != cudaSuccess) {
         if (it->d_frame) cudaFree(it->d_frame);
+        if (it->d_film) cudaFree(it->d_film);
         delete it;
         cuda_check(e, "zgl_integrator_create");
     }
@@ -270,13 +687,31 @@ zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integ
 zgl_status zgl_integrator_render_pass(zgl_integrator* it, void* stream) {
     ZGL_API_BEGIN
     if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_pass: NULL");
-    it->freeCounter++;  // NaivePath.cpp:79: counts every call
-    if (it->params.finite_sample && it->curSample > it->params.max_sample) {
-        it->finished = true;
-        return ZGL_OK;
+    it->freeCounter++;  // counts every call (NaivePath.cpp:79, LightPath.cpp:85, TriplePath.cpp:268)
+    const zgl_scene* sc = it->scene;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (it->kind == ZGL_INTEGRATOR_PATH) {
+        if (it->params.finite_sample && it->curSample > it->params.max_sample) {
+            it->finished = true;
+            return ZGL_OK;
+        }
+        ZGL_CUDA(launch_path_pass(sc, it->params, it->curSample, it->freeCounter, it->d_frame, st));
+    } else if (it->kind == ZGL_INTEGRATOR_LIGHT) {
+        if (it->params.finite_sample && it->samplePerPixel > (float)it->params.max_sample) {
+            it->finished = true;
+            return ZGL_OK;
+        }
+        ZGL_CUDA(launch_light_pass(sc, it->params, it->blocks, it->curSample, it->freeCounter, it->d_film, st));
+        it->samplePerPixel += (float)it->blocks * 1536.0f / (float)(sc->filmW * sc->filmH);
+    } else {
+        if (it->params.finite_sample && it->curSample > it->params.max_sample) {
+            it->finished = true;
+            return ZGL_OK;
+        }
+        ZGL_CUDA(launch_triple_pass(sc, it->params, it->blocks, it->loops, it->curSample, it->freeCounter,
+                                    it->d_film, st));
+        it->samplePerPixel += 1.0f;
     }
-    ZGL_CUDA(launch_path_pass(it->scene, it->params, it->curSample, it->freeCounter, it->d_frame,
-                              (cudaStream_t)stream));
     it->curSample++;
     ZGL_API_END
 }
@@ -284,21 +719,46 @@ zgl_status zgl_integrator_render_pass(zgl_integrator* it, void* stream) {
 zgl_status zgl_integrator_reset(zgl_integrator* it) {
     ZGL_API_BEGIN
     if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_reset: NULL");
+    const zgl_scene* sc = it->scene;
     it->curSample = 0;
     it->finished = false;
+    if (it->kind != ZGL_INTEGRATOR_PATH) {
+        // the film is cleared (img_clear_1x32f.glsl); samplePerPixel restarts
+        // at one pass worth (LightPath.cpp:133, TriplePath.cpp:322)
+        ZGL_CUDA(cudaMemset(it->d_film, 0, sizeof(float) * 3 * (size_t)sc->filmW * sc->filmH));
+        it->samplePerPixel = it->kind == ZGL_INTEGRATOR_LIGHT
+                                 ? (float)it->blocks * 1536.0f / (float)(sc->filmW * sc->filmH)
+                                 : 1.0f;
+    }
     ZGL_API_END
 }
 
 zgl_status zgl_integrator_frame(zgl_integrator* it, float* out, int32_t* spp, void* stream) {
     ZGL_API_BEGIN
     if (!it || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_frame: NULL");
-    size_t bytes = sizeof(float4) * (size_t)it->scene->filmW * it->scene->filmH;
+    size_t npix = (size_t)it->scene->filmW * it->scene->filmH;
+    size_t bytes = sizeof(float4) * npix;
     cudaStream_t st = (cudaStream_t)stream;
-    if (is_device_memory(out)) {
-        ZGL_CUDA(cudaMemcpyAsync(out, it->d_frame, bytes, cudaMemcpyDeviceToDevice, st));
+    bool dev = is_device_memory(out);
+    if (it->kind == ZGL_INTEGRATOR_PATH) {
+        if (dev) {
+            ZGL_CUDA(cudaMemcpyAsync(out, it->d_frame, bytes, cudaMemcpyDeviceToDevice, st));
+        } else {
+            ZGL_CUDA(cudaMemcpyAsync(out, it->d_frame, bytes, cudaMemcpyDeviceToHost, st));
+            ZGL_CUDA(cudaStreamSynchronize(st));
+        }
+    } else if (dev) {
+        ZGL_CUDA(launch_film_to_frame(it->d_film, reinterpret_cast<float4*>(out), (int64_t)npix, st));
     } else {
-        ZGL_CUDA(cudaMemcpyAsync(out, it->d_frame, bytes, cudaMemcpyDeviceToHost, st));
+        std::vector<float> film(3 * npix);
+        ZGL_CUDA(cudaMemcpyAsync(film.data(), it->d_film, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, st));
         ZGL_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < npix; i++) {
+            out[4 * i] = film[3 * i];
+            out[4 * i + 1] = film[3 * i + 1];
+            out[4 * i + 2] = film[3 * i + 2];
+            out[4 * i + 3] = 1.0f;
+        }
     }
     if (spp) *spp = it->curSample;
     ZGL_API_END
@@ -307,7 +767,7 @@ zgl_status zgl_integrator_frame(zgl_integrator* it, float* out, int32_t* spp, vo
 zgl_status zgl_integrator_result_scale(const zgl_integrator* it, float* out) {
     ZGL_API_BEGIN
     if (!it || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_result_scale: NULL");
-    *out = 1.0f / (float)(it->curSample + 1);
+    *out = it->kind == ZGL_INTEGRATOR_PATH ? 1.0f / (float)(it->curSample + 1) : 1.0f / it->samplePerPixel;
     ZGL_API_END
 }
 
@@ -315,6 +775,7 @@ zgl_status zgl_integrator_destroy(zgl_integrator* it) {
     ZGL_API_BEGIN
     if (!it) return ZGL_OK;
     if (it->d_frame) cudaFree(it->d_frame);
+    if (it->d_film) cudaFree(it->d_film);
     delete it;
     ZGL_API_END
 }

@@ -510,4 +510,114 @@ __device__ __forceinline__ Ray thinLensCameraSampleRay(const DeviceScene& sc, v2
     return Ray{f3(sc.camPos) + R * lens.x + U * lens.y, dir};
 }
 
+// ------------------------------------------------ camera importance (camera.glsl)
+__device__ __forceinline__ bool inFilmBound(v2 uv) { return uv.x >= 0.0f && uv.x <= 1.0f && uv.y >= 0.0f && uv.y <= 1.0f; }
+__device__ __forceinline__ bool thinLensCameraDelta(const DeviceScene& sc) { return sc.lensRadius <= 1e-6f; }
+__device__ __forceinline__ v2 thinLensCameraRasterPos(const DeviceScene& sc, const Ray& ray) {  // camera.glsl:79-91
+    float cosTheta = dot(ray.dir, f3(sc.camF));
+    float dFocus = sc.focalDist / cosTheta;
+    const float* mi = sc.camMatInv;
+    m3 inv{mk3(mi[0], mi[1], mi[2]), mk3(mi[3], mi[4], mi[5]), mk3(mi[6], mi[7], mi[8])};
+    v3 pFocus = mul(inv, rayPoint(ray, dFocus) - f3(sc.camPos));
+    float aspect = (float)sc.filmW / (float)sc.filmH;
+    v3 div = mk3(aspect * sc.tanFOV * sc.focalDist, 1.0f * sc.tanFOV * sc.focalDist, 1.0f * sc.focalDist);
+    pFocus = pFocus / div;
+    return mk2((pFocus.x + 1.0f) * 0.5f, (pFocus.y + 1.0f) * 0.5f);
+}
+__device__ __forceinline__ v3 thinLensCameraIe(const DeviceScene& sc, const Ray& ray) {  // camera.glsl:93-107
+    float cosTheta = dot(ray.dir, f3(sc.camF));
+    if (cosTheta < 1e-6f) return mk3(0.0f);
+    v2 pRaster = thinLensCameraRasterPos(sc, ray);
+    if (!inFilmBound(pRaster)) return mk3(0.0f);
+    float tanFOVInv = 1.0f / sc.tanFOV;
+    float cos2Theta = cosTheta * cosTheta;
+    float lensArea = thinLensCameraDelta(sc) ? 1.0f : kPi * sc.lensRadius * sc.lensRadius;
+    return mk3(0.25f) * sq(tanFOVInv / cos2Theta) / (lensArea * sc.camAsp);
+}
+struct CameraIiSample {
+    v3 wi, Ii;
+    float dist;
+    v2 uv;
+    float pdf;
+};
+__device__ __forceinline__ CameraIiSample thinLensCameraSampleIi(const DeviceScene& sc, v3 ref, v2 u) {  // :109-127
+    v2 l = toConcentricDisk(u) * sc.lensRadius;
+    v3 y = f3(sc.camPos) + f3(sc.camR) * l.x + f3(sc.camU) * l.y + f3(sc.camF) * 0.0f;
+    float dist = distance(ref, y);
+    v3 wi = normalize(y - ref);
+    float cosTheta = satDot(f3(sc.camF), -wi);
+    CameraIiSample r;
+    if (cosTheta < 1e-6f) {
+        r.wi = r.Ii = mk3(0.0f);
+        r.dist = 0.0f;
+        r.uv = mk2(0.0f, 0.0f);
+        r.pdf = 0.0f;
+        return r;
+    }
+    Ray ray{y, -wi};
+    r.wi = wi;
+    r.Ii = thinLensCameraIe(sc, ray);
+    r.uv = thinLensCameraRasterPos(sc, ray);
+    float lensArea = thinLensCameraDelta(sc) ? 1.0f : kPi * sc.lensRadius * sc.lensRadius;
+    r.dist = dist;
+    r.pdf = dist * dist / (cosTheta * lensArea);
+    return r;
+}
+struct PdfPair {
+    float pdfPos, pdfDir;
+};
+__device__ __forceinline__ PdfPair thinLensCameraPdfIe(const DeviceScene& sc, const Ray& ray) {  // :129-141
+    float cosTheta = dot(f3(sc.camF), ray.dir);
+    if (cosTheta < 1e-6f) return PdfPair{0.0f, 0.0f};
+    v2 pRaster = thinLensCameraRasterPos(sc, ray);
+    if (!inFilmBound(pRaster)) return PdfPair{0.0f, 0.0f};
+    float pdfPos = thinLensCameraDelta(sc) ? 1.0f : 1.0f / (kPi * sc.lensRadius * sc.lensRadius);
+    float pdfDir = 1.0f / (cosTheta * cosTheta * cosTheta);
+    return PdfPair{pdfPos, pdfDir};
+}
+
+// ------------------------------------------------------- light emission (light.glsl)
+struct LightLeSample {
+    Ray ray;
+    v3 Le;
+    float pdfPos, pdfDir;
+};
+__device__ __forceinline__ LightLeSample lightSampleOneLe(const DeviceScene& sc, int id, float u0, float u1, float u2,
+                                                          float u3) {  // light.glsl:111-120
+    int triId = id + sc.objPrimCount;
+    TriShade t = loadTri(sc, triId);
+    v3 ori = sampleTriangleUniform(t.a, t.b, t.c, mk2(u0, u1));
+    v3 norm = surfaceInfo(t, ori).ng;
+    float pdfDir;
+    v3 dir = sampleCosineWeighted(norm, mk2(u2, u3), pdfDir);
+    float area;
+    lightPowerOf(sc, id, area);
+    LightLeSample r;
+    r.ray = rayOffseted(ori, dir);
+    r.Le = lightLe(sc, id, ori, dir);
+    r.pdfPos = 1.0f / area;
+    r.pdfDir = pdfDir;
+    return r;
+}
+__device__ __forceinline__ PdfPair lightPdfLe(const DeviceScene& sc, int id, const Ray& ray) {  // light.glsl:100-109
+    int triId = id + sc.objPrimCount;
+    v3 norm = geomNormal(sc, triId, ray.ori);
+    float area;
+    lightPowerOf(sc, id, area);
+    PdfPair r;
+    r.pdfPos = 1.0f / area;
+    r.pdfDir = (dot(norm, ray.dir) <= 0.0f) ? 0.0f : 0.5f * kPiInv;
+    return r;
+}
+__device__ __forceinline__ v3 triangleNormalShad(const DeviceScene& sc, int id, v3 p) {  // intersection.glsl:149-173
+    TriShade t = loadTri(sc, id);
+    v3 pa = t.a - p, pb = t.b - p, pc = t.c - p;
+    float areaInv = 1.0f / length(cross(t.b - t.a, t.c - t.a));
+    float la = length(cross(pb, pc)) * areaInv;
+    float lb = length(cross(pc, pa)) * areaInv;
+    float lc = 1.0f - la - lb;
+    return normalize(t.na * la + t.nb * lb + t.nc * lc);
+}
+__device__ __forceinline__ float remap(float p) { return p < 1e-8f ? 1.0f : p * p; }
+
 }  // namespace zgl

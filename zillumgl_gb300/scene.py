@@ -4,8 +4,9 @@
 takes world-space object and light meshes, materials in the 64-byte
 ``Material`` layout (src/core/Material.h:32-53), an optional environment image
 and the camera, and builds the sampling tables and device buffers through the
-C ABI.  ``PathIntegrator`` mirrors ``NaivePathIntegrator``
-(src/core/Integrator.h:68-91): ``render_one_pass``, ``reset``, ``get_frame``
+C ABI.  ``PathIntegrator``, ``LightIntegrator`` and ``TripleIntegrator`` mirror
+``NaivePathIntegrator``, ``LightPathIntegrator`` and ``TriplePathIntegrator``
+(src/core/Integrator.h:68-172): ``render_one_pass``, ``reset``, ``get_frame``
 and ``result_scale``.
 """
 from __future__ import annotations
@@ -70,7 +71,8 @@ class IntegratorParams(C.Structure):
     _fields_ = [
         ("max_depth", C.c_int32), ("russian_roulette", C.c_int32), ("rr_start_depth", C.c_int32),
         ("sample_light", C.c_int32), ("light_env_uniform_sample", C.c_int32), ("light_portion", C.c_float),
-        ("finite_sample", C.c_int32), ("max_sample", C.c_int32),
+        ("finite_sample", C.c_int32), ("max_sample", C.c_int32), ("blocks_per_pass", C.c_int32),
+        ("loops_per_pass", C.c_int32),
     ]
 
 
@@ -259,3 +261,17 @@ class PathIntegrator:
             self.close()
         except Exception:
             pass
+
+
+class LightIntegrator(PathIntegrator):
+    """LightPathIntegrator (src/core/Integrator.h:103-129): the particle
+    tracer; the frame is the film sum, result_scale() = 1 / samplePerPixel."""
+
+    KIND = 1
+
+
+class TripleIntegrator(PathIntegrator):
+    """TriplePathIntegrator (src/core/Integrator.h:145-172): MIS-weighted
+    (s=0) + (s=1) + (t=1) strategies, camera pass then light pass."""
+
+    KIND = 2
