@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent"])
     ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
+    ap.add_argument("--render", default="cornell,city", help="render workloads to time ('' for none)")
+    ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
+    ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
     return ap.parse_args()
 
 
@@ -157,6 +160,9 @@ def run_ours(args):
 
         dist.init_process_group("nccl", device_id=dev)
     stream = torch.cuda.Stream(device=dev)
+    if args.no_traversal:  # render workloads only (profiling)
+        print(json.dumps({"render": run_render(args, stream, dev)}), flush=True)
+        return
     sizes = [SIZES[s] for s in args.sizes.split(",")]
     side = args.side
     nray = side * side
@@ -332,6 +338,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scenes, specs, args.cpu_seconds)
+    for N, v, idx, acc in scenes:
+        acc.close()
+    render = run_render(args, stream, dev) if args.render else None
 
     line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
@@ -341,15 +350,100 @@ def run_ours(args):
                        "triangles": sizes, "rays_per_launch": nray, "launches_per_step": len(specs),
                        "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write); inputs > L2"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": len(specs) * args.steps,
-            "clocks": clk.summary(), "workloads": workloads}
+            "clocks": clk.summary(), "workloads": workloads, "render": render}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    for N, v, idx, acc in scenes:
-        acc.close()
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# render workloads (secondary metrics): samples/s of the integrators
+# --------------------------------------------------------------------------
+def run_render(args, stream, dev):
+    """samples/s of one progressive pass of each integrator (CUDA events over
+    `--render-passes` passes after one warm-up pass)."""
+    import torch
+
+    from zillumgl_gb300.scene import LightIntegrator, PathIntegrator, Scene, TripleIntegrator
+    from zillumgl_gb300.synthetic import city_scene, cornell_scene
+
+    out = {}
+    names = [n for n in args.render.split(",") if n]
+    for name in names:
+        t0 = time.time()
+        if name == "cornell":
+            data = cornell_scene(seed=1, width=256, height=256)
+            runs = [("path", PathIntegrator, dict(max_depth=5))]
+        elif name == "city":
+            data = city_scene(seed=2)
+            runs = [("path", PathIntegrator, dict(max_depth=8, russian_roulette=1, rr_start_depth=3)),
+                    ("light", LightIntegrator, dict(max_depth=8, russian_roulette=1, rr_start_depth=3)),
+                    ("triple", TripleIntegrator, dict(max_depth=8, russian_roulette=1, rr_start_depth=3))]
+        else:
+            raise ValueError(name)
+        scene = Scene(data)
+        W, H = data.film
+        log(f"[bench] render scene {name}: {data.obj_indices.size // 3 + data.light_indices.size // 3} tris, "
+            f"setup {time.time() - t0:.1f}s")
+        res = {"film": [W, H], "triangles": int(data.obj_indices.size // 3 + data.light_indices.size // 3)}
+        for kind, cls, params in runs:
+            integ = cls(scene, **params)
+            integ.render_one_pass(stream)  # warm-up
+            stream.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.render_passes):
+                integ.render_one_pass(stream)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / args.render_passes
+            if kind == "light":
+                paths = 32 * 1536
+                res[kind] = {"ms_per_pass": round(ms, 3), "light_paths_per_s": round(paths / (ms * 1e-3), 1)}
+            else:
+                res[kind] = {"ms_per_pass": round(ms, 3), "samples_per_s": round(W * H / (ms * 1e-3), 1)}
+                if kind == "triple":
+                    res[kind]["light_paths_per_pass"] = 64 * 1536
+            res[kind]["params"] = params
+            integ.close()
+        # end to end through the C ABI: one pass + the frame read back to pinned host memory
+        integ = PathIntegrator(scene, **runs[0][2])
+        host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+        integ.render_one_pass(stream)
+        integ.get_frame(host, stream)
+        t1 = time.perf_counter()
+        for _ in range(args.render_passes):
+            integ.render_one_pass(stream)
+            integ.get_frame(host, stream)
+        e2e_s = (time.perf_counter() - t1) / args.render_passes
+        res["path"]["e2e_samples_per_s"] = round(W * H / e2e_s, 1)
+        res["path"]["e2e_d2h_bytes_per_pass"] = W * H * 16
+        integ.close()
+        if name == "cornell" and not args.no_cpu_baseline:
+            res["path"]["cpu_baseline"] = render_cpu_baseline(data, scene, runs[0][2])
+        scene.close()
+        out[name] = res
+    return out
+
+
+def render_cpu_baseline(data, scene, params):
+    """The oracle path tracer on every host thread, one pass over a pixel sample."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    orc = oracle.OracleScene(data, scene.export("sobol"), params)
+    W, H = data.film
+    pix = np.arange(W * H, dtype=np.int32)
+    orc.render_pt(pix[:256], 1)
+    t0 = time.perf_counter()
+    orc.render_pt(pix, 1)
+    dt = time.perf_counter() - t0
+    return {"samples_per_s": round(W * H / dt, 1), "cores": nthreads, "kind": "port",
+            "sample": f"one {W}x{H} pass of the oracle path tracer ({dt:.2f}s)"}
 
 
 def cpu_baseline(scenes, specs, target_s: float):

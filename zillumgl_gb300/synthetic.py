@@ -237,3 +237,92 @@ def sky_environment(width: int, height: int, seed: int = 2, sun_dir=(0.4, -0.3, 
     scale = (peak_over_mean * img.mean() - sky_mean) if peak > 0 else 0.0
     img = sky + lobe[..., None] * np.array([1.0, 0.95, 0.85]) * max(scale, 1.0)
     return np.clip(img, 0.0, None).astype(np.float32)
+
+
+def _sphere_batch(centers, radii, segments, rings):
+    """Vertices/normals/indices of many UV spheres at once."""
+    unit_v, unit_n, unit_i = _uv_sphere((0.0, 0.0, 0.0), 1.0, segments, rings)
+    k = centers.shape[0]
+    nv = unit_v.shape[0]
+    verts = centers[:, None, :] + radii[:, None, None] * unit_v[None]
+    norms = np.broadcast_to(unit_n[None], (k, nv, 3))
+    idx = unit_i[None, :] + (np.arange(k) * nv)[:, None]
+    return verts.reshape(-1, 3), norms.reshape(-1, 3), idx.reshape(-1)
+
+
+def city_scene(seed: int = 2, width: int = 1920, height: int = 1080, grid: int = 64, n_spheres: int = 2000,
+               sphere_segments: int = 64, sphere_rings: int = 16, env_size=(2048, 1024), n_lights: int = 8):
+    """Seeded procedural city: a grid x grid block of boxes with heights
+    lognormal(0, 0.5) on a ground plane, n_spheres UV spheres (64x16 by
+    default, about 4M triangles in total) scattered above it, 16 principled
+    materials with every parameter uniform in its range, a sky-gradient plus
+    sun environment (peak/mean about 1e3) and n_lights small emissive quads
+    (the light and triple integrators sample light triangles)."""
+    from .scene import PRINCIPLED, SceneData, mat_tex, material
+
+    rng = np.random.default_rng(seed)
+    mats = [material(PRINCIPLED, base_color=rng.uniform(0, 1, 3), roughness=rng.uniform(),
+                     subsurface=rng.uniform(), metallic=rng.uniform(), specular=rng.uniform(),
+                     specular_tint=rng.uniform(), sheen=rng.uniform(), sheen_tint=rng.uniform(),
+                     clearcoat=rng.uniform(), clearcoat_gloss=rng.uniform()) for _ in range(16)]
+    vs, ns, ids, mt = [], [], [], []
+    base = 0
+
+    def add(v, n, i, m):
+        nonlocal base
+        vs.append(np.asarray(v, np.float64))
+        ns.append(np.asarray(n, np.float64))
+        ids.append(np.asarray(i, np.int64) + base)
+        mt.append(np.full(len(i) // 3, mat_tex(m), np.int32))
+        base += len(v)
+
+    # ground
+    g = float(grid)
+    v, n, i = _quad((0, 0, 0), (g, 0, 0), (g, g, 0), (0, g, 0), (0, 0, 1))
+    add(v, n, i, int(rng.integers(16)))
+    # buildings: one box per cell, 12 triangles each
+    heights = rng.lognormal(0.0, 0.5, (grid, grid))
+    foot = rng.uniform(0.55, 0.85, (grid, grid))
+    bm = rng.integers(0, 16, (grid, grid))
+    for gx in range(grid):
+        for gy in range(grid):
+            h, f = heights[gx, gy], foot[gx, gy]
+            cx, cy = gx + 0.5, gy + 0.5
+            bv, bn, bi = [], [], []
+            off = 0
+            for qv, qn, qi in _box((cx - f / 2, cy - f / 2, 0.0), (cx + f / 2, cy + f / 2, h)):
+                bv.append(qv)
+                bn.append(qn)
+                bi.append(qi + off)
+                off += 4
+            add(np.concatenate(bv), np.concatenate(bn), np.concatenate(bi), int(bm[gx, gy]))
+    # spheres, grouped by material
+    centers = np.stack([rng.uniform(0, g, n_spheres), rng.uniform(0, g, n_spheres),
+                        rng.uniform(2.0, 6.0, n_spheres)], 1)
+    radii = rng.uniform(0.1, 0.45, n_spheres)
+    sm = rng.integers(0, 16, n_spheres)
+    for m in range(16):
+        sel = sm == m
+        if sel.any():
+            v, n, i = _sphere_batch(centers[sel], radii[sel], sphere_segments, sphere_rings)
+            add(v, n, i, m)
+    # emissive quads facing down, above the city
+    lv, ln, li, lf, lp = [], [], [], [0], []
+    for k in range(n_lights):
+        x, y = rng.uniform(4, g - 4, 2)
+        z = 8.0
+        s = 0.5
+        qv, qn, qi = _quad((x - s, y - s, z), (x + s, y - s, z), (x + s, y + s, z), (x - s, y + s, z), (0, 0, -1))
+        li.append(qi + 4 * k)
+        lv.append(qv)
+        ln.append(qn)
+        lf.append(lf[-1] + 2)
+        lp.append([2.0e4, 1.8e4, 1.5e4])
+    return SceneData(
+        obj_vertices=np.concatenate(vs), obj_normals=np.concatenate(ns), obj_indices=np.concatenate(ids),
+        obj_mat_tex=np.concatenate(mt), materials=np.stack(mats),
+        light_vertices=np.concatenate(lv), light_normals=np.concatenate(ln), light_indices=np.concatenate(li),
+        light_first=np.array(lf, np.uint32), light_power=np.array(lp), film=(width, height),
+        cam_pos=(-6.0, -6.0, 14.0), cam_angle=(45.0, -28.0, 0.0), cam_fov=50.0, sampler=1,
+        env_rgb=sky_environment(env_size[0], env_size[1], seed=seed + 1), env_rotation=0.0,
+    ).normalized()
