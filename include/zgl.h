@@ -266,6 +266,59 @@ zgl_status zgl_integrator_result_scale(const zgl_integrator* integ, float* out);
 
 zgl_status zgl_integrator_destroy(zgl_integrator* integ);
 
+/* ------------------------------------------------------------------------ */
+/* Batched rendering: many requests in persistent launches                   */
+/* ------------------------------------------------------------------------ */
+
+/* One render request: `spp` path-tracer samples per pixel of `scene` (its film
+ * size and camera) into `frame`, a DEVICE buffer of filmW*filmH RGBA floats
+ * that receives the running sum, exactly what zgl_integrator_frame returns
+ * after `spp` passes of a fresh ZGL_INTEGRATOR_PATH integrator with `params`.
+ * No counterpart in the reference (its queue experiments
+ * pt_global_queue_*.glsl / pt_shared_queue.glsl are the nearest). */
+typedef struct zgl_render_request {
+    zgl_scene* scene;
+    int32_t spp;
+    zgl_integrator_params params;
+    float* frame;
+} zgl_render_request;
+
+/* Schedule of the batched renderer; 0 picks the default (or, after
+ * zgl_batch_autotune, the tuned value).  block_size: 64, 128 or 256 threads;
+ * queue_capacity: work items a warp claims per atomic fetch;
+ * regen_threshold: idle lanes a warp waits for before refilling them (1-32);
+ * samples_per_launch: samples per pixel rendered by one persistent launch (the
+ * CUDA graph holds one launch per chunk). */
+typedef struct zgl_batch_config {
+    int32_t block_size;
+    int32_t queue_capacity;
+    int32_t regen_threshold;
+    int32_t samples_per_launch;
+} zgl_batch_config;
+
+typedef struct zgl_batch zgl_batch;
+
+zgl_status zgl_batch_config_default(zgl_batch_config* config);
+
+/* Validates the requests and uploads their descriptors.  Scenes and frames
+ * are borrowed and must outlive the batch. */
+zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const zgl_batch_config* config,
+                            zgl_batch** out);
+
+/* Renders every request (all samples) as one CUDA graph, captured on the
+ * first call and replayed afterwards; ordered after prior work on `stream`,
+ * and later work on `stream` waits for it. */
+zgl_status zgl_batch_render(zgl_batch* batch, void* stream);
+
+/* Times every combination of block size, queue capacity and regeneration
+ * threshold on the first samples of the batch, keeps the fastest for later
+ * renders and returns it in `chosen` (may be NULL).  Overwrites the frames. */
+zgl_status zgl_batch_autotune(zgl_batch* batch, void* stream, zgl_batch_config* chosen);
+
+zgl_status zgl_batch_set_config(zgl_batch* batch, const zgl_batch_config* config);
+zgl_status zgl_batch_get_config(const zgl_batch* batch, zgl_batch_config* out);
+zgl_status zgl_batch_destroy(zgl_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

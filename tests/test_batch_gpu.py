@@ -1,0 +1,96 @@
+"""Batched wavefront renderer vs the plain path integrator.
+
+Each request's frame after one zgl_batch_render must equal, bit for bit, the
+frame of a fresh ZGL_INTEGRATOR_PATH integrator after `spp` passes: the
+batched schedule changes which lane renders which sample and when, not the
+arithmetic, the RNG streams or the per-pixel summation order.  Checked for
+uneven requests (scenes, film sizes, spp, depth, Russian roulette, sampler),
+for several schedules (block size, queue capacity, regeneration threshold,
+samples per launch) and after autotuning and graph replay.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from zillumgl_gb300.scene import BatchRenderer, PathIntegrator, Scene, default_params
+from zillumgl_gb300.synthetic import cornell_scene, sky_environment
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(cuda):
+    import torch
+
+    specs = [
+        (cornell_scene(seed=21, width=40, height=24), 5, dict(max_depth=5)),
+        (cornell_scene(seed=22, width=17, height=31, sampler=0), 3, dict(max_depth=3)),
+        (cornell_scene(seed=23, width=33, height=33), 7, dict(max_depth=8, russian_roulette=1, rr_start_depth=3)),
+        (cornell_scene(seed=24, width=8, height=8), 1, dict(max_depth=4)),
+    ]
+    d = cornell_scene(seed=25, width=24, height=20)
+    d.env_rgb = sky_environment(32, 16, seed=6)
+    specs.append((d.normalized(), 4, dict(max_depth=4, light_env_uniform_sample=1, light_portion=0.4)))
+    out = []
+    for data, spp, params in specs:
+        sc = Scene(data)
+        W, H = data.film
+        frame = torch.full((H, W, 4), 7.0, dtype=torch.float32, device=cuda)
+        out.append((sc, spp, params, frame))
+    return out
+
+
+def _plain(sc, spp, params):
+    integ = PathIntegrator(sc, **params)
+    for _ in range(spp):
+        integ.render_one_pass()
+    f, n = integ.get_frame()
+    integ.close()
+    return f
+
+
+@pytest.fixture(scope="module")
+def batch_setup(zgl_lib, cuda):
+    reqs = _requests(cuda)
+    refs = [_plain(sc, spp, params) for sc, spp, params, _ in reqs]
+    yield reqs, refs
+    for sc, *_ in reqs:
+        sc.close()
+
+
+def _check(reqs, refs):
+    import torch
+
+    torch.cuda.synchronize()
+    for i, ((_, _, _, frame), ref) in enumerate(zip(reqs, refs)):
+        got = frame.cpu().numpy()
+        bad = np.sum(np.any(got.view(np.uint32) != ref.view(np.uint32), axis=-1))
+        assert bad == 0, f"request {i}: {bad} pixels differ from the plain integrator"
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(),
+    dict(block_size=64, queue_capacity=8, regen_threshold=1, samples_per_launch=2),
+    dict(block_size=256, queue_capacity=128, regen_threshold=32, samples_per_launch=3),
+    dict(block_size=128, queue_capacity=1, regen_threshold=8, samples_per_launch=1),
+])
+def test_batch_equals_plain_integrator(batch_setup, cfg):
+    reqs, refs = batch_setup
+    b = BatchRenderer(reqs, **cfg)
+    b.render()
+    _check(reqs, refs)
+    # replaying the captured graph gives the same frames again
+    b.render()
+    _check(reqs, refs)
+    b.close()
+
+
+def test_autotune_then_render(batch_setup):
+    reqs, refs = batch_setup
+    b = BatchRenderer(reqs)
+    chosen = b.autotune()
+    assert chosen["block_size"] in (64, 128, 256)
+    assert b.config()["block_size"] == chosen["block_size"]
+    b.render()
+    _check(reqs, refs)
+    b.close()

@@ -69,6 +69,13 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_integrator_frame": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_integrator_result_scale": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "zgl_integrator_destroy": (C.c_int32, [C.c_void_p]),
+    "zgl_batch_config_default": (C.c_int32, [C.c_void_p]),
+    "zgl_batch_create": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "zgl_batch_render": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_batch_autotune": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_batch_set_config": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_batch_get_config": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_batch_destroy": (C.c_int32, [C.c_void_p]),
 }
 
 

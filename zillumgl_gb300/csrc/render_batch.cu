@@ -1,0 +1,612 @@
+// render_batch.cu — batched wavefront path tracing: many render requests
+// (each its own scene, film, samples per pixel and depth) in one persistent
+// launch per chunk of samples, with the chunk loop captured in a CUDA graph.
+//
+// Work items are (request, pixel) pairs; an item covers the samples of the
+// current chunk of its request.  Persistent warps claim ranges of
+// `queue_capacity` items with one atomicAdd on the chunk's work counter and
+// hand items to idle lanes with __ballot_sync/__popc, but only once at least
+// `regen_threshold` lanes are idle (or the warp has no live path), so fetches
+// are batched.  Each lane runs its path as an explicit state machine whose
+// step is one bounce (closest-hit trace, emission/MIS, Russian roulette, then
+// next-event estimation and BSDF sampling at the new vertex); a lane whose
+// path ends starts its pixel's next sample at once (path regeneration).
+//
+// The per-sample arithmetic, RNG streams and sample dimensions are those of
+// path_integ_naive.glsl (pathIntegTrace :35-143, main :145-174), and each
+// pixel's samples are summed in sample order, so a request's frame is bit
+// for bit the frame of the plain path integrator after `spp` passes from a
+// fresh start (freeCounter = sample + 1).  This batched schedule has no
+// counterpart in the reference; its nearest relatives are the queue
+// experiments pt_global_queue_*.glsl and pt_shared_queue.glsl.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "scene.h"
+#include "shading.cuh"
+#include "zgl_internal.h"
+
+namespace zgl {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct BatchPathParams {
+    int32_t maxDepth, rr, rrStart, sampleLight, uniformSel;
+    float portion;
+};
+
+struct BatchRequest {
+    DeviceScene sc;
+    BatchPathParams pp;
+    int32_t spp;
+    float4* frame;
+    int64_t itemBase;  // first work item of this request
+    int32_t npix;
+};
+
+struct BatchArgs {
+    const BatchRequest* req;
+    int32_t nreq;
+    int64_t nitems;
+    const uint32_t* sobolRows;  // [maxSpp][256]
+    int32_t chunk0, chunk1;     // samples [chunk0, chunk1) of every request
+    unsigned long long* counter;
+    int32_t queueCap;
+    int32_t regenThreshold;
+};
+
+__device__ __forceinline__ LiSample sampleLightAndEnvB(const DeviceScene& sc, const BatchPathParams& pp, v3 x,
+                                                       float ud, float u0, float u1, float u2, float u3) {
+    float pdfSampleLight = 0.0f;  // light.glsl:221-235
+    if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
+    bool sampleLight = ud < pdfSampleLight;
+    float pdfSelect = sampleLight ? pdfSampleLight : 1.0f - pdfSampleLight;
+    LiSample s;
+    if (sampleLight) {
+        int id = lightSampleOne(sc, mk2(u0, u1));
+        s = lightSampleLi(sc, id, x, mk2(u2, u3));
+    } else {
+        s = envSampleLi(sc, x, u0, u1, u2, u3);
+    }
+    s.coef = s.coef / pdfSelect;
+    s.pdf *= pdfSelect;
+    return s;
+}
+
+// Sobol values of sample row `s` come from a per-launch table instead of a
+// block-wide shared row, because lanes of one warp render different samples.
+__device__ __forceinline__ float sample1DB(Sampler& g, const uint32_t* rows, int32_t s) {
+    if (g.mode == 0) return rand01(g);
+    uint32_t r;
+    if (g.dim < 256) {
+        r = __ldg(rows + (size_t)s * 256 + g.dim);
+    } else {
+        uint32_t idx = g.sampleOffset + (uint32_t)g.dim;
+        r = sobol_value(g.mats, idx >> 8, idx & 255u);
+    }
+    r ^= g.sampleSeed;
+    g.sampleSeed = zhash(g.sampleSeed);
+    g.dim++;
+    return (float)r / 4294967296.0f;
+}
+
+struct PathState {
+    Ray ray;        // pending ray
+    v3 result, throughput;
+    v3 wo, pos;     // vertex being left (valid after the first bounce)
+    v3 bsdfOverPdf; // bsdf / pdf of the last sample (Russian roulette)
+    float bsdfPdf;
+    int32_t bounce; // 0 = camera ray pending
+    bool delta;
+};
+
+__device__ __forceinline__ uint32_t sample_offset_dev(int32_t spp) {
+    int32_t off = (int32_t)((uint32_t)spp * 256u);
+    if (off > 131072 * 256) off -= 131072 * 256;
+    return (uint32_t)off;
+}
+
+// Starts sample `s` of pixel `pix`: seeds and the camera ray (main(),
+// path_integ_naive.glsl:145-166).
+__device__ __forceinline__ void start_sample(const BatchRequest& rq, const uint32_t* rows, int pix, int32_t s,
+                                             Sampler& g, PathState& st) {
+    const DeviceScene& sc = rq.sc;
+    const int px = pix % sc.filmW, py = pix / sc.filmW;
+    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+    const uint32_t freeCounter = (uint32_t)s + 1u;
+    g.randSeed = seed.x * freeCounter + seed.y;
+    g.sampleSeed = seed.x * seed.y;
+    g.sampleOffset = sample_offset_dev(s);
+    g.dim = 0;
+    g.mode = sc.sampler;
+    g.rowCache = nullptr;
+    g.mats = sc.sobol;
+    v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    float u0 = sample1DB(g, rows, s), u1 = sample1DB(g, rows, s), u2 = sample1DB(g, rows, s),
+          u3 = sample1DB(g, rows, s);
+    st.ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    st.result = mk3(0.0f);
+    st.throughput = mk3(1.0f);
+    st.bounce = 0;
+}
+
+// One step of pathIntegTrace: trace the pending ray, account for what it hits,
+// and, if the path continues, shade the new vertex (light sample + BSDF
+// sample) to produce the next pending ray.  Returns false when the path ends.
+__device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t* rows, int32_t s, Sampler& g,
+                                          PathState& st) {
+    const DeviceScene& sc = rq.sc;
+    const BatchPathParams& pp = rq.pp;
+    float dist;
+    int id = bvhHit(sc, st.ray, dist);
+    v3 hitPos = rayPoint(st.ray, dist);
+    if (st.bounce == 0) {
+        // primary hit (path_integ_naive.glsl:37-44)
+        if (id == -1) {
+            st.result = envLe(sc, st.ray.dir);
+            return false;
+        }
+        if (id - sc.objPrimCount >= 0) {
+            st.result = lightLe(sc, id - sc.objPrimCount, hitPos, -st.ray.dir);
+            return false;
+        }
+        st.wo = -st.ray.dir;
+    } else {
+        // extension hit of bounce st.bounce (path_integ_naive.glsl:97-133)
+        v3 wi = st.ray.dir;
+        int lightId = id - sc.objPrimCount;
+        if (id == -1) {
+            v3 radiance = envLe(sc, wi);
+            float weight = 1.0f;
+            if (pp.sampleLight && !st.delta) {
+                float envPdf = envPdfLi(sc, wi) * (pp.uniformSel ? (1.0f - pp.portion)
+                                                                 : sc.envSum / (sc.lightSum + sc.envSum));
+                weight = (envPdf <= 0.0f) ? 0.0f : biHeuristic(st.bsdfPdf, envPdf);
+            }
+            st.result = st.result + radiance * st.throughput * weight;
+            return false;
+        }
+        if (lightId >= 0) {
+            v3 radiance = lightLe(sc, lightId, hitPos, -wi);
+            float weight = 1.0f;
+            if (pp.sampleLight && !st.delta) {
+                float snd = pp.uniformSel ? pp.portion : sc.lightSum / (sc.lightSum + sc.envSum);
+                float lightPdf = lightPdfLi(sc, lightId, st.pos, hitPos) * (lightPdfSampleOne(sc, lightId) * snd);
+                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(st.bsdfPdf, lightPdf);
+            }
+            st.result = st.result + radiance * st.throughput * weight;
+            return false;
+        }
+        if (pp.rr && st.bounce >= pp.rrStart) {
+            float continueProb = zmin(maxComponent(st.bsdfOverPdf), 0.95f);
+            if (sample1DB(g, rows, s) >= continueProb) return false;
+            st.throughput = st.throughput / continueProb;
+        }
+        st.wo = -wi;
+    }
+    // next bounce at the new vertex
+    st.bounce++;
+    if (st.bounce > pp.maxDepth) return false;
+    st.pos = hitPos;
+    TriShade tri = loadTri(sc, id);
+    Surface surf = surfaceInfo(tri, hitPos);
+    int matId = tri.matTex & 0x0000ffff;
+    uint32_t matType = loadMaterialType(sc, matId);
+    if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, st.wo) < 0.0f) {
+        surf.ns = -surf.ns;
+        surf.ng = -surf.ng;
+    }
+    BSDFParam mp = loadMaterial(sc, matType, matId);
+    if (pp.sampleLight) {
+        float ud = sample1DB(g, rows, s);
+        float u0 = sample1DB(g, rows, s), u1 = sample1DB(g, rows, s), u2 = sample1DB(g, rows, s),
+              u3 = sample1DB(g, rows, s);
+        LiSample ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3);
+        if (ls.pdf > 0.0f) {
+            v3 f = materialBSDF(matType, mp, st.wo, ls.wi, surf.ns);
+            float fpdf = materialPdf(matType, mp, st.wo, ls.wi, surf.ns);
+            float weight = biHeuristic(ls.pdf, fpdf);
+            st.result = st.result + f * st.throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+        }
+    }
+    float b0 = sample1DB(g, rows, s), b1 = sample1DB(g, rows, s), b2 = sample1DB(g, rows, s);
+    BSDFSample bs = materialSample(matType, mp, surf.ns, st.wo, mk3(b0, b1, b2), g);
+    st.delta = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+    if (bs.pdf < 1e-8f) return false;
+    st.throughput = st.throughput * (bs.bsdf / bs.pdf * (st.delta ? 1.0f : absDot(surf.ns, bs.wi)));
+    st.bsdfPdf = bs.pdf;
+    st.bsdfOverPdf = bs.bsdf / bs.pdf;
+    st.ray = rayOffseted(hitPos, bs.wi);
+    return true;
+}
+
+__device__ __forceinline__ int find_request(const BatchArgs& a, int64_t item) {
+    int lo = 0, hi = a.nreq - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (a.req[mid].itemBase <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) batch_kernel(BatchArgs a) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    // warp-uniform: claimed but not yet handed-out work items [qnext, qend)
+    int64_t qnext = 0, qend = 0;
+    bool exhausted = false;
+    // lane state
+    bool live = false;  // holds a work item with samples left
+    int rid = 0, pix = 0;
+    int32_t s = 0, s1 = 0;
+    v3 acc = mk3(0.0f);
+    bool wrote = false;
+    Sampler g;
+    PathState st;
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !live);
+        const int nidle = __popc(idle);
+        const int64_t tail = qend - qnext;
+        if (nidle != 0 && (nidle >= a.regenThreshold || nidle == 32) && (!exhausted || tail > 0)) {
+            // idle lanes take the leftover of the claimed range first, then a
+            // freshly claimed range of queueCap items (one atomic per claim)
+            int64_t nb = 0, nlen = 0;
+            if (!exhausted && tail < nidle) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(a.counter, (unsigned long long)a.queueCap);
+                b = __shfl_sync(kFull, b, 0);
+                if ((int64_t)b >= a.nitems) {
+                    exhausted = true;
+                } else {
+                    nb = (int64_t)b;
+                    nlen = min((int64_t)a.queueCap, a.nitems - nb);
+                }
+            }
+            if (!live) {
+                const int r = __popc(idle & lt);
+                int64_t item = -1;
+                if (r < tail) item = qnext + r;
+                else if (r - tail < nlen) item = nb + (r - tail);
+                if (item >= 0) {
+                    rid = find_request(a, item);
+                    const BatchRequest& rq = a.req[rid];
+                    pix = (int)(item - rq.itemBase);
+                    s = a.chunk0;
+                    s1 = min(a.chunk1, rq.spp);
+                    if (s < s1) {
+                        live = true;
+                        acc = mk3(0.0f);
+                        wrote = false;
+                        if (s > 0) {  // continue the sum of the previous chunks
+                            float4 f = rq.frame[pix];
+                            acc = mk3(f.x, f.y, f.z);
+                            wrote = f.w != 0.0f;
+                        }
+                        start_sample(rq, a.sobolRows, pix, s, g, st);
+                    }
+                }
+            }
+            const int64_t used = min((int64_t)nidle, tail + nlen);
+            if (used <= tail) {
+                qnext += used;
+            } else {
+                qnext = nb + (used - tail);
+                qend = nb + nlen;
+            }
+        }
+        if (__ballot_sync(kFull, live) == 0u) {
+            if (exhausted && qnext >= qend) break;
+            continue;
+        }
+        if (live) {
+            const BatchRequest& rq = a.req[rid];
+            if (!path_step(rq, a.sobolRows, s, g, st)) {
+                // the sample is complete; main() drops NaN samples
+                if (!hasNan(st.result)) {
+                    acc = acc + st.result;
+                    wrote = true;
+                }
+                s++;
+                if (s < s1) {
+                    start_sample(rq, a.sobolRows, pix, s, g, st);
+                } else {
+                    if (wrote) rq.frame[pix] = make_float4(acc.x, acc.y, acc.z, 1.0f);
+                    live = false;
+                }
+            }
+        }
+    }
+}
+
+int occupancy_grid(const void* kernel, int block) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    return sms * std::max(per_sm, 1);
+}
+
+cudaError_t launch_batch(const BatchArgs& a, int block, cudaStream_t st) {
+    switch (block) {
+        case 64:
+            batch_kernel<64><<<occupancy_grid((const void*)batch_kernel<64>, 64), 64, 0, st>>>(a);
+            break;
+        case 256:
+            batch_kernel<256><<<occupancy_grid((const void*)batch_kernel<256>, 256), 256, 0, st>>>(a);
+            break;
+        default:
+            batch_kernel<128><<<occupancy_grid((const void*)batch_kernel<128>, 128), 128, 0, st>>>(a);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace zgl
+
+struct zgl_batch {
+    int device = 0;
+    int32_t nreq = 0;
+    int64_t nitems = 0;
+    int32_t maxSpp = 0;
+    std::vector<zgl::BatchRequest> req;
+    zgl::BatchRequest* d_req = nullptr;
+    uint32_t* d_rows = nullptr;
+    unsigned long long* d_counters = nullptr;
+    int32_t nchunks_cap = 0;
+    zgl_batch_config cfg{};
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    zgl_batch_config graph_cfg{};
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+};
+
+namespace zgl {
+namespace {
+
+void batch_free(zgl_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->ev_in) cudaEventDestroy(b->ev_in);
+    if (b->ev_out) cudaEventDestroy(b->ev_out);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->d_req) cudaFree(b->d_req);
+    if (b->d_rows) cudaFree(b->d_rows);
+    if (b->d_counters) cudaFree(b->d_counters);
+    delete b;
+}
+
+zgl_batch_config resolve(const zgl_batch_config& c, int32_t maxSpp) {
+    zgl_batch_config r = c;
+    if (r.block_size == 0) r.block_size = 128;
+    if (r.queue_capacity == 0) r.queue_capacity = 32;
+    if (r.regen_threshold == 0) r.regen_threshold = 16;
+    if (r.samples_per_launch == 0 || r.samples_per_launch > maxSpp) r.samples_per_launch = maxSpp;
+    return r;
+}
+
+void check_config(const zgl_batch_config& c) {
+    if (c.block_size != 0 && c.block_size != 64 && c.block_size != 128 && c.block_size != 256)
+        fail(ZGL_ERR_INVALID_ARG, "batch: block_size must be 64, 128 or 256");
+    if (c.queue_capacity < 0 || c.queue_capacity > 4096) fail(ZGL_ERR_INVALID_ARG, "batch: queue_capacity out of range");
+    if (c.regen_threshold < 0 || c.regen_threshold > 32) fail(ZGL_ERR_INVALID_ARG, "batch: regen_threshold out of range");
+    if (c.samples_per_launch < 0) fail(ZGL_ERR_INVALID_ARG, "batch: samples_per_launch out of range");
+}
+
+// Enqueues the whole render (frame clears, one counter reset and one
+// persistent launch per chunk of samples) on `st`; `first_chunk_only` renders
+// only the first chunk (autotuning).
+void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, bool first_chunk_only) {
+    for (const auto& r : b->req)
+        ZGL_CUDA(cudaMemsetAsync(r.frame, 0, sizeof(float4) * (size_t)r.npix, st));
+    int nchunks = (b->maxSpp + c.samples_per_launch - 1) / c.samples_per_launch;
+    if (first_chunk_only) nchunks = std::min(nchunks, 1);
+    if (nchunks > b->nchunks_cap) fail(ZGL_ERR_STATE, "batch: chunk count exceeds the counter array");
+    for (int k = 0; k < nchunks; k++) {
+        BatchArgs a;
+        a.req = b->d_req;
+        a.nreq = b->nreq;
+        a.nitems = b->nitems;
+        a.sobolRows = b->d_rows;
+        a.chunk0 = k * c.samples_per_launch;
+        a.chunk1 = std::min(b->maxSpp, (k + 1) * c.samples_per_launch);
+        a.counter = b->d_counters + k;
+        a.queueCap = c.queue_capacity;
+        a.regenThreshold = c.regen_threshold;
+        ZGL_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st));
+        ZGL_CUDA(launch_batch(a, c.block_size, st));
+    }
+}
+
+bool same_cfg(const zgl_batch_config& x, const zgl_batch_config& y) {
+    return x.block_size == y.block_size && x.queue_capacity == y.queue_capacity &&
+           x.regen_threshold == y.regen_threshold && x.samples_per_launch == y.samples_per_launch;
+}
+
+}  // namespace
+}  // namespace zgl
+
+using namespace zgl;
+
+extern "C" {
+
+zgl_status zgl_batch_config_default(zgl_batch_config* c) {
+    ZGL_API_BEGIN
+    if (!c) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_config_default: NULL");
+    std::memset(c, 0, sizeof(*c));
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const zgl_batch_config* config,
+                            zgl_batch** out) {
+    ZGL_API_BEGIN
+    if (!requests || !out || n <= 0) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_create: empty request list");
+    *out = nullptr;
+    zgl_batch_config cfg{};
+    if (config) cfg = *config;
+    check_config(cfg);
+    auto* b = new zgl_batch();
+    try {
+        ZGL_CUDA(cudaGetDevice(&b->device));
+        b->nreq = n;
+        int64_t base = 0;
+        for (int i = 0; i < n; i++) {
+            const zgl_render_request& r = requests[i];
+            if (!r.scene || !r.frame) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_create: request %d lacks scene or frame", i);
+            if (r.scene->host_only) fail(ZGL_ERR_STATE, "zgl_batch_create: request %d scene is host-only", i);
+            if (r.scene->device != b->device) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_create: request %d on another device", i);
+            if (r.spp < 1 || r.spp > 65536) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_create: request %d spp %d out of range", i, r.spp);
+            zgl_integrator_params p = r.params;
+            if (p.max_depth < 0 || p.max_depth > 1024 || p.rr_start_depth < 1 || !(p.light_portion >= 0.0f && p.light_portion <= 1.0f))
+                fail(ZGL_ERR_INVALID_ARG, "zgl_batch_create: request %d has invalid parameters", i);
+            BatchRequest q{};
+            q.sc = r.scene->view();
+            q.pp = BatchPathParams{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light,
+                                   p.light_env_uniform_sample, p.light_portion};
+            q.spp = r.spp;
+            q.frame = reinterpret_cast<float4*>(r.frame);
+            q.npix = r.scene->filmW * r.scene->filmH;
+            q.itemBase = base;
+            base += q.npix;
+            b->maxSpp = std::max(b->maxSpp, r.spp);
+            b->req.push_back(q);
+        }
+        b->nitems = base;
+        ZGL_CUDA(cudaMalloc(&b->d_req, sizeof(BatchRequest) * (size_t)n));
+        ZGL_CUDA(cudaMemcpy(b->d_req, b->req.data(), sizeof(BatchRequest) * (size_t)n, cudaMemcpyHostToDevice));
+        // Sobol values of rows 0 .. maxSpp-1 (sample index s uses row s)
+        std::vector<uint32_t> mats;
+        sobol_matrices(mats);
+        std::vector<uint32_t> rows((size_t)b->maxSpp * 256);
+        for (int sidx = 0; sidx < b->maxSpp; sidx++)
+            for (int d = 0; d < 256; d++) {
+                uint32_t r = 0, idx = (uint32_t)sidx;
+                for (int i = 0; idx != 0; idx >>= 1, i++)
+                    if (idx & 1u) r ^= mats[(size_t)d * 32 + i];
+                rows[(size_t)sidx * 256 + d] = r;
+            }
+        ZGL_CUDA(cudaMalloc(&b->d_rows, sizeof(uint32_t) * rows.size()));
+        ZGL_CUDA(cudaMemcpy(b->d_rows, rows.data(), sizeof(uint32_t) * rows.size(), cudaMemcpyHostToDevice));
+        b->nchunks_cap = b->maxSpp;
+        ZGL_CUDA(cudaMalloc(&b->d_counters, sizeof(unsigned long long) * (size_t)b->nchunks_cap));
+        ZGL_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        ZGL_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming));
+        ZGL_CUDA(cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming));
+        b->cfg = resolve(cfg, b->maxSpp);
+    } catch (...) {
+        batch_free(b);
+        throw;
+    }
+    *out = b;
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_set_config(zgl_batch* b, const zgl_batch_config* config) {
+    ZGL_API_BEGIN
+    if (!b || !config) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_set_config: NULL");
+    check_config(*config);
+    b->cfg = resolve(*config, b->maxSpp);
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_get_config(const zgl_batch* b, zgl_batch_config* out) {
+    ZGL_API_BEGIN
+    if (!b || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_get_config: NULL");
+    *out = b->cfg;
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_render(zgl_batch* b, void* stream) {
+    ZGL_API_BEGIN
+    if (!b) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_render: NULL");
+    cudaStream_t user = (cudaStream_t)stream;
+    if (!b->exec || !same_cfg(b->graph_cfg, b->cfg)) {
+        if (b->exec) {
+            ZGL_CUDA(cudaGraphExecDestroy(b->exec));
+            b->exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        ZGL_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_render(b, b->cfg, b->stream, false);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(b->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        ZGL_CUDA(cudaStreamEndCapture(b->stream, &graph));
+        cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ZGL_CUDA(e);
+        b->graph_cfg = b->cfg;
+    }
+    // order the graph after the caller's stream and the caller's stream after it
+    ZGL_CUDA(cudaEventRecord(b->ev_in, user));
+    ZGL_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+    ZGL_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    ZGL_CUDA(cudaEventRecord(b->ev_out, b->stream));
+    ZGL_CUDA(cudaStreamWaitEvent(user, b->ev_out, 0));
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chosen) {
+    ZGL_API_BEGIN
+    if (!b) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_autotune: NULL");
+    cudaStream_t st = b->stream;
+    ZGL_CUDA(cudaEventRecord(b->ev_in, (cudaStream_t)stream));
+    ZGL_CUDA(cudaStreamWaitEvent(st, b->ev_in, 0));
+    cudaEvent_t e0, e1;
+    ZGL_CUDA(cudaEventCreate(&e0));
+    ZGL_CUDA(cudaEventCreate(&e1));
+    const int blocks[] = {64, 128, 256};
+    const int caps[] = {8, 32, 128};
+    const int thresholds[] = {4, 16, 32};
+    zgl_batch_config best = b->cfg;
+    float bestMs = 1e30f;
+    int chunk = std::min(b->maxSpp, 2);  // time the first two samples of every request
+    try {
+        for (int bs : blocks)
+            for (int cap : caps)
+                for (int th : thresholds) {
+                    zgl_batch_config c = b->cfg;
+                    c.block_size = bs;
+                    c.queue_capacity = cap;
+                    c.regen_threshold = th;
+                    c.samples_per_launch = chunk;
+                    ZGL_CUDA(cudaEventRecord(e0, st));
+                    enqueue_render(b, c, st, true);
+                    ZGL_CUDA(cudaEventRecord(e1, st));
+                    ZGL_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.0f;
+                    ZGL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < bestMs) {
+                        bestMs = ms;
+                        best = c;
+                    }
+                }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    best.samples_per_launch = b->cfg.samples_per_launch;
+    b->cfg = best;
+    if (chosen) *chosen = best;
+    ZGL_API_END
+}
+
+zgl_status zgl_batch_destroy(zgl_batch* b) {
+    ZGL_API_BEGIN
+    if (b) cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    ZGL_API_END
+}
+
+}  // extern "C"

@@ -275,3 +275,77 @@ class TripleIntegrator(PathIntegrator):
     (s=0) + (s=1) + (t=1) strategies, camera pass then light pass."""
 
     KIND = 2
+
+
+class RenderRequest(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("spp", C.c_int32), ("params", IntegratorParams), ("frame", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("queue_capacity", C.c_int32), ("regen_threshold", C.c_int32),
+                ("samples_per_launch", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchRenderer:
+    """Many path-tracing requests in persistent launches (zgl_batch_*).
+
+    ``requests`` is a list of ``(scene, spp, params, frame)`` with ``frame`` a
+    CUDA float32 tensor of shape (H, W, 4); after :meth:`render` each frame
+    holds what :class:`PathIntegrator` holds after ``spp`` passes."""
+
+    def __init__(self, requests, **config):
+        from .accel import _ptr
+
+        arr = (RenderRequest * len(requests))()
+        self._keep = []
+        for i, (scene, spp, params, frame) in enumerate(requests):
+            arr[i].scene = scene.handle.value
+            arr[i].spp = spp
+            arr[i].params = params if isinstance(params, IntegratorParams) else default_params(**params)
+            arr[i].frame = _ptr(frame)
+            self._keep.append((scene, frame))
+        cfg = BatchConfig()
+        call("zgl_batch_config_default", C.byref(cfg))
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        h = C.c_void_p()
+        call("zgl_batch_create", arr, len(requests), C.byref(cfg), C.byref(h))
+        self._h = h
+
+    def render(self, stream=None) -> None:
+        from .accel import _stream_handle
+
+        call("zgl_batch_render", self._h, _stream_handle(stream))
+
+    def autotune(self, stream=None) -> dict:
+        from .accel import _stream_handle
+
+        cfg = BatchConfig()
+        call("zgl_batch_autotune", self._h, _stream_handle(stream), C.byref(cfg))
+        return cfg.as_dict()
+
+    def config(self) -> dict:
+        cfg = BatchConfig()
+        call("zgl_batch_get_config", self._h, C.byref(cfg))
+        return cfg.as_dict()
+
+    def set_config(self, **config) -> None:
+        cfg = BatchConfig()
+        call("zgl_batch_get_config", self._h, C.byref(cfg))
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        call("zgl_batch_set_config", self._h, C.byref(cfg))
+
+    def close(self):
+        if self._h:
+            call("zgl_batch_destroy", self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
