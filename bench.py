@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent"])
     ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
-    ap.add_argument("--render", default="cornell,city", help="render workloads to time ('' for none)")
+    ap.add_argument("--render", default="cornell,city,batch", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
     ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
     return ap.parse_args()
@@ -374,6 +374,9 @@ def run_render(args, stream, dev):
     names = [n for n in args.render.split(",") if n]
     for name in names:
         t0 = time.time()
+        if name == "batch":
+            out[name] = run_batch(args, stream, dev)
+            continue
         if name == "cornell":
             data = cornell_scene(seed=1, width=256, height=256)
             runs = [("path", PathIntegrator, dict(max_depth=5))]
@@ -428,6 +431,72 @@ def run_render(args, stream, dev):
         scene.close()
         out[name] = res
     return out
+
+
+def run_batch(args, stream, dev):
+    """Batched serving: 64 seeded requests (1k-500k triangles, 128^2-1024^2,
+    4-64 spp, depth 4-8).  Plain = one path-tracer launch per request per
+    pass; batched = the persistent wavefront renderer (autotuned, graph).
+    Both produce the same frames bit for bit."""
+    import torch
+
+    from zillumgl_gb300.scene import BatchRenderer, PathIntegrator, Scene
+    from zillumgl_gb300.synthetic import batch_requests
+
+    t0 = time.time()
+    reqs = batch_requests(seed=3, n=64)
+    scenes, frames, total = [], [], 0
+    for data, spp, params in reqs:
+        scenes.append(Scene(data))
+        W, H = data.film
+        frames.append(torch.zeros((H, W, 4), dtype=torch.float32, device=dev))
+        total += W * H * spp
+    log(f"[bench] batch: {len(reqs)} requests, {total / 1e6:.1f}M samples, setup {time.time() - t0:.1f}s")
+    # plain: one integrator per request, one launch per pass
+    integs = [PathIntegrator(sc, **params) for sc, (_, _, params) in zip(scenes, reqs)]
+    integs[0].render_one_pass(stream)
+    stream.synchronize()
+    for it in integs:
+        it.close()
+    integs = [PathIntegrator(sc, **params) for sc, (_, _, params) in zip(scenes, reqs)]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for it, (_, spp, _) in zip(integs, reqs):
+        for _ in range(spp):
+            it.render_one_pass(stream)
+    e1.record(stream)
+    stream.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    launches_plain = sum(spp for _, spp, _ in reqs)
+    # batched
+    batch = BatchRenderer([(sc, spp, params, fr) for sc, (_, spp, params), fr in zip(scenes, reqs, frames)])
+    t1 = time.time()
+    tuned = batch.autotune(stream)
+    tune_s = time.time() - t1
+    batch.render(stream)  # captures the graph
+    stream.synchronize()
+    e0.record(stream)
+    batch.render(stream)
+    e1.record(stream)
+    stream.synchronize()
+    batch_ms = e0.elapsed_time(e1)
+    # spot check: the batched frames equal the plain ones
+    same = 0
+    for it, fr in zip(integs[:4], frames[:4]):
+        f, _ = it.get_frame()
+        same += int(np.array_equal(f.view(np.uint32), fr.cpu().numpy().view(np.uint32)))
+    for it in integs:
+        it.close()
+    batch.close()
+    for sc in scenes:
+        sc.close()
+    return {"requests": len(reqs), "samples": total,
+            "plain": {"ms": round(plain_ms, 2), "samples_per_s": round(total / (plain_ms * 1e-3), 1),
+                      "launches": launches_plain},
+            "batched": {"ms": round(batch_ms, 2), "samples_per_s": round(total / (batch_ms * 1e-3), 1),
+                        "config": tuned, "autotune_s": round(tune_s, 2)},
+            "speedup": round(plain_ms / batch_ms, 3), "frames_bit_identical_checked": f"{same}/4"}
 
 
 def render_cpu_baseline(data, scene, params):

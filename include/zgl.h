@@ -286,14 +286,13 @@ typedef struct zgl_render_request {
 /* Schedule of the batched renderer; 0 picks the default (or, after
  * zgl_batch_autotune, the tuned value).  block_size: 64, 128 or 256 threads;
  * queue_capacity: work items a warp claims per atomic fetch;
- * regen_threshold: idle lanes a warp waits for before refilling them (1-32);
- * samples_per_launch: samples per pixel rendered by one persistent launch (the
- * CUDA graph holds one launch per chunk). */
+ * regen_threshold: idle lanes a warp waits for before refilling them (1-32).
+ * The CUDA graph holds one persistent launch per sample index (per group of
+ * up to 64 requests that still need that sample). */
 typedef struct zgl_batch_config {
     int32_t block_size;
     int32_t queue_capacity;
     int32_t regen_threshold;
-    int32_t samples_per_launch;
 } zgl_batch_config;
 
 typedef struct zgl_batch zgl_batch;

@@ -5,8 +5,8 @@ frame of a fresh ZGL_INTEGRATOR_PATH integrator after `spp` passes: the
 batched schedule changes which lane renders which sample and when, not the
 arithmetic, the RNG streams or the per-pixel summation order.  Checked for
 uneven requests (scenes, film sizes, spp, depth, Russian roulette, sampler),
-for several schedules (block size, queue capacity, regeneration threshold,
-samples per launch) and after autotuning and graph replay.
+for several schedules (block size, queue capacity, regeneration threshold)
+and after autotuning and graph replay.
 """
 from __future__ import annotations
 
@@ -70,9 +70,9 @@ def _check(reqs, refs):
 
 @pytest.mark.parametrize("cfg", [
     dict(),
-    dict(block_size=64, queue_capacity=8, regen_threshold=1, samples_per_launch=2),
-    dict(block_size=256, queue_capacity=128, regen_threshold=32, samples_per_launch=3),
-    dict(block_size=128, queue_capacity=1, regen_threshold=8, samples_per_launch=1),
+    dict(block_size=64, queue_capacity=8, regen_threshold=1),
+    dict(block_size=256, queue_capacity=128, regen_threshold=32),
+    dict(block_size=128, queue_capacity=1, regen_threshold=8),
 ])
 def test_batch_equals_plain_integrator(batch_setup, cfg):
     reqs, refs = batch_setup

@@ -1,22 +1,25 @@
 // render_batch.cu — batched wavefront path tracing: many render requests
-// (each its own scene, film, samples per pixel and depth) in one persistent
-// launch per chunk of samples, with the chunk loop captured in a CUDA graph.
+// (each its own scene, film, samples per pixel and depth) rendered by
+// persistent launches, one per sample index, captured in one CUDA graph.
 //
-// Work items are (request, pixel) pairs; an item covers the samples of the
-// current chunk of its request.  Persistent warps claim ranges of
-// `queue_capacity` items with one atomicAdd on the chunk's work counter and
-// hand items to idle lanes with __ballot_sync/__popc, but only once at least
-// `regen_threshold` lanes are idle (or the warp has no live path), so fetches
-// are batched.  Each lane runs its path as an explicit state machine whose
-// step is one bounce (closest-hit trace, emission/MIS, Russian roulette, then
-// next-event estimation and BSDF sampling at the new vertex); a lane whose
-// path ends starts its pixel's next sample at once (path regeneration).
+// A launch renders sample s of every request that still needs it.  Its work
+// items are the pixels of those requests in 8x4 tiles, so a warp's lanes hold
+// neighbouring pixels of one sample.  Persistent warps claim ranges of
+// `queue_capacity` items with one atomicAdd on the launch's work counter and
+// hand them to idle lanes with __ballot_sync/__popc once at least
+// `regen_threshold` lanes are idle (or none is live).  Each lane runs its path
+// as an explicit state machine whose step is one bounce (closest-hit trace,
+// emission/MIS, Russian roulette, then next-event estimation and BSDF
+// sampling at the new vertex); a lane whose path ends takes the next pixel at
+// once (path regeneration).  Request descriptors travel in the kernel
+// parameter block (up to 64 per launch), the sample's Sobol row sits in
+// shared memory.
 //
 // The per-sample arithmetic, RNG streams and sample dimensions are those of
-// path_integ_naive.glsl (pathIntegTrace :35-143, main :145-174), and each
-// pixel's samples are summed in sample order, so a request's frame is bit
-// for bit the frame of the plain path integrator after `spp` passes from a
-// fresh start (freeCounter = sample + 1).  This batched schedule has no
+// path_integ_naive.glsl (pathIntegTrace :35-143, main :145-174), launches run
+// in sample order and each pixel has one owner per launch, so a request's
+// frame is bit for bit the frame of the plain path integrator after `spp`
+// passes from a fresh start (freeCounter = sample + 1).  This batched schedule has no
 // counterpart in the reference; its nearest relatives are the queue
 // experiments pt_global_queue_*.glsl and pt_shared_queue.glsl.
 #include <algorithm>
@@ -42,20 +45,25 @@ struct BatchRequest {
     BatchPathParams pp;
     int32_t spp;
     float4* frame;
-    int64_t itemBase;  // first work item of this request
+    int64_t itemBase;  // first work item of this request in its launch
     int32_t npix;
+    int32_t tilesX;    // 8x4 pixel tiles per film row
 };
 
-struct BatchArgs {
-    const BatchRequest* req;
+constexpr int kMaxReqPerLaunch = 64;
+
+struct BatchLaunch {
+    BatchRequest req[kMaxReqPerLaunch];
     int32_t nreq;
     int64_t nitems;
-    const uint32_t* sobolRows;  // [maxSpp][256]
-    int32_t chunk0, chunk1;     // samples [chunk0, chunk1) of every request
+    int32_t s;              // sample index of this launch
+    uint32_t sampleOffset;  // s * 256, wrapped (path_integ_naive.glsl:163-164)
     unsigned long long* counter;
     int32_t queueCap;
     int32_t regenThreshold;
+    const uint32_t* mats;   // Sobol generator matrices
 };
+static_assert(sizeof(BatchLaunch) <= 32000, "kernel parameter block too large");
 
 __device__ __forceinline__ LiSample sampleLightAndEnvB(const DeviceScene& sc, const BatchPathParams& pp, v3 x,
                                                        float ud, float u0, float u1, float u2, float u3) {
@@ -75,23 +83,6 @@ __device__ __forceinline__ LiSample sampleLightAndEnvB(const DeviceScene& sc, co
     return s;
 }
 
-// Sobol values of sample row `s` come from a per-launch table instead of a
-// block-wide shared row, because lanes of one warp render different samples.
-__device__ __forceinline__ float sample1DB(Sampler& g, const uint32_t* rows, int32_t s) {
-    if (g.mode == 0) return rand01(g);
-    uint32_t r;
-    if (g.dim < 256) {
-        r = __ldg(rows + (size_t)s * 256 + g.dim);
-    } else {
-        uint32_t idx = g.sampleOffset + (uint32_t)g.dim;
-        r = sobol_value(g.mats, idx >> 8, idx & 255u);
-    }
-    r ^= g.sampleSeed;
-    g.sampleSeed = zhash(g.sampleSeed);
-    g.dim++;
-    return (float)r / 4294967296.0f;
-}
-
 struct PathState {
     Ray ray;        // pending ray
     v3 result, throughput;
@@ -108,24 +99,22 @@ __device__ __forceinline__ uint32_t sample_offset_dev(int32_t spp) {
     return (uint32_t)off;
 }
 
-// Starts sample `s` of pixel `pix`: seeds and the camera ray (main(),
+// Starts sample `s` of pixel (px, py): seeds and the camera ray (main(),
 // path_integ_naive.glsl:145-166).
-__device__ __forceinline__ void start_sample(const BatchRequest& rq, const uint32_t* rows, int pix, int32_t s,
-                                             Sampler& g, PathState& st) {
+__device__ __forceinline__ void start_sample(const BatchRequest& rq, const BatchLaunch& L, const uint32_t* row,
+                                             int px, int py, Sampler& g, PathState& st) {
     const DeviceScene& sc = rq.sc;
-    const int px = pix % sc.filmW, py = pix / sc.filmW;
-    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
-    const uint32_t freeCounter = (uint32_t)s + 1u;
+    const uint2 seed = __ldg(&sc.pixelSeeds[(size_t)py * sc.filmW + px]);
+    const uint32_t freeCounter = (uint32_t)L.s + 1u;
     g.randSeed = seed.x * freeCounter + seed.y;
     g.sampleSeed = seed.x * seed.y;
-    g.sampleOffset = sample_offset_dev(s);
+    g.sampleOffset = L.sampleOffset;
     g.dim = 0;
     g.mode = sc.sampler;
-    g.rowCache = nullptr;
-    g.mats = sc.sobol;
+    g.rowCache = row;
+    g.mats = L.mats;
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
-    float u0 = sample1DB(g, rows, s), u1 = sample1DB(g, rows, s), u2 = sample1DB(g, rows, s),
-          u3 = sample1DB(g, rows, s);
+    float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     st.ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
     st.result = mk3(0.0f);
     st.throughput = mk3(1.0f);
@@ -135,8 +124,7 @@ __device__ __forceinline__ void start_sample(const BatchRequest& rq, const uint3
 // One step of pathIntegTrace: trace the pending ray, account for what it hits,
 // and, if the path continues, shade the new vertex (light sample + BSDF
 // sample) to produce the next pending ray.  Returns false when the path ends.
-__device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t* rows, int32_t s, Sampler& g,
-                                          PathState& st) {
+__device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, PathState& st) {
     const DeviceScene& sc = rq.sc;
     const BatchPathParams& pp = rq.pp;
     float dist;
@@ -181,7 +169,7 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t
         }
         if (pp.rr && st.bounce >= pp.rrStart) {
             float continueProb = zmin(maxComponent(st.bsdfOverPdf), 0.95f);
-            if (sample1DB(g, rows, s) >= continueProb) return false;
+            if (sample1D(g) >= continueProb) return false;
             st.throughput = st.throughput / continueProb;
         }
         st.wo = -wi;
@@ -200,9 +188,9 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t
     }
     BSDFParam mp = loadMaterial(sc, matType, matId);
     if (pp.sampleLight) {
-        float ud = sample1DB(g, rows, s);
-        float u0 = sample1DB(g, rows, s), u1 = sample1DB(g, rows, s), u2 = sample1DB(g, rows, s),
-              u3 = sample1DB(g, rows, s);
+        float ud = sample1D(g);
+        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g),
+              u3 = sample1D(g);
         LiSample ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3);
         if (ls.pdf > 0.0f) {
             v3 f = materialBSDF(matType, mp, st.wo, ls.wi, surf.ns);
@@ -211,7 +199,7 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t
             st.result = st.result + f * st.throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
         }
     }
-    float b0 = sample1DB(g, rows, s), b1 = sample1DB(g, rows, s), b2 = sample1DB(g, rows, s);
+    float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
     BSDFSample bs = materialSample(matType, mp, surf.ns, st.wo, mk3(b0, b1, b2), g);
     st.delta = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
     if (bs.pdf < 1e-8f) return false;
@@ -222,48 +210,47 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, const uint32_t
     return true;
 }
 
-__device__ __forceinline__ int find_request(const BatchArgs& a, int64_t item) {
-    int lo = 0, hi = a.nreq - 1;
+__device__ __forceinline__ int find_request(const BatchLaunch& L, int64_t item) {
+    int lo = 0, hi = L.nreq - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (a.req[mid].itemBase <= item) lo = mid;
+        if (L.req[mid].itemBase <= item) lo = mid;
         else hi = mid - 1;
     }
     return lo;
 }
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) batch_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ BatchLaunch L) {
+    __shared__ uint32_t row[256];
+    for (int i = threadIdx.x; i < 256; i += BLOCK) row[i] = sobol_value(L.mats, L.sampleOffset >> 8, (uint32_t)i);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     // warp-uniform: claimed but not yet handed-out work items [qnext, qend)
     int64_t qnext = 0, qend = 0;
     bool exhausted = false;
-    // lane state
-    bool live = false;  // holds a work item with samples left
-    int rid = 0, pix = 0;
-    int32_t s = 0, s1 = 0;
-    v3 acc = mk3(0.0f);
-    bool wrote = false;
+    bool live = false;
+    int rid = 0, px = 0, py = 0;
     Sampler g;
     PathState st;
     for (;;) {
         const unsigned idle = __ballot_sync(kFull, !live);
         const int nidle = __popc(idle);
         const int64_t tail = qend - qnext;
-        if (nidle != 0 && (nidle >= a.regenThreshold || nidle == 32) && (!exhausted || tail > 0)) {
+        if (nidle != 0 && (nidle >= L.regenThreshold || nidle == 32) && (!exhausted || tail > 0)) {
             // idle lanes take the leftover of the claimed range first, then a
             // freshly claimed range of queueCap items (one atomic per claim)
             int64_t nb = 0, nlen = 0;
             if (!exhausted && tail < nidle) {
                 unsigned long long b = 0;
-                if (lane == 0) b = atomicAdd(a.counter, (unsigned long long)a.queueCap);
+                if (lane == 0) b = atomicAdd(L.counter, (unsigned long long)L.queueCap);
                 b = __shfl_sync(kFull, b, 0);
-                if ((int64_t)b >= a.nitems) {
+                if ((int64_t)b >= L.nitems) {
                     exhausted = true;
                 } else {
                     nb = (int64_t)b;
-                    nlen = min((int64_t)a.queueCap, a.nitems - nb);
+                    nlen = min((int64_t)L.queueCap, L.nitems - nb);
                 }
             }
             if (!live) {
@@ -272,21 +259,16 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchArgs a) {
                 if (r < tail) item = qnext + r;
                 else if (r - tail < nlen) item = nb + (r - tail);
                 if (item >= 0) {
-                    rid = find_request(a, item);
-                    const BatchRequest& rq = a.req[rid];
-                    pix = (int)(item - rq.itemBase);
-                    s = a.chunk0;
-                    s1 = min(a.chunk1, rq.spp);
-                    if (s < s1) {
+                    rid = find_request(L, item);
+                    const BatchRequest& rq = L.req[rid];
+                    const int64_t local = item - rq.itemBase;
+                    const int64_t tile = local >> 5;
+                    const int w = (int)(local & 31);
+                    px = (int)(tile % rq.tilesX) * 8 + (w & 7);
+                    py = (int)(tile / rq.tilesX) * 4 + (w >> 3);
+                    if (px < rq.sc.filmW && py < rq.sc.filmH) {
                         live = true;
-                        acc = mk3(0.0f);
-                        wrote = false;
-                        if (s > 0) {  // continue the sum of the previous chunks
-                            float4 f = rq.frame[pix];
-                            acc = mk3(f.x, f.y, f.z);
-                            wrote = f.w != 0.0f;
-                        }
-                        start_sample(rq, a.sobolRows, pix, s, g, st);
+                        start_sample(rq, L, row, px, py, g, st);
                     }
                 }
             }
@@ -303,20 +285,20 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchArgs a) {
             continue;
         }
         if (live) {
-            const BatchRequest& rq = a.req[rid];
-            if (!path_step(rq, a.sobolRows, s, g, st)) {
-                // the sample is complete; main() drops NaN samples
+            const BatchRequest& rq = L.req[rid];
+            if (!path_step(rq, g, st)) {
+                // main(): lastRes + result, NaN samples dropped; one owner per pixel
                 if (!hasNan(st.result)) {
-                    acc = acc + st.result;
-                    wrote = true;
+                    float4* f = rq.frame + (size_t)py * rq.sc.filmW + px;
+                    v3 last = mk3(0.0f);
+                    if (L.s != 0) {
+                        float4 o = *f;
+                        last = mk3(o.x, o.y, o.z);
+                    }
+                    v3 r = last + st.result;
+                    *f = make_float4(r.x, r.y, r.z, 1.0f);
                 }
-                s++;
-                if (s < s1) {
-                    start_sample(rq, a.sobolRows, pix, s, g, st);
-                } else {
-                    if (wrote) rq.frame[pix] = make_float4(acc.x, acc.y, acc.z, 1.0f);
-                    live = false;
-                }
+                live = false;
             }
         }
     }
@@ -330,7 +312,7 @@ int occupancy_grid(const void* kernel, int block) {
     return sms * std::max(per_sm, 1);
 }
 
-cudaError_t launch_batch(const BatchArgs& a, int block, cudaStream_t st) {
+cudaError_t launch_batch(const BatchLaunch& a, int block, cudaStream_t st) {
     switch (block) {
         case 64:
             batch_kernel<64><<<occupancy_grid((const void*)batch_kernel<64>, 64), 64, 0, st>>>(a);
@@ -354,8 +336,7 @@ struct zgl_batch {
     int64_t nitems = 0;
     int32_t maxSpp = 0;
     std::vector<zgl::BatchRequest> req;
-    zgl::BatchRequest* d_req = nullptr;
-    uint32_t* d_rows = nullptr;
+    uint32_t* d_mats = nullptr;
     unsigned long long* d_counters = nullptr;
     int32_t nchunks_cap = 0;
     zgl_batch_config cfg{};
@@ -374,18 +355,16 @@ void batch_free(zgl_batch* b) {
     if (b->ev_in) cudaEventDestroy(b->ev_in);
     if (b->ev_out) cudaEventDestroy(b->ev_out);
     if (b->stream) cudaStreamDestroy(b->stream);
-    if (b->d_req) cudaFree(b->d_req);
-    if (b->d_rows) cudaFree(b->d_rows);
+    if (b->d_mats) cudaFree(b->d_mats);
     if (b->d_counters) cudaFree(b->d_counters);
     delete b;
 }
 
-zgl_batch_config resolve(const zgl_batch_config& c, int32_t maxSpp) {
+zgl_batch_config resolve(const zgl_batch_config& c) {
     zgl_batch_config r = c;
     if (r.block_size == 0) r.block_size = 128;
     if (r.queue_capacity == 0) r.queue_capacity = 32;
     if (r.regen_threshold == 0) r.regen_threshold = 16;
-    if (r.samples_per_launch == 0 || r.samples_per_launch > maxSpp) r.samples_per_launch = maxSpp;
     return r;
 }
 
@@ -394,37 +373,52 @@ void check_config(const zgl_batch_config& c) {
         fail(ZGL_ERR_INVALID_ARG, "batch: block_size must be 64, 128 or 256");
     if (c.queue_capacity < 0 || c.queue_capacity > 4096) fail(ZGL_ERR_INVALID_ARG, "batch: queue_capacity out of range");
     if (c.regen_threshold < 0 || c.regen_threshold > 32) fail(ZGL_ERR_INVALID_ARG, "batch: regen_threshold out of range");
-    if (c.samples_per_launch < 0) fail(ZGL_ERR_INVALID_ARG, "batch: samples_per_launch out of range");
 }
 
-// Enqueues the whole render (frame clears, one counter reset and one
-// persistent launch per chunk of samples) on `st`; `first_chunk_only` renders
-// only the first chunk (autotuning).
-void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, bool first_chunk_only) {
+// Enqueues the whole render on `st`: frame clears, then for every sample
+// index one persistent launch per group of up to 64 requests that still need
+// that sample (each with its own counter reset).  `first_samples` > 0 renders
+// only that many sample indices (autotuning).
+void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, int first_samples) {
     for (const auto& r : b->req)
         ZGL_CUDA(cudaMemsetAsync(r.frame, 0, sizeof(float4) * (size_t)r.npix, st));
-    int nchunks = (b->maxSpp + c.samples_per_launch - 1) / c.samples_per_launch;
-    if (first_chunk_only) nchunks = std::min(nchunks, 1);
-    if (nchunks > b->nchunks_cap) fail(ZGL_ERR_STATE, "batch: chunk count exceeds the counter array");
-    for (int k = 0; k < nchunks; k++) {
-        BatchArgs a;
-        a.req = b->d_req;
-        a.nreq = b->nreq;
-        a.nitems = b->nitems;
-        a.sobolRows = b->d_rows;
-        a.chunk0 = k * c.samples_per_launch;
-        a.chunk1 = std::min(b->maxSpp, (k + 1) * c.samples_per_launch);
-        a.counter = b->d_counters + k;
-        a.queueCap = c.queue_capacity;
-        a.regenThreshold = c.regen_threshold;
-        ZGL_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st));
-        ZGL_CUDA(launch_batch(a, c.block_size, st));
+    int nsamples = first_samples > 0 ? std::min(first_samples, b->maxSpp) : b->maxSpp;
+    int k = 0;
+    for (int s = 0; s < nsamples; s++) {
+        std::vector<int> active;
+        for (int i = 0; i < b->nreq; i++)
+            if (b->req[(size_t)i].spp > s) active.push_back(i);
+        for (size_t g0 = 0; g0 < active.size(); g0 += kMaxReqPerLaunch) {
+            if (k >= b->nchunks_cap) fail(ZGL_ERR_STATE, "batch: launch count exceeds the counter array");
+            BatchLaunch L;
+            std::memset(&L, 0, sizeof(L));
+            int64_t base = 0;
+            for (size_t j = g0; j < active.size() && (int)(j - g0) < kMaxReqPerLaunch; j++) {
+                BatchRequest q = b->req[(size_t)active[j]];
+                q.itemBase = base;
+                int tilesY = (q.sc.filmH + 3) / 4;
+                base += (int64_t)q.tilesX * tilesY * 32;
+                L.req[L.nreq++] = q;
+            }
+            L.nitems = base;
+            L.s = s;
+            int32_t off = (int32_t)((uint32_t)s * 256u);
+            if (off > 131072 * 256) off -= 131072 * 256;
+            L.sampleOffset = (uint32_t)off;
+            L.counter = b->d_counters + k;
+            L.queueCap = c.queue_capacity;
+            L.regenThreshold = c.regen_threshold;
+            L.mats = b->d_mats;
+            ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
+            ZGL_CUDA(launch_batch(L, c.block_size, st));
+            k++;
+        }
     }
 }
 
 bool same_cfg(const zgl_batch_config& x, const zgl_batch_config& y) {
     return x.block_size == y.block_size && x.queue_capacity == y.queue_capacity &&
-           x.regen_threshold == y.regen_threshold && x.samples_per_launch == y.samples_per_launch;
+           x.regen_threshold == y.regen_threshold;
 }
 
 }  // namespace
@@ -470,33 +464,23 @@ zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const
             q.spp = r.spp;
             q.frame = reinterpret_cast<float4*>(r.frame);
             q.npix = r.scene->filmW * r.scene->filmH;
+            q.tilesX = (r.scene->filmW + 7) / 8;
             q.itemBase = base;
             base += q.npix;
             b->maxSpp = std::max(b->maxSpp, r.spp);
             b->req.push_back(q);
         }
         b->nitems = base;
-        ZGL_CUDA(cudaMalloc(&b->d_req, sizeof(BatchRequest) * (size_t)n));
-        ZGL_CUDA(cudaMemcpy(b->d_req, b->req.data(), sizeof(BatchRequest) * (size_t)n, cudaMemcpyHostToDevice));
-        // Sobol values of rows 0 .. maxSpp-1 (sample index s uses row s)
         std::vector<uint32_t> mats;
         sobol_matrices(mats);
-        std::vector<uint32_t> rows((size_t)b->maxSpp * 256);
-        for (int sidx = 0; sidx < b->maxSpp; sidx++)
-            for (int d = 0; d < 256; d++) {
-                uint32_t r = 0, idx = (uint32_t)sidx;
-                for (int i = 0; idx != 0; idx >>= 1, i++)
-                    if (idx & 1u) r ^= mats[(size_t)d * 32 + i];
-                rows[(size_t)sidx * 256 + d] = r;
-            }
-        ZGL_CUDA(cudaMalloc(&b->d_rows, sizeof(uint32_t) * rows.size()));
-        ZGL_CUDA(cudaMemcpy(b->d_rows, rows.data(), sizeof(uint32_t) * rows.size(), cudaMemcpyHostToDevice));
-        b->nchunks_cap = b->maxSpp;
+        ZGL_CUDA(cudaMalloc(&b->d_mats, sizeof(uint32_t) * mats.size()));
+        ZGL_CUDA(cudaMemcpy(b->d_mats, mats.data(), sizeof(uint32_t) * mats.size(), cudaMemcpyHostToDevice));
+        b->nchunks_cap = b->maxSpp * ((n + kMaxReqPerLaunch - 1) / kMaxReqPerLaunch);
         ZGL_CUDA(cudaMalloc(&b->d_counters, sizeof(unsigned long long) * (size_t)b->nchunks_cap));
         ZGL_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
         ZGL_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming));
         ZGL_CUDA(cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming));
-        b->cfg = resolve(cfg, b->maxSpp);
+        b->cfg = resolve(cfg);
     } catch (...) {
         batch_free(b);
         throw;
@@ -509,7 +493,7 @@ zgl_status zgl_batch_set_config(zgl_batch* b, const zgl_batch_config* config) {
     ZGL_API_BEGIN
     if (!b || !config) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_set_config: NULL");
     check_config(*config);
-    b->cfg = resolve(*config, b->maxSpp);
+    b->cfg = resolve(*config);
     ZGL_API_END
 }
 
@@ -532,7 +516,7 @@ zgl_status zgl_batch_render(zgl_batch* b, void* stream) {
         cudaGraph_t graph = nullptr;
         ZGL_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         try {
-            enqueue_render(b, b->cfg, b->stream, false);
+            enqueue_render(b, b->cfg, b->stream, 0);
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(b->stream, &g);
@@ -568,7 +552,6 @@ zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chos
     const int thresholds[] = {4, 16, 32};
     zgl_batch_config best = b->cfg;
     float bestMs = 1e30f;
-    int chunk = std::min(b->maxSpp, 2);  // time the first two samples of every request
     try {
         for (int bs : blocks)
             for (int cap : caps)
@@ -577,9 +560,8 @@ zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chos
                     c.block_size = bs;
                     c.queue_capacity = cap;
                     c.regen_threshold = th;
-                    c.samples_per_launch = chunk;
                     ZGL_CUDA(cudaEventRecord(e0, st));
-                    enqueue_render(b, c, st, true);
+                    enqueue_render(b, c, st, 2);
                     ZGL_CUDA(cudaEventRecord(e1, st));
                     ZGL_CUDA(cudaEventSynchronize(e1));
                     float ms = 0.0f;
@@ -596,7 +578,6 @@ zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chos
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    best.samples_per_launch = b->cfg.samples_per_launch;
     b->cfg = best;
     if (chosen) *chosen = best;
     ZGL_API_END

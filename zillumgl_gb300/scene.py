@@ -282,8 +282,7 @@ class RenderRequest(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("block_size", C.c_int32), ("queue_capacity", C.c_int32), ("regen_threshold", C.c_int32),
-                ("samples_per_launch", C.c_int32)]
+    _fields_ = [("block_size", C.c_int32), ("queue_capacity", C.c_int32), ("regen_threshold", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -326,3 +326,52 @@ def city_scene(seed: int = 2, width: int = 1920, height: int = 1080, grid: int =
         cam_pos=(-6.0, -6.0, 14.0), cam_angle=(45.0, -28.0, 0.0), cam_fov=50.0, sampler=1,
         env_rgb=sky_environment(env_size[0], env_size[1], seed=seed + 1), env_rotation=0.0,
     ).normalized()
+
+
+def sphere_box_scene(seed: int, n_tris: int, width: int, height: int, sampler: int = 1):
+    """Cornell box plus enough 32x16 UV spheres (960 triangles each) scattered
+    inside it to reach about `n_tris` triangles, materials drawn per sphere
+    (Lambertian or principled)."""
+    from .scene import LAMBERTIAN, PRINCIPLED, mat_tex, material
+
+    d = cornell_scene(seed=seed, width=width, height=height, sampler=sampler)
+    rng = np.random.default_rng(seed + 1000)
+    k = max(0, (n_tris - d.obj_indices.size // 3) // 960)
+    if k == 0:
+        return d
+    centers = np.stack([rng.uniform(-0.9, 0.9, k), rng.uniform(-0.9, 0.9, k), rng.uniform(0.1, 1.9, k)], 1)
+    radii = rng.uniform(0.02, 0.12, k)
+    mats = list(d.materials)
+    v, n, i = _sphere_batch(centers, radii, 32, 16)
+    base = d.obj_vertices.shape[0]
+    per = i.size // 3 // k
+    sphere_mat = []
+    for j in range(k):
+        if rng.uniform() < 0.5:
+            mats.append(material(LAMBERTIAN, base_color=rng.uniform(0.2, 0.8, 3)))
+        else:
+            mats.append(material(PRINCIPLED, base_color=rng.uniform(0.2, 0.8, 3), roughness=rng.uniform(0.1, 0.9),
+                                 metallic=float(rng.integers(0, 2))))
+        sphere_mat += [mat_tex(len(mats) - 1)] * per
+    d.obj_vertices = np.concatenate([d.obj_vertices, v.astype(np.float32)])
+    d.obj_normals = np.concatenate([d.obj_normals, n.astype(np.float32)])
+    d.obj_indices = np.concatenate([d.obj_indices, (i + base).astype(np.uint32)])
+    d.obj_mat_tex = np.concatenate([d.obj_mat_tex, np.array(sphere_mat, np.int32)])
+    d.materials = np.stack(mats)
+    return d.normalized()
+
+
+def batch_requests(seed: int = 3, n: int = 64):
+    """Seeded request list of the batched-serving workload: n scenes with
+    log-uniform triangle counts in [1k, 500k], log-uniform square films in
+    [128, 1024], spp uniform in {4..64} and depth uniform in {4..8}.
+    Returns [(SceneData, spp, params)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n):
+        tris = int(np.exp(rng.uniform(np.log(1e3), np.log(5e5))))
+        side = int(np.exp(rng.uniform(np.log(128), np.log(1024))))
+        spp = int(rng.integers(4, 65))
+        depth = int(rng.integers(4, 9))
+        out.append((sphere_box_scene(seed * 1000 + r, tris, side, side), spp, dict(max_depth=depth)))
+    return out
