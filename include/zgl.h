@@ -192,8 +192,21 @@ zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene
  *   "noise" float[filmW*filmH*2], "pixel_seeds" uint32[filmW*filmH*2],
  *   "camera" float[19] (front, right, up, inverse camera matrix column-major,
  *   tan(fov/2)), "scalars" float[4] (lightSum, envSum as used by the shaders,
- *   objPrimCount, nLightTriangles). */
+ *   objPrimCount, nLightTriangles), "info" int64[10] (film width, film
+ *   height, vertices, object vertices, triangles, object triangles, light
+ *   triangles, materials, environment width, environment height), the
+ *   flattened "vertices" and "normals"
+ *   float[nv*3], "indices" uint32[ntri*3], "mat_tex" int32[objPrimCount] and
+ *   "materials" float[nmat*16]. */
 zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out, size_t bytes);
+
+/* Scene::load (src/core/Scene.cpp:58-127) + createGLContext: read a scene XML
+ * file (integrator size, sampler, camera, model instances with transforms,
+ * materials or light radiance, environment map) and build the scene.  Models
+ * are Wavefront OBJ files and the environment map a PFM image (the reference
+ * uses assimp and stb_image, which this build does not include).  `flags` as
+ * for zgl_scene_create.  Malformed files give ZGL_ERR_PARSE. */
+zgl_status zgl_scene_load_xml(const char* path, int32_t flags, zgl_scene** out);
 
 zgl_status zgl_scene_destroy(zgl_scene* scene);
 

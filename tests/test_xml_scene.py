@@ -1,0 +1,158 @@
+"""Scene XML loading (Scene::load, src/core/Scene.cpp:58-127): host-side
+parsing, model transforms (Model.cpp:62-71), material records
+(MaterialLoader.cpp:5-68), light instances and the environment map."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from zillumgl_gb300 import ZglError
+from zillumgl_gb300.scene import Scene
+
+CUBE = """# unit cube without normals, faces wound counter-clockwise from outside
+# (smooth normals are generated from the winding)
+v -0.5 -0.5 -0.5
+v 0.5 -0.5 -0.5
+v 0.5 0.5 -0.5
+v -0.5 0.5 -0.5
+v -0.5 -0.5 0.5
+v 0.5 -0.5 0.5
+v 0.5 0.5 0.5
+v -0.5 0.5 0.5
+f 1 4 3 2
+f 5 6 7 8
+f 1 2 6 5
+f 2 3 7 6
+f 3 4 8 7
+f 4 1 5 8
+"""
+QUAD = """v -1 -1 0
+v 1 -1 0
+v 1 1 0
+v -1 1 0
+vn 0 0 1
+f 1//1 2//1 3//1 4//1
+"""
+SCENE = """<?xml version="1.0"?>
+<scene name="t">
+  <integrator type="path"><maxBounce value="3"/><size width="40" height="24"/></integrator>
+  <sampler type="sobol"><numSamples value="16"/></sampler>
+  <camera type="thinLens">
+    <position value="0 -6 2"/><angle value="0 -5 0"/><fov value="50"/>
+    <lensRadius value="0"/><focalDistance value="1"/>
+  </camera>
+  <modelInstances>
+    <!-- floor -->
+    <modelInstance path="quad.obj" name="floor" type="object">
+      <transform translate="0 0 0" scale="4 4 1" rotate="0 -90 0"/>
+      <material type="lambertian"><baseColor value="0.6 0.5 0.4"/></material>
+    </modelInstance>
+    <modelInstance path="cube.obj" name="box" type="object">
+      <transform translate="0.3 0.2 0.5" scale="1 1 1" rotate="30 0 0"/>
+      <material type="principled">
+        <baseColor value="0.2 0.7 0.3"/><roughness value="0.4"/><metallic value="1"/><clearcoat value="0.5"/>
+      </material>
+    </modelInstance>
+    <modelInstance path="quad.obj" name="lamp" type="light">
+      <transform translate="0 0 3" scale="0.5 0.5 1" rotate="0 90 0"/>
+      <radiance value="20 18 16"/>
+    </modelInstance>
+  </modelInstances>
+  <envMap path="sky.pfm"/>
+</scene>
+"""
+
+
+def _write(tmp_path, scene=SCENE, env=True):
+    (tmp_path / "cube.obj").write_text(CUBE)
+    (tmp_path / "quad.obj").write_text(QUAD)
+    (tmp_path / "scene.xml").write_text(scene)
+    if env:
+        H, W = 8, 16
+        img = np.linspace(0.1, 2.0, H * W * 3, dtype=np.float32).reshape(H, W, 3)
+        with open(tmp_path / "sky.pfm", "wb") as f:
+            f.write(f"PF\n{W} {H}\n-1.0\n".encode())
+            f.write(img[::-1].astype("<f4").tobytes())  # PFM stores the bottom row first
+        return img
+    return None
+
+
+def _rot(axis, deg):
+    a = np.radians(deg)
+    c, s = np.cos(a), np.sin(a)
+    x, y, z = axis
+    return np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                     [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                     [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
+
+
+def _model(t, sc, r):
+    # translate * scale * rotX(90) * rotZ(r0) * rotX(r1) * rotY(r2)
+    m = np.diag(sc) @ _rot((1, 0, 0), 90) @ _rot((0, 0, 1), r[0]) @ _rot((1, 0, 0), r[1]) @ _rot((0, 1, 0), r[2])
+    return m, np.asarray(t, float)
+
+
+def test_xml_scene_tables(zgl_lib, tmp_path):
+    img = _write(tmp_path)
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    info = sc.info
+    assert sc.film == (40, 24)
+    assert info["obj_triangles"] == 2 + 12 and info["light_triangles"] == 2 and info["materials"] == 2
+    assert (info["env_w"], info["env_h"]) == (16, 8)
+    v = sc.export("vertices").reshape(-1, 3)
+    # floor quad: corners at (+-4, +-4) in the z = 0 plane after the transform
+    m, t = _model((0, 0, 0), (4, 4, 1), (0, -90, 0))
+    quad = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], float)
+    assert np.allclose(v[:4], quad @ m.T + t, atol=1e-5)
+    assert np.allclose(np.abs(v[:4, 2]), 0, atol=1e-5)
+    # box: 8 joined corners, rotated 30 degrees about z after the fixed +90 about x
+    m, t = _model((0.3, 0.2, 0.5), (1, 1, 1), (30, 0, 0))
+    cube = np.array([[-0.5, -0.5, -0.5], [0.5, -0.5, -0.5], [0.5, 0.5, -0.5], [-0.5, 0.5, -0.5],
+                     [-0.5, -0.5, 0.5], [0.5, -0.5, 0.5], [0.5, 0.5, 0.5], [-0.5, 0.5, 0.5]])
+    assert np.allclose(np.sort(v[4:12], axis=0), np.sort(cube @ m.T + t, axis=0), atol=1e-5)
+    n = sc.export("normals").reshape(-1, 3)
+    assert np.allclose(np.linalg.norm(n, axis=1), 1, atol=1e-5)
+    # floor normal is +z after the transform; cube normals point outwards
+    assert np.allclose(n[:4], [0, 0, 1], atol=1e-5)
+    centre = v[4:12].mean(0)
+    assert np.all(np.sum((v[4:12] - centre) * n[4:12], axis=1) > 0)
+    mats = sc.export("materials").reshape(-1, 16)
+    assert np.allclose(mats[0, :3], [0.6, 0.5, 0.4]) and mats[0, 13:14].view(np.int32)[0] == 0
+    assert np.allclose(mats[1, :4], [0.2, 0.7, 0.3, 0.4]) and mats[1, 5] == 1.0 and mats[1, 10] == 0.5
+    assert mats[1, 13:14].view(np.int32)[0] == 1
+    assert mats[1, 6] == 1.0 and mats[1, 12] == np.float32(1.5)  # Material.h defaults kept
+    mt = sc.export("mat_tex")
+    assert np.all((mt & 0xFFFF)[:2] == 0) and np.all((mt & 0xFFFF)[2:] == 1) and np.all((mt >> 16) == -1)
+    # light power split by area over the lamp's two triangles (Scene.cpp:200-243)
+    lp = sc.export("light_power").reshape(-1, 3)
+    assert np.allclose(lp.sum(0), [20, 18, 16], rtol=1e-6)
+    # camera uniforms as Camera::update computes them
+    assert np.array_equal(sc.export("camera"), oracle.camera((0, -5, 0), 50))
+    # environment: rows top first, RGB16F-rounded
+    assert np.array_equal(sc.export("env_texels"), img.astype(np.float16).astype(np.float32).reshape(-1))
+    sc.close()
+
+
+@pytest.mark.parametrize("broken", ["unclosed", "no_scene", "missing_model", "bad_face"])
+def test_xml_errors_are_parse_status(zgl_lib, tmp_path, broken):
+    text = SCENE
+    if broken == "unclosed":
+        text = SCENE.replace("</modelInstances>", "")
+    elif broken == "no_scene":
+        text = "<?xml version='1.0'?><world/>"
+    elif broken == "missing_model":
+        text = SCENE.replace("cube.obj", "nothing.obj")
+    _write(tmp_path, text)
+    if broken == "bad_face":
+        (tmp_path / "cube.obj").write_text("v 0 0 0\nv 1 0 0\nf 1 2 9\n")
+    with pytest.raises(ZglError) as e:
+        Scene.load(tmp_path / "scene.xml", host_only=True)
+    assert e.value.status == 5
+
+
+def test_xml_without_env_is_black(zgl_lib, tmp_path):
+    _write(tmp_path, SCENE.replace('<envMap path="sky.pfm"/>', ""), env=False)
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    assert sc.info["env_w"] == 0 and sc.export("scalars")[1] == 0.0
+    sc.close()

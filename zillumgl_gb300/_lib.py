@@ -60,6 +60,7 @@ SIGNATURES: dict[str, tuple] = {
                                               C.c_void_p, C.c_void_p]),
     "zgl_scene_create": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "zgl_scene_export": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_size_t]),
+    "zgl_scene_load_xml": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "zgl_scene_destroy": (C.c_int32, [C.c_void_p]),
     "zgl_alias_table_build": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     "zgl_integrator_params_default": (C.c_int32, [C.c_void_p]),

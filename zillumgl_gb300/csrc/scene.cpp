@@ -273,6 +273,7 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
         s.indices.push_back((uint32_t)(d.light_indices[i] + nvo));
     }
     s.objPrimCount = (int32_t)d.obj_n_triangles;
+    s.nObjVertices = (int64_t)nvo;
     s.nLight = (int32_t)d.light_n_triangles;
     s.ntri = (int64_t)(d.obj_n_triangles + d.light_n_triangles);
 
@@ -521,7 +522,16 @@ zgl_status zgl_scene_export(const zgl_scene* s, const char* table, void* out, si
         std::memcpy(c + 9, s->camMatInv, 36);
         c[18] = s->tanFOV;
         give(c, sizeof(c));
-    } else if (t == "scalars") {
+    } else if (t == "info") {
+        int64_t c[10] = {s->filmW, s->filmH, (int64_t)s->vertices.size() / 3, s->nObjVertices, s->ntri,
+                         s->objPrimCount, s->nLight, (int64_t)s->materials.size() / 16, s->envW, s->envH};
+        give(c, sizeof(c));
+    } else if (t == "vertices") give(s->vertices.data(), 4 * s->vertices.size());
+    else if (t == "normals") give(s->normals.data(), 4 * s->normals.size());
+    else if (t == "indices") give(s->indices.data(), 4 * s->indices.size());
+    else if (t == "mat_tex") give(s->matTex.data(), 4 * s->matTex.size());
+    else if (t == "materials") give(s->materials.data(), 4 * s->materials.size());
+    else if (t == "scalars") {
         float c[4] = {s->lightSum, s->envSum, (float)s->objPrimCount, (float)s->nLight};
         give(c, sizeof(c));
     } else fail(ZGL_ERR_INVALID_ARG, "zgl_scene_export: unknown table '%s'", table);

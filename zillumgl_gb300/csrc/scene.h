@@ -20,6 +20,7 @@ struct zgl_scene {
     std::vector<int32_t> matTex;  // per object triangle
     int64_t ntri = 0;
     int32_t objPrimCount = 0;
+    int64_t nObjVertices = 0;
     int32_t nLight = 0;
     std::vector<float> materials;  // 16 per material
 

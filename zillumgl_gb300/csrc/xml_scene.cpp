@@ -1,0 +1,554 @@
+// xml_scene.cpp — Scene::load (src/core/Scene.cpp:58-127) for the scene XML
+// format, with the model and material conventions of the reference:
+//   * <integrator><size width height/></integrator>, <sampler type="sobol"/>,
+//     <camera><position/><angle/><fov/><lensRadius/><focalDistance/></camera>
+//     (Scene.cpp:69-111), <modelInstances> (:112-122), <envMap path/> (:123-125);
+//   * a model instance's matrix is translate * scale * rotX(+90 deg) *
+//     rotZ(rx) * rotX(ry) * rotY(rz) (Model.cpp:6, :62-71); normals go through
+//     transpose(inverse(mat3(model))) and are normalised (Scene.cpp:153-162);
+//   * type="light" instances carry <radiance value/> = total power
+//     (Scene.cpp:39-45, :235); other instances take the <material> of
+//     MaterialLoader.cpp:5-68 for all their meshes ("default" keeps
+//     Material's defaults).
+// The reference imports meshes with assimp and images with stb_image, which
+// are not part of this build: meshes are read from Wavefront OBJ files (v, vn,
+// f with fan triangulation, identical (position, normal) corners joined,
+// smooth area-weighted normals when the file has none) and the environment
+// from a PFM float image.
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "scene.h"
+#include "zgl_internal.h"
+
+namespace zgl {
+namespace {
+
+// ------------------------------------------------------------- tiny XML DOM
+struct XmlNode {
+    std::string name;
+    std::map<std::string, std::string> attrs;
+    std::vector<std::unique_ptr<XmlNode>> children;
+    const XmlNode* child(const std::string& n) const {
+        for (auto& c : children)
+            if (c->name == n) return c.get();
+        return nullptr;
+    }
+    std::string attr(const std::string& n) const {
+        auto it = attrs.find(n);
+        return it == attrs.end() ? std::string() : it->second;
+    }
+};
+
+class XmlParser {
+public:
+    explicit XmlParser(const std::string& text) : s_(text) {}
+
+    std::unique_ptr<XmlNode> parse() {
+        auto root = std::make_unique<XmlNode>();
+        root->name = "#document";
+        while (true) {
+            skip_misc();
+            if (pos_ >= s_.size()) break;
+            if (s_[pos_] != '<') fail(ZGL_ERR_PARSE, "XML: text outside the root element at byte %zu", pos_);
+            root->children.push_back(element());
+        }
+        return root;
+    }
+
+private:
+    void skip_ws() {
+        while (pos_ < s_.size() && std::isspace((unsigned char)s_[pos_])) pos_++;
+    }
+    bool starts(const char* p) const { return s_.compare(pos_, std::strlen(p), p) == 0; }
+    void skip_misc() {
+        for (;;) {
+            skip_ws();
+            if (starts("<?")) {
+                size_t e = s_.find("?>", pos_);
+                if (e == std::string::npos) fail(ZGL_ERR_PARSE, "XML: unterminated declaration");
+                pos_ = e + 2;
+            } else if (starts("<!--")) {
+                size_t e = s_.find("-->", pos_);
+                if (e == std::string::npos) fail(ZGL_ERR_PARSE, "XML: unterminated comment");
+                pos_ = e + 3;
+            } else if (starts("<!")) {
+                size_t e = s_.find('>', pos_);
+                if (e == std::string::npos) fail(ZGL_ERR_PARSE, "XML: unterminated markup");
+                pos_ = e + 1;
+            } else {
+                return;
+            }
+        }
+    }
+    std::string name() {
+        size_t b = pos_;
+        while (pos_ < s_.size() && (std::isalnum((unsigned char)s_[pos_]) || s_[pos_] == '_' || s_[pos_] == '-' ||
+                                    s_[pos_] == ':' || s_[pos_] == '.'))
+            pos_++;
+        if (b == pos_) fail(ZGL_ERR_PARSE, "XML: expected a name at byte %zu", pos_);
+        return s_.substr(b, pos_ - b);
+    }
+    static std::string unescape(const std::string& v) {
+        std::string o;
+        for (size_t i = 0; i < v.size(); i++) {
+            if (v[i] == '&') {
+                size_t e = v.find(';', i);
+                if (e != std::string::npos) {
+                    std::string ent = v.substr(i + 1, e - i - 1);
+                    if (ent == "amp") o += '&';
+                    else if (ent == "lt") o += '<';
+                    else if (ent == "gt") o += '>';
+                    else if (ent == "quot") o += '"';
+                    else if (ent == "apos") o += '\'';
+                    else o += v.substr(i, e - i + 1);
+                    i = e;
+                    continue;
+                }
+            }
+            o += v[i];
+        }
+        return o;
+    }
+    std::unique_ptr<XmlNode> element() {
+        pos_++;  // '<'
+        auto n = std::make_unique<XmlNode>();
+        n->name = name();
+        for (;;) {
+            skip_ws();
+            if (pos_ >= s_.size()) fail(ZGL_ERR_PARSE, "XML: unterminated tag <%s>", n->name.c_str());
+            if (starts("/>")) {
+                pos_ += 2;
+                return n;
+            }
+            if (s_[pos_] == '>') {
+                pos_++;
+                break;
+            }
+            std::string a = name();
+            skip_ws();
+            if (pos_ >= s_.size() || s_[pos_] != '=') fail(ZGL_ERR_PARSE, "XML: attribute %s without value", a.c_str());
+            pos_++;
+            skip_ws();
+            if (pos_ >= s_.size() || (s_[pos_] != '"' && s_[pos_] != '\''))
+                fail(ZGL_ERR_PARSE, "XML: unquoted attribute %s", a.c_str());
+            char q = s_[pos_++];
+            size_t e = s_.find(q, pos_);
+            if (e == std::string::npos) fail(ZGL_ERR_PARSE, "XML: unterminated attribute %s", a.c_str());
+            n->attrs[a] = unescape(s_.substr(pos_, e - pos_));
+            pos_ = e + 1;
+        }
+        for (;;) {
+            // text content is ignored (the format keeps values in attributes)
+            while (pos_ < s_.size() && s_[pos_] != '<') pos_++;
+            if (pos_ >= s_.size()) fail(ZGL_ERR_PARSE, "XML: <%s> is not closed", n->name.c_str());
+            if (starts("<!--") || starts("<?") || starts("<!")) {
+                skip_misc();
+                continue;
+            }
+            if (starts("</")) {
+                pos_ += 2;
+                std::string cn = name();
+                if (cn != n->name) fail(ZGL_ERR_PARSE, "XML: </%s> closes <%s>", cn.c_str(), n->name.c_str());
+                skip_ws();
+                if (pos_ >= s_.size() || s_[pos_] != '>') fail(ZGL_ERR_PARSE, "XML: malformed closing tag");
+                pos_++;
+                return n;
+            }
+            n->children.push_back(element());
+        }
+    }
+
+    const std::string& s_;
+    size_t pos_ = 0;
+};
+
+// ------------------------------------------------------------- small math
+struct M4 {
+    float m[4][4];  // m[col][row], like glm
+};
+M4 identity() {
+    M4 r{};
+    for (int i = 0; i < 4; i++) r.m[i][i] = 1.0f;
+    return r;
+}
+M4 mul(const M4& a, const M4& b) {
+    M4 r{};
+    for (int c = 0; c < 4; c++)
+        for (int rr = 0; rr < 4; rr++) {
+            float s = 0.0f;
+            for (int k = 0; k < 4; k++) s += a.m[k][rr] * b.m[c][k];
+            r.m[c][rr] = s;
+        }
+    return r;
+}
+// rotation by `angle` radians about the unit axis (Rodrigues), as glm::rotate
+M4 rotation(float angle, float ax, float ay, float az) {
+    float len = std::sqrt(ax * ax + ay * ay + az * az);
+    ax /= len;
+    ay /= len;
+    az /= len;
+    float c = std::cos(angle), s = std::sin(angle), t = 1.0f - c;
+    M4 r = identity();
+    r.m[0][0] = c + t * ax * ax;
+    r.m[0][1] = t * ax * ay + s * az;
+    r.m[0][2] = t * ax * az - s * ay;
+    r.m[1][0] = t * ay * ax - s * az;
+    r.m[1][1] = c + t * ay * ay;
+    r.m[1][2] = t * ay * az + s * ax;
+    r.m[2][0] = t * az * ax + s * ay;
+    r.m[2][1] = t * az * ay - s * ax;
+    r.m[2][2] = c + t * az * az;
+    return r;
+}
+const float kRad = 0.01745329251994329576923690768489f;
+
+M4 model_matrix(const float pos[3], const float scale[3], const float rot[3]) {  // Model.cpp:62-71
+    M4 t = identity();
+    t.m[3][0] = pos[0];
+    t.m[3][1] = pos[1];
+    t.m[3][2] = pos[2];
+    M4 s = identity();
+    s.m[0][0] = scale[0];
+    s.m[1][1] = scale[1];
+    s.m[2][2] = scale[2];
+    M4 m = mul(t, s);
+    m = mul(m, rotation(90.0f * kRad, 1, 0, 0));  // ConstRot (Model.cpp:6)
+    m = mul(m, rotation(rot[0] * kRad, 0, 0, 1));
+    m = mul(m, rotation(rot[1] * kRad, 1, 0, 0));
+    m = mul(m, rotation(rot[2] * kRad, 0, 1, 0));
+    return m;
+}
+
+void parse_floats(const std::string& s, float* out, int n, const float* dflt) {
+    std::istringstream is(s);
+    for (int i = 0; i < n; i++) {
+        float v;
+        if (is >> v) out[i] = v;
+        else out[i] = dflt[i];
+    }
+}
+
+// ------------------------------------------------------------- OBJ meshes
+struct Mesh {
+    std::vector<float> v, n;  // 3 per vertex
+    std::vector<uint32_t> idx;
+};
+
+Mesh load_obj(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) fail(ZGL_ERR_PARSE, "cannot open model '%s'", path.c_str());
+    std::vector<float> P, N;
+    std::map<std::pair<long, long>, uint32_t> corner;
+    Mesh m;
+    std::vector<std::pair<long, long>> keys;
+    std::string line;
+    size_t lineno = 0;
+    while (std::getline(f, line)) {
+        lineno++;
+        std::istringstream is(line);
+        std::string tag;
+        if (!(is >> tag) || tag[0] == '#') continue;
+        if (tag == "v") {
+            float x, y, z;
+            if (!(is >> x >> y >> z)) fail(ZGL_ERR_PARSE, "%s:%zu: bad vertex", path.c_str(), lineno);
+            P.insert(P.end(), {x, y, z});
+        } else if (tag == "vn") {
+            float x, y, z;
+            if (!(is >> x >> y >> z)) fail(ZGL_ERR_PARSE, "%s:%zu: bad normal", path.c_str(), lineno);
+            N.insert(N.end(), {x, y, z});
+        } else if (tag == "f") {
+            std::vector<uint32_t> poly;
+            std::string tok;
+            while (is >> tok) {
+                long vi = 0, ni = 0;
+                size_t s1 = tok.find('/');
+                vi = std::stol(tok.substr(0, s1));
+                if (s1 != std::string::npos) {
+                    size_t s2 = tok.find('/', s1 + 1);
+                    if (s2 != std::string::npos && s2 + 1 < tok.size()) ni = std::stol(tok.substr(s2 + 1));
+                }
+                long nv = (long)P.size() / 3, nn = (long)N.size() / 3;
+                if (vi < 0) vi += nv + 1;
+                if (ni < 0) ni += nn + 1;
+                if (vi < 1 || vi > nv || ni < 0 || ni > nn)
+                    fail(ZGL_ERR_PARSE, "%s:%zu: face index out of range", path.c_str(), lineno);
+                auto key = std::make_pair(vi, ni);
+                auto it = corner.find(key);
+                uint32_t id;
+                if (it == corner.end()) {
+                    id = (uint32_t)keys.size();
+                    corner[key] = id;
+                    keys.push_back(key);
+                } else {
+                    id = it->second;
+                }
+                poly.push_back(id);
+            }
+            if (poly.size() < 3) fail(ZGL_ERR_PARSE, "%s:%zu: face with fewer than 3 corners", path.c_str(), lineno);
+            for (size_t k = 1; k + 1 < poly.size(); k++) m.idx.insert(m.idx.end(), {poly[0], poly[k], poly[k + 1]});
+        }
+    }
+    bool haveN = true;
+    for (auto& k : keys) {
+        m.v.insert(m.v.end(), {P[3 * (k.first - 1)], P[3 * (k.first - 1) + 1], P[3 * (k.first - 1) + 2]});
+        if (k.second == 0) haveN = false;
+    }
+    m.n.assign(m.v.size(), 0.0f);
+    if (haveN) {
+        for (size_t i = 0; i < keys.size(); i++)
+            for (int c = 0; c < 3; c++) m.n[3 * i + c] = N[3 * (keys[i].second - 1) + c];
+    } else {
+        // smooth normals: area-weighted face normals summed per position
+        std::map<long, std::vector<float>> acc;
+        for (size_t t = 0; t < m.idx.size() / 3; t++) {
+            const float* a = &m.v[3 * m.idx[3 * t]];
+            const float* b = &m.v[3 * m.idx[3 * t + 1]];
+            const float* c = &m.v[3 * m.idx[3 * t + 2]];
+            float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            float fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            for (int j = 0; j < 3; j++) {
+                auto& s = acc[keys[m.idx[3 * t + j]].first];
+                if (s.empty()) s.assign(3, 0.0f);
+                for (int c2 = 0; c2 < 3; c2++) s[c2] += fn[c2];
+            }
+        }
+        for (size_t i = 0; i < keys.size(); i++) {
+            auto& s = acc[keys[i].first];
+            float l = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+            for (int c = 0; c < 3; c++) m.n[3 * i + c] = l > 0.0f ? s[c] / l : (c == 2 ? 1.0f : 0.0f);
+        }
+    }
+    if (m.idx.empty()) fail(ZGL_ERR_PARSE, "model '%s' has no faces", path.c_str());
+    return m;
+}
+
+// PFM float image (bottom row first in the file); returned top row first.
+std::vector<float> load_pfm(const std::string& path, int& W, int& H) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail(ZGL_ERR_PARSE, "cannot open environment map '%s'", path.c_str());
+    std::string magic;
+    double scale;
+    f >> magic >> W >> H >> scale;
+    f.get();
+    if ((magic != "PF" && magic != "Pf") || W <= 0 || H <= 0 || (int64_t)W * H > (1ll << 28))
+        fail(ZGL_ERR_PARSE, "'%s' is not a PFM image", path.c_str());
+    int ch = magic == "PF" ? 3 : 1;
+    std::vector<float> raw((size_t)W * H * ch);
+    f.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * 4));
+    if (!f) fail(ZGL_ERR_PARSE, "'%s' is truncated", path.c_str());
+    if (scale > 0) {  // big-endian
+        for (auto& v : raw) {
+            uint32_t u;
+            std::memcpy(&u, &v, 4);
+            u = (u >> 24) | ((u >> 8) & 0xff00u) | ((u << 8) & 0xff0000u) | (u << 24);
+            std::memcpy(&v, &u, 4);
+        }
+    }
+    std::vector<float> rgb((size_t)W * H * 3);
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++)
+            for (int c = 0; c < 3; c++)
+                rgb[3 * ((size_t)(H - 1 - y) * W + x) + c] = raw[ch * ((size_t)y * W + x) + (ch == 3 ? c : 0)];
+    return rgb;
+}
+
+std::string resolve_path(const std::string& base, const std::string& p) {
+    if (p.empty() || p[0] == '/') return p;
+    std::ifstream probe(p);
+    if (probe) return p;  // relative to the working directory, like the reference
+    size_t slash = base.find_last_of('/');
+    return slash == std::string::npos ? p : base.substr(0, slash + 1) + p;
+}
+
+void material_from_xml(const XmlNode* node, float* out16, bool& useDefault) {
+    // Material defaults (Material.h:32-53)
+    float d[16] = {1, 1, 1, 1, 0, 0, 1, 1, 0, 1, 0, 0, 1.5f, 0, 0, 0};
+    std::memcpy(out16, d, sizeof(d));
+    int32_t type = 0;
+    useDefault = false;
+    std::string t = node ? node->attr("type") : std::string();
+    auto val = [&](const char* n, float* dst, int cnt) {
+        const XmlNode* c = node->child(n);
+        if (!c) return;
+        std::istringstream is(c->attr("value"));
+        for (int i = 0; i < cnt; i++) {
+            float v;
+            if (is >> v) dst[i] = v;
+        }
+    };
+    if (!node || t == "default") {
+        useDefault = true;
+    } else if (t == "principled") {
+        val("baseColor", out16, 3);
+        val("subsurface", out16 + 4, 1);
+        val("metallic", out16 + 5, 1);
+        val("roughness", out16 + 3, 1);
+        val("specular", out16 + 6, 1);
+        val("specularTint", out16 + 7, 1);
+        val("sheen", out16 + 8, 1);
+        val("sheenTint", out16 + 9, 1);
+        val("clearcoat", out16 + 10, 1);
+        val("clearcoatGloss", out16 + 11, 1);
+        type = 1;
+    } else if (t == "metalWorkflow") {
+        val("baseColor", out16, 3);
+        val("metallic", out16 + 5, 1);
+        val("roughness", out16 + 3, 1);
+        type = 2;
+    } else if (t == "dielectric") {
+        val("baseColor", out16, 3);
+        val("ior", out16 + 12, 1);
+        val("roughness", out16 + 3, 1);
+        type = 3;
+    } else if (t == "thinDielectric") {
+        val("baseColor", out16, 3);
+        val("ior", out16 + 12, 1);
+        type = 4;
+    } else if (t == "lambertian") {
+        val("baseColor", out16, 3);
+        type = 0;
+    }
+    std::memcpy(out16 + 13, &type, 4);
+}
+
+}  // namespace
+
+// Parses the scene XML into world-space arrays and builds the scene.
+zgl_scene* load_scene_xml(const std::string& path, int32_t flags) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail(ZGL_ERR_PARSE, "cannot open scene '%s'", path.c_str());
+    std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    XmlParser parser(text);
+    auto doc = parser.parse();
+    const XmlNode* scene = doc->child("scene");
+    if (!scene) fail(ZGL_ERR_PARSE, "'%s' has no <scene> element", path.c_str());
+
+    zgl_scene_desc d{};
+    const float zero3[3] = {0, 0, 0}, one3[3] = {1, 1, 1};
+    if (const XmlNode* integ = scene->child("integrator"))
+        if (const XmlNode* size = integ->child("size")) {
+            d.film_width = std::atoi(size->attr("width").c_str());
+            d.film_height = std::atoi(size->attr("height").c_str());
+        }
+    const XmlNode* sampler = scene->child("sampler");
+    d.sampler = (sampler && sampler->attr("type") == "sobol") ? 1 : 0;
+    if (const XmlNode* cam = scene->child("camera")) {
+        auto get = [&](const char* n) { const XmlNode* c = cam->child(n); return c ? c->attr("value") : std::string(); };
+        parse_floats(get("position"), d.cam_pos, 3, zero3);
+        parse_floats(get("angle"), d.cam_angle, 3, zero3);
+        d.cam_fov = (float)std::atof(get("fov").c_str());
+        d.cam_lens_radius = (float)std::atof(get("lensRadius").c_str());
+        d.cam_focal_dist = (float)std::atof(get("focalDistance").c_str());
+    }
+    std::vector<float> ov, on, lv, ln, lp, mats;
+    std::vector<uint32_t> oi, li, lf{0};
+    std::vector<int32_t> omt;
+    if (const XmlNode* insts = scene->child("modelInstances")) {
+        for (auto& inst : insts->children) {
+            Mesh mesh = load_obj(resolve_path(path, inst->attr("path")));
+            float pos[3], scale[3], rot[3];
+            const XmlNode* tr = inst->child("transform");
+            parse_floats(tr ? tr->attr("translate") : "", pos, 3, zero3);
+            parse_floats(tr ? tr->attr("scale") : "", scale, 3, one3);
+            parse_floats(tr ? tr->attr("rotate") : "", rot, 3, zero3);
+            M4 M = model_matrix(pos, scale, rot);
+            // normal matrix = transpose(inverse(mat3(M)))
+            float a[3][3];
+            for (int c = 0; c < 3; c++)
+                for (int r = 0; r < 3; r++) a[c][r] = M.m[c][r];
+            float det = a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[1][0] * (a[0][1] * a[2][2] - a[2][1] * a[0][2]) +
+                        a[2][0] * (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+            if (det == 0.0f) fail(ZGL_ERR_INVALID_ARG, "model instance with a singular transform");
+            float cof[3][3];  // cofactor matrix = transpose(inverse) * det
+            cof[0][0] = a[1][1] * a[2][2] - a[2][1] * a[1][2];
+            cof[0][1] = a[2][0] * a[1][2] - a[1][0] * a[2][2];
+            cof[0][2] = a[1][0] * a[2][1] - a[2][0] * a[1][1];
+            cof[1][0] = a[2][1] * a[0][2] - a[0][1] * a[2][2];
+            cof[1][1] = a[0][0] * a[2][2] - a[2][0] * a[0][2];
+            cof[1][2] = a[2][0] * a[0][1] - a[0][0] * a[2][1];
+            cof[2][0] = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+            cof[2][1] = a[1][0] * a[0][2] - a[0][0] * a[1][2];
+            cof[2][2] = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+            bool light = inst->attr("type") == "light";
+            std::vector<float>& V = light ? lv : ov;
+            std::vector<float>& Nn = light ? ln : on;
+            uint32_t base = (uint32_t)(V.size() / 3);
+            for (size_t i = 0; i < mesh.v.size() / 3; i++) {
+                const float* p = &mesh.v[3 * i];
+                for (int r = 0; r < 3; r++) V.push_back(M.m[0][r] * p[0] + M.m[1][r] * p[1] + M.m[2][r] * p[2] + M.m[3][r]);
+                const float* q = &mesh.n[3 * i];
+                float nn[3];
+                for (int r = 0; r < 3; r++) nn[r] = (cof[0][r] * q[0] + cof[1][r] * q[1] + cof[2][r] * q[2]) / det;
+                float l = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+                for (int r = 0; r < 3; r++) Nn.push_back(l > 0.0f ? nn[r] / l : 0.0f);
+            }
+            if (light) {
+                for (uint32_t k : mesh.idx) li.push_back(base + k);
+                lf.push_back((uint32_t)(li.size() / 3));
+                float rad[3];
+                const XmlNode* r = inst->child("radiance");
+                parse_floats(r ? r->attr("value") : "", rad, 3, zero3);
+                lp.insert(lp.end(), rad, rad + 3);
+            } else {
+                float m16[16];
+                bool dflt;
+                material_from_xml(inst->child("material"), m16, dflt);
+                mats.insert(mats.end(), m16, m16 + 16);
+                int32_t mi = (int32_t)(mats.size() / 16 - 1);
+                for (uint32_t k : mesh.idx) oi.push_back(base + k);
+                for (size_t t = 0; t < mesh.idx.size() / 3; t++) omt.push_back((int32_t)(0xffff0000u | (uint32_t)mi));
+            }
+        }
+    }
+    std::vector<float> env;
+    if (const XmlNode* e = scene->child("envMap")) {
+        std::string p = e->attr("path");
+        if (!p.empty()) {
+            int W, H;
+            env = load_pfm(resolve_path(path, p), W, H);
+            d.env_width = W;
+            d.env_height = H;
+        }
+    }
+    d.obj_vertices = ov.data();
+    d.obj_n_vertices = ov.size() / 3;
+    d.obj_normals = on.data();
+    d.obj_indices = oi.data();
+    d.obj_n_triangles = oi.size() / 3;
+    d.obj_mat_tex = omt.data();
+    d.materials = mats.data();
+    d.n_materials = mats.size() / 16;
+    d.light_vertices = lv.data();
+    d.light_n_vertices = lv.size() / 3;
+    d.light_normals = ln.data();
+    d.light_indices = li.data();
+    d.light_n_triangles = li.size() / 3;
+    d.light_first = lf.data();
+    d.light_power = lp.data();
+    d.n_light_instances = lp.size() / 3;
+    d.env_rgb = env.empty() ? nullptr : env.data();
+    zgl_scene* out = nullptr;
+    zgl_status st = zgl_scene_create(&d, flags, &out);
+    if (st != ZGL_OK) throw Error{st};
+    return out;
+}
+
+}  // namespace zgl
+
+extern "C" zgl_status zgl_scene_load_xml(const char* path, int32_t flags, zgl_scene** out) {
+    ZGL_API_BEGIN
+    if (!path || !out) zgl::fail(ZGL_ERR_INVALID_ARG, "zgl_scene_load_xml: NULL argument");
+    *out = nullptr;
+    *out = zgl::load_scene_xml(path, flags);
+    ZGL_API_END
+}

@@ -160,6 +160,8 @@ class Scene:
     """Device-resident scene (owner of a ``zgl_scene`` handle)."""
 
     TABLES = {
+        "info": np.int64, "vertices": np.float32, "normals": np.float32, "indices": np.uint32,
+        "mat_tex": np.int32, "materials": np.float32,
         "light_power": np.float32, "light_alias": np.int32, "light_prob": np.float32, "env_alias": np.int32,
         "env_prob": np.float32, "env_texels": np.float32, "sobol": np.uint32, "noise": np.float32,
         "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32,
@@ -171,18 +173,36 @@ class Scene:
         h = C.c_void_p()
         call("zgl_scene_create", C.byref(desc), 1 if host_only else 0, C.byref(h))
         self._h = h
-        self.film = tuple(data.film)
+        self._info()
+
+    @classmethod
+    def load(cls, path, host_only: bool = False) -> "Scene":
+        """Scene::load of a scene XML file (OBJ models, PFM environment)."""
+        self = cls.__new__(cls)
+        self.data = None
+        h = C.c_void_p()
+        call("zgl_scene_load_xml", str(path).encode(), 1 if host_only else 0, C.byref(h))
+        self._h = h
+        self._info()
+        return self
+
+    def _info(self):
+        info = np.empty(10, np.int64)
+        call("zgl_scene_export", self._h, b"info", info.ctypes.data, info.nbytes)
+        self.info = {k: int(v) for k, v in zip(
+            ["film_w", "film_h", "vertices", "obj_vertices", "triangles", "obj_triangles", "light_triangles",
+             "materials", "env_w", "env_h"], info)}
+        self.film = (self.info["film_w"], self.info["film_h"])
 
     def table_size(self, name: str) -> int:
-        d = self.data
-        nl = d.light_indices.size // 3
-        W, H = self.film
-        ew, eh = (d.env_rgb.shape[1], d.env_rgb.shape[0]) if d.env_rgb is not None else (0, 0)
+        i = self.info
+        nl, (W, H), ew, eh = i["light_triangles"], self.film, i["env_w"], i["env_h"]
         return {
+            "info": 10, "vertices": 3 * i["vertices"], "normals": 3 * i["vertices"], "indices": 3 * i["triangles"],
+            "mat_tex": i["obj_triangles"], "materials": 16 * i["materials"],
             "light_power": nl * 3, "light_alias": nl, "light_prob": nl,
-            "env_alias": (ew + 1) * eh if ew else 0, "env_prob": (ew + 1) * eh if ew else 0,
-            "env_texels": ew * eh * 3, "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2,
-            "camera": 19, "scalars": 4,
+            "env_alias": (ew + 1) * eh, "env_prob": (ew + 1) * eh, "env_texels": ew * eh * 3,
+            "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2, "camera": 19, "scalars": 4,
         }[name]
 
     def export(self, name: str) -> np.ndarray:
