@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent"])
     ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
-    ap.add_argument("--render", default="cornell,city,batch", help="render workloads to time ('' for none)")
+    ap.add_argument("--render", default="cornell,city,batch,diff", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
     ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
     return ap.parse_args()
@@ -377,6 +377,9 @@ def run_render(args, stream, dev):
         if name == "batch":
             out[name] = run_batch(args, stream, dev)
             continue
+        if name == "diff":
+            out[name] = run_diff(args, stream, dev)
+            continue
         if name == "cornell":
             data = cornell_scene(seed=1, width=256, height=256)
             runs = [("path", PathIntegrator, dict(max_depth=5))]
@@ -497,6 +500,113 @@ def run_batch(args, stream, dev):
             "batched": {"ms": round(batch_ms, 2), "samples_per_s": round(total / (batch_ms * 1e-3), 1),
                         "config": tuned, "autotune_s": round(tune_s, 2)},
             "speedup": round(plain_ms / batch_ms, 3), "frames_bit_identical_checked": f"{same}/4"}
+
+
+def run_diff(args, stream, dev):
+    """Differentiable rendering: the 8-material principled box at 512^2,
+    32 spp, depth 6.  The target is rendered at the seed parameters; the
+    optimised parameters start perturbed by U(-0.3, 0.3).  One iteration =
+    parameter upload, forward (per-sample radiance + mean image), L2 loss
+    adjoint, path-replay backward, Adam step; timed with CUDA events over
+    `--render-passes` iterations after two warm-up iterations."""
+    import torch
+
+    from zillumgl_gb300.scene import DiffRenderer, Scene
+    from zillumgl_gb300.synthetic import diff_scene, perturbed_params
+
+    data = diff_scene(seed=11, width=512, height=512)
+    W, H = data.film
+    spp, params = 32, dict(max_depth=6)
+    scene = Scene(data)
+    dr = DiffRenderer(scene, spp, **params)
+    p_true = dr.params()
+    target = dr.forward(stream=stream).clone()
+    p = torch.tensor(perturbed_params(p_true, 8, seed=12), device=dev, requires_grad=True)
+    opt = torch.optim.Adam([p], lr=0.01)
+    img = torch.empty((H, W, 3), dtype=torch.float32, device=dev)
+    losses = []
+
+    def iteration(ev=None):
+        dr.set_params(p.detach())
+        if ev:
+            ev[0].record(stream)
+        dr.forward(out=img, stream=stream)
+        with torch.cuda.stream(stream):
+            diff = img - target
+            loss = (diff * diff).mean()
+            dimg = diff * (2.0 / diff.numel())
+        g = dr.backward(dimg, stream=stream)
+        if ev:
+            ev[1].record(stream)
+        with torch.cuda.stream(stream):
+            p.grad = g
+            opt.step()
+            with torch.no_grad():
+                p.clamp_(0.01, 100.0)
+        losses.append(loss)
+
+    for _ in range(2):
+        iteration()
+    stream.synchronize()
+    n = max(args.render_passes, 3)
+    fb = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(n):
+        iteration(fb[k])
+    e1.record(stream)
+    stream.synchronize()
+    it_ms = e0.elapsed_time(e1) / n
+    fb_ms = sorted(a.elapsed_time(b) for a, b in fb)[n // 2]
+    # kernel split of one forward + backward
+    ef = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        dimg = torch.full_like(img, 1e-3)
+    ef[0].record(stream)
+    dr.forward(out=img, stream=stream)
+    ef[1].record(stream)
+    dr.backward(dimg, stream=stream)
+    ef[2].record(stream)
+    stream.synchronize()
+    loss_first, loss_last = float(losses[0]), float(losses[-1])
+    dr.close()
+    scene.close()
+    res = {"film": [W, H], "spp": spp, "params": params, "n_params": int(p.numel()),
+           "fwd_bwd_ms": round(fb_ms, 2), "iteration_ms": round(it_ms, 2),
+           "forward_ms": round(ef[0].elapsed_time(ef[1]), 2), "backward_ms": round(ef[1].elapsed_time(ef[2]), 2),
+           "samples_per_s_fwd_bwd": round(W * H * spp / (fb_ms * 1e-3), 1),
+           "loss_first": loss_first, "loss_last": loss_last, "iterations": len(losses)}
+    res["grad_check"] = diff_grad_check()
+    return res
+
+
+def diff_grad_check():
+    """Gradient error of the adjoint against the FP64 oracle adjoint on a
+    reduced case of the same scene (48x48, 2 spp, depth 6): max abs error
+    over parameters divided by the largest oracle gradient."""
+    import torch
+
+    import oracle
+    from zillumgl_gb300.scene import DiffRenderer, Scene
+    from zillumgl_gb300.synthetic import diff_scene
+
+    data = diff_scene(seed=11, width=48, height=48)
+    params = dict(max_depth=6)
+    scene = Scene(data)
+    dr = DiffRenderer(scene, 2, **params)
+    rng = np.random.default_rng(5)
+    dimage = rng.uniform(-1.0, 1.0, (48, 48, 3)).astype(np.float32)
+    dr.forward()
+    g = dr.backward(torch.from_numpy(dimage).cuda()).cpu().numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    ref = oracle.OracleScene(data, scene.export("sobol"), params).diff_grad(data, 2, dimage)
+    dt = time.perf_counter() - t0
+    dr.close()
+    scene.close()
+    scale = float(np.abs(ref).max())
+    return {"case": "48x48, 2 spp, depth 6, random image adjoint", "max_abs_err_over_max_grad":
+            float(np.abs(g - ref).max() / scale), "oracle_s": round(dt, 2)}
 
 
 def render_cpu_baseline(data, scene, params):

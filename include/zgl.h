@@ -331,6 +331,41 @@ zgl_status zgl_batch_set_config(zgl_batch* batch, const zgl_batch_config* config
 zgl_status zgl_batch_get_config(const zgl_batch* batch, zgl_batch_config* out);
 zgl_status zgl_batch_destroy(zgl_batch* batch);
 
+/* ------------------------------------------------------------------------ */
+/* Differentiable path tracing (path replay adjoint)                         */
+/* ------------------------------------------------------------------------ */
+
+/* A differentiable renderer over `scene` with the path tracer's `params`
+ * (NULL = defaults) and `spp` samples per pixel.  Its image is the mean of
+ * the path tracer's first `spp` samples: after zgl_diff_forward it equals
+ * zgl_integrator_frame / spp of a fresh ZGL_INTEGRATOR_PATH integrator with
+ * the same params after `spp` passes (up to float summation order of the
+ * RGB channels).  Parameters, in order: per material baseColor r, g, b,
+ * roughness (before the 0.0134..1 remap), metallic, specular (Lambertian
+ * materials use only baseColor); then per light instance power r, g, b.
+ * zgl_diff_backward returns d(sum(d_image * image)) / d(params) by path
+ * replay with detached sampling, pdfs, MIS weights and Russian roulette;
+ * visibility changes are not differentiated.  No counterpart in the
+ * reference. */
+typedef struct zgl_diff zgl_diff;
+
+zgl_status zgl_diff_create(zgl_scene* scene, const zgl_integrator_params* params, int32_t spp, zgl_diff** out);
+zgl_status zgl_diff_param_count(const zgl_diff* diff, int32_t* n);
+/* Current parameter values into `out` (host, param_count floats). */
+zgl_status zgl_diff_get_params(const zgl_diff* diff, float* out);
+/* Writes parameters (host or device array) into the scene: its material
+ * records and light tables change for every user of the scene.  Waits for
+ * all work queued on the device first (it may read the scene or produce
+ * `params`). */
+zgl_status zgl_diff_set_params(zgl_diff* diff, const float* params);
+/* Renders the image: `image` is a DEVICE buffer of filmW*filmH RGB floats. */
+zgl_status zgl_diff_forward(zgl_diff* diff, float* image, void* stream);
+/* d_image: DEVICE filmW*filmH RGB adjoint of the image; d_params: DEVICE
+ * param_count floats, overwritten with the gradient.  Uses the per-sample
+ * radiance kept by the last zgl_diff_forward. */
+zgl_status zgl_diff_backward(zgl_diff* diff, const float* d_image, float* d_params, void* stream);
+zgl_status zgl_diff_destroy(zgl_diff* diff);
+
 #ifdef __cplusplus
 }
 #endif

@@ -146,6 +146,9 @@ def _render_lib():
         L.orc_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.orc_transc.restype = None
         L.orc_transc.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L.orc_diff_grad.restype = None
+        L.orc_diff_grad.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                    C.c_int32, C.c_void_p, C.c_int32]
         L._render_ready = True
     return L
 
@@ -291,3 +294,21 @@ class OracleScene:
         film = np.zeros((H, W, 3), np.float32)
         _render_lib().orc_render_triple(C.byref(self.s), spp0, passes, fc0, blocks, loops, _p(film))
         return film
+
+    def diff_grad(self, data, spp, dimage, nthreads=None):
+        """Gradient oracle of the differentiable renderer: d sum(dimage * mean
+        image of samples 0..spp-1) / d (material, light power) parameters, FP64."""
+        nmat = data.materials.size // 16
+        first = np.asarray(data.light_first, np.int64)
+        ninst = max(first.size - 1, 0)
+        inst = np.zeros(max(data.light_indices.size // 3, 1), np.int32)
+        for k in range(ninst):
+            inst[first[k]:first[k + 1]] = k
+        power = np.ascontiguousarray(data.light_power, np.float32).reshape(-1)
+        if power.size == 0:
+            power = np.zeros(1, np.float32)
+        dimg = np.ascontiguousarray(dimage, np.float32)
+        grad = np.zeros(nmat * 6 + ninst * 3, np.float64)
+        _render_lib().orc_diff_grad(C.byref(self.s), spp, _p(dimg), _p(inst), _p(power), nmat, ninst, _p(grad),
+                                    nthreads or threads())
+        return grad

@@ -1154,6 +1154,246 @@ vec3 renderPixel(const OrcScene& sc, int px, int py, int spp, int freeCounter, b
     return r;
 }
 
+// ------------------------------------------------- adjoint of the path tracer
+// The gradient oracle of the differentiable renderer.  Every contribution C
+// of a path (light sample, emitter hit, environment) is a product of the
+// sampled BSDF values along the path, the BSDF value of its own light
+// sample, and emitted radiance (linear in its light instance's power), with
+// pdfs, MIS weights and Russian roulette held fixed.  Its derivative is
+// therefore C * (sum of dlog f over those BSDF values) plus C / P for the
+// power P of its emitter, accumulated here in double precision per
+// contribution.  BSDF log-derivatives are central differences of a double
+// precision evaluation of the same BRDF formulas (material.glsl:357-490).
+
+struct D3 {
+    double x, y, z;
+};
+inline D3 d3(vec3 a) { return D3{a.x, a.y, a.z}; }
+inline D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator*(D3 a, D3 b) { return D3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline D3 operator*(D3 a, double t) { return D3{a.x * t, a.y * t, a.z * t}; }
+inline D3 operator/(D3 a, double t) { return D3{a.x / t, a.y / t, a.z / t}; }
+inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 dnormalize(D3 a) { return a / std::sqrt(ddot(a, a)); }
+inline D3 dmix(D3 a, D3 b, double t) { return a * (1.0 - t) + b * t; }
+inline double dpow5(double x) { return x * x * x * x * x; }
+inline double dschlickG(double c, double alpha) { return c / (c * (1.0 - alpha * 0.5) + alpha * 0.5); }
+
+const double kPiD = 3.14159265358979323846;
+
+// principledBRDF with the differentiable values q = (baseColor rgb, raw
+// roughness, metallic, specular) and the rest of the record from m.
+D3 principledD(const float* m, const double* q, D3 wo, D3 wi, D3 n) {
+    const D3 base{q[0], q[1], q[2]}, one{1.0, 1.0, 1.0};
+    const double rough = 0.0134 * (1.0 - q[3]) + q[3];
+    const double subsurface = m[4], metallic = q[4], specular = q[5], specTint = m[7];
+    const double sheen = m[8], sheenTint = m[9], clearcoat = m[10], ccGloss = m[11];
+    const double alpha = rough * rough, a2 = alpha * alpha;
+    const double ccAlpha = 0.1 * (1.0 - ccGloss) + 0.001 * ccGloss;
+    const double lum = base.x * 0.299 + base.y * 0.587 + base.z * 0.114;
+    const D3 tint = lum > 0.0 ? base / lum : one;
+    const D3 fm0 = dmix(dmix(one, tint, specTint) * (0.08 * specular), base, metallic);
+    const double cosWo = std::max(ddot(n, wo), 0.0), cosWi = std::max(ddot(n, wi), 0.0);
+    const D3 h = dnormalize(wo + wi);
+    const double hCosWi = ddot(h, wi);
+    D3 res{0.0, 0.0, 0.0};
+    if (!(cosWo < 1e-10 || cosWi < 1e-10)) {
+        // diffuse with the subsurface mix, times (1 - metallic)
+        const double hc2 = hCosWi * hCosWi;
+        const double fi = dpow5(1.0 - cosWi), fo = dpow5(1.0 - cosWo);
+        const double fd90 = 0.5 + 2.0 * rough * hc2;
+        const double fd = ((1.0 - fi) + fd90 * fi) * ((1.0 - fo) + fd90 * fo);
+        const double fss90 = rough * hc2;
+        const double fss = ((1.0 - fi) + fss90 * fi) * ((1.0 - fo) + fss90 * fo);
+        const double ss = 1.25 * (fss * (1.0 / (cosWi + cosWo) - 0.5) + 0.5);
+        res = res + base * ((fd * (1.0 - subsurface) + ss * subsurface) / kPiD * (1.0 - metallic));
+        // metal: Schlick Fresnel, GGX, Smith-Schlick G
+        const double w5 = dpow5(1.0 - std::fabs(ddot(h, wo)));
+        const D3 fm = fm0 + (one - fm0) * w5;
+        const double c = ddot(n, h);
+        double dm = 0.0;
+        if (!(c < 1e-6)) {
+            const double den = c * c * (a2 - 1.0) + 1.0;
+            dm = a2 / (den * den * kPiD);
+        }
+        const double gm = dschlickG(std::fabs(ddot(n, wo)), alpha) * dschlickG(std::fabs(ddot(n, wi)), alpha);
+        const double denom = 4.0 * cosWi * cosWo;
+        if (!(denom < 1e-7)) res = res + fm * (dm * gm / denom);
+    }
+    if (!(cosWo < 1e-6 || cosWi < 1e-6)) {  // clearcoat
+        const double w5 = dpow5(1.0 - std::fabs(ddot(h, wo)));
+        const D3 fc = base + (one - base) * w5;
+        const double c = std::max(ddot(n, h), 0.0), ca2 = ccAlpha * ccAlpha;
+        const double dc = (ca2 - 1.0) / (2.0 * kPiD * std::log(ccAlpha) * (1.0 + (ca2 - 1.0) * c * c));
+        const double gc = dschlickG(std::fabs(ddot(n, wo)), 0.25) * dschlickG(std::fabs(ddot(n, wi)), 0.25);
+        const double denom = 4.0 * cosWi * cosWo;
+        if (!(denom < 1e-7)) res = res + fc * (dc * gc / denom * clearcoat * 0.25);
+    }
+    const double sheenScale = dpow5(1.0 - hCosWi) * sheen * (ddot(n, wi) < 0.0 ? 0.0 : 1.0);
+    res = res + dmix(one, tint, sheenTint) * sheenScale;
+    return res;
+}
+
+// out[i][c] = (d f_c / d q_i) / f_c for the BSDF value of material matId.
+void bsdfLogGrad(const OrcScene& sc, int matId, vec3 wo, vec3 wi, vec3 n, double out[6][3]) {
+    const float* m = sc.materials + 16 * matId;
+    for (int i = 0; i < 6; i++) out[i][0] = out[i][1] = out[i][2] = 0.0;
+    if (loadMaterialType(sc, matId) != PrincipledBRDF) {
+        for (int c = 0; c < 3; c++) out[c][c] = m[c] != 0.0f ? 1.0 / (double)m[c] : 0.0;
+        return;
+    }
+    const D3 o = d3(wo), i3 = d3(wi), nn = d3(n);
+    double q[6] = {m[0], m[1], m[2], m[3], m[5], m[6]};
+    const D3 f = principledD(m, q, o, i3, nn);
+    const double fv[3] = {f.x, f.y, f.z};
+    for (int i = 0; i < 6; i++) {
+        const double q0 = q[i], h = 1e-6 * std::max(1.0, std::fabs(q0));
+        q[i] = q0 + h;
+        const D3 fp = principledD(m, q, o, i3, nn);
+        q[i] = q0 - h;
+        const D3 fmn = principledD(m, q, o, i3, nn);
+        q[i] = q0;
+        const double dv[3] = {(fp.x - fmn.x) / (2 * h), (fp.y - fmn.y) / (2 * h), (fp.z - fmn.z) / (2 * h)};
+        for (int c = 0; c < 3; c++) out[i][c] = fv[c] != 0.0 ? dv[c] / fv[c] : 0.0;
+    }
+}
+
+struct AdjCtx {
+    const int32_t* lightInst;  // per light triangle: its instance
+    const float* instPower;    // 3 per instance
+    int nmat;
+    double delta[3];           // d loss / d sample radiance
+    std::vector<double> A;     // nmat*6*3: sum of dlog f of the path's sampled BSDF values
+    double* grad;              // nmat*6 + 3*ninst
+};
+
+void addContribution(AdjCtx& cx, vec3 C, const double (*local)[3], int localMat, int lightId) {
+    const double Cc[3] = {C.x, C.y, C.z};
+    for (int m = 0; m < cx.nmat; m++)
+        for (int i = 0; i < 6; i++) {
+            double g = 0.0;
+            for (int c = 0; c < 3; c++) {
+                double l = cx.A[(size_t)(6 * m + i) * 3 + c] + (local && m == localMat ? local[i][c] : 0.0);
+                g += cx.delta[c] * Cc[c] * l;
+            }
+            cx.grad[6 * m + i] += g;
+        }
+    if (lightId >= 0) {
+        const int k = cx.lightInst[lightId];
+        for (int c = 0; c < 3; c++) {
+            const double P = cx.instPower[3 * k + c];
+            if (P != 0.0) cx.grad[6 * cx.nmat + 3 * k + c] += cx.delta[c] * Cc[c] / P;
+        }
+    }
+}
+
+// pathIntegTrace (path_integ_naive.glsl:35-143) with the same sample
+// consumption, feeding every contribution to addContribution.
+void pathAdjoint(const OrcScene& sc, Ray ray, int& s, Rng& g, AdjCtx& cx) {
+    std::fill(cx.A.begin(), cx.A.end(), 0.0);
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    vec3 pos = rayPoint(ray, primDist);
+    if (id == -1) return;
+    if (id - sc.objPrimCount >= 0) {
+        addContribution(cx, lightLe(sc, id - sc.objPrimCount, pos, -ray.dir), nullptr, -1, id - sc.objPrimCount);
+        return;
+    }
+    vec3 wo = -ray.dir;
+    vec3 throughput(1.0f);
+    double lg[6][3];
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        SurfaceInfo surf = triangleSurfaceInfo(sc, id, pos);
+        int matId = sc.matTexIndex[id] & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != Dielectric && matType != ThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        if (sc.sampleLight) {
+            float ud = sample1D(sc, g, s);
+            float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
+            float pdfSampleLight = 0.0f;
+            if (sc.nLightTriangles > 0)
+                pdfSampleLight = sc.lightEnvUniformSample ? sc.lightPortion : sc.lightSum / (sc.lightSum + sc.envSum);
+            int lid = ud < pdfSampleLight ? lightSampleOne(sc, vec2(u0, u1)) : -1;
+            LightLiSample ls = sampleLightAndEnv(sc, pos, ud, u0, u1, u2, u3);
+            if (ls.pdf > 0.0f) {
+                vec3 f = materialBSDF(matType, mp, wo, ls.wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                float weight = biHeuristic(ls.pdf, fpdf);
+                vec3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+                bsdfLogGrad(sc, matId, wo, ls.wi, surf.ns, lg);
+                addContribution(cx, C, lg, matId, lid);
+            }
+        }
+        float b0 = sample1D(sc, g, s), b1 = sample1D(sc, g, s), b2 = sample1D(sc, g, s);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        bsdfLogGrad(sc, matId, wo, wi, surf.ns, lg);
+        for (int i = 0; i < 6; i++)
+            for (int c = 0; c < 3; c++) cx.A[(size_t)(6 * matId + i) * 3 + c] += lg[i][c];
+        throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        ray = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, ray, dist);
+        int lightId = nextId - sc.objPrimCount;
+        vec3 nextPos = rayPoint(ray, dist);
+        if (nextId == -1) {
+            vec3 radiance = envLe(sc, wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float envPdf = envPdfLi(sc, wi) * pdfSelectEnv(sc);
+                weight = (envPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, envPdf);
+            }
+            addContribution(cx, radiance * throughput * weight, nullptr, -1, -1);
+            break;
+        } else if (lightId >= 0) {
+            vec3 radiance = lightLe(sc, lightId, nextPos, -wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, lightId);
+                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
+            }
+            addContribution(cx, radiance * throughput * weight, nullptr, -1, lightId);
+            break;
+        }
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+            if (sample1D(sc, g, s) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        id = nextId;
+        pos = nextPos;
+        wo = -wi;
+    }
+}
+
+// One sample of renderPixel replayed through pathAdjoint.
+void pixelAdjoint(const OrcScene& sc, int px, int py, int spp, int freeCounter, AdjCtx& cx) {
+    vec2 texSize((float)sc.filmW, (float)sc.filmH);
+    vec2 scr = vec2((float)px, (float)py) / texSize;
+    vec2 nc = noiseTexture(sc, scr);
+    nc = noiseTexture(sc, nc);
+    vec2 tc = texSize * nc;
+    Rng g;
+    g.randSeed = f2u(tc.x) * (uint32_t)freeCounter + f2u(tc.y);
+    g.sampleSeed = f2u(tc.x) * f2u(tc.y);
+    const int sampleNum = 131072, sampleDim = 256;
+    int off = (int)((uint32_t)spp * (uint32_t)sampleDim);
+    if (off > sampleNum * sampleDim) off -= sampleNum * sampleDim;
+    g.sampleOffset = off;
+    int s = 0;
+    float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    pathAdjoint(sc, ray, s, g, cx);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1472,6 +1712,53 @@ void orc_camera(const float* angle, float fov, float* out) {
     o[12] = inv.c1.x; o[13] = inv.c1.y; o[14] = inv.c1.z;
     o[15] = inv.c2.x; o[16] = inv.c2.y; o[17] = inv.c2.z;
     o[18] = std::tan(fov * 0.5f * rad);
+}
+
+// Gradient of sum(dimage * image) for the image = mean of samples 0..spp-1
+// of the path tracer (sample k with freeCounter k + 1; NaN samples dropped),
+// with respect to (per material: baseColor rgb, raw roughness, metallic,
+// specular; per light instance: power rgb), into grad[nmat*6 + ninst*3].
+void orc_diff_grad(const OrcScene* sc, int32_t spp, const float* dimage, const int32_t* lightInst,
+                   const float* instPower, int32_t nmat, int32_t ninst, double* grad, int32_t nthreads) {
+    const int64_t npix = (int64_t)sc->filmW * sc->filmH;
+    const size_t np = (size_t)nmat * 6 + (size_t)ninst * 3;
+    std::atomic<int64_t> next{0};
+    std::vector<std::vector<double>> part((size_t)std::max(nthreads, 1), std::vector<double>(np, 0.0));
+    auto work = [&](int t) {
+        AdjCtx cx;
+        cx.lightInst = lightInst;
+        cx.instPower = instPower;
+        cx.nmat = nmat;
+        cx.A.assign((size_t)nmat * 18, 0.0);
+        cx.grad = part[(size_t)t].data();
+        for (;;) {
+            int64_t i = next.fetch_add(8);
+            if (i >= npix) break;
+            int64_t e = std::min<int64_t>(npix, i + 8);
+            for (; i < e; i++) {
+                int px = (int)(i % sc->filmW), py = (int)(i / sc->filmW);
+                for (int c = 0; c < 3; c++) cx.delta[c] = (double)dimage[3 * i + c] / spp;
+                if (cx.delta[0] == 0.0 && cx.delta[1] == 0.0 && cx.delta[2] == 0.0) continue;
+                for (int k = 0; k < spp; k++) {
+                    bool ok;
+                    renderPixel(*sc, px, py, k, k + 1, ok);
+                    if (ok) pixelAdjoint(*sc, px, py, k, k + 1, cx);
+                }
+            }
+        }
+    };
+    if (nthreads <= 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthreads; t++) th.emplace_back(work, t);
+        for (auto& t : th) t.join();
+    }
+    for (size_t j = 0; j < np; j++) {
+        double acc = 0.0;
+        for (auto& p : part) acc += p[j];
+        grad[j] = acc;
+    }
 }
 
 }  // extern "C"

@@ -77,6 +77,13 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_batch_set_config": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "zgl_batch_get_config": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "zgl_batch_destroy": (C.c_int32, [C.c_void_p]),
+    "zgl_diff_create": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "zgl_diff_param_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "zgl_diff_get_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_diff_set_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_diff_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_diff_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_diff_destroy": (C.c_int32, [C.c_void_p]),
 }
 
 

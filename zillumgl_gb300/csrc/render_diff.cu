@@ -1,0 +1,408 @@
+// render_diff.cu — differentiable path tracing by path replay.
+//
+// Forward: every (pixel, sample) path of the MIS path tracer
+// (pathIntegTrace, path_integ_naive.glsl:35-143, with the plain integrator's
+// seeds: sample s uses freeCounter = s + 1) is traced once; its radiance is
+// kept per sample and the image is the per-pixel sum over samples in sample
+// order divided by spp.
+//
+// Backward (Path Replay Backpropagation, Vicini, Speierer and Jakob 2021):
+// each path is replayed from its seed (no path storage), with sampling
+// decisions, pdfs, MIS weights and Russian roulette detached.  The replay
+// carries the remaining radiance L_rem = L_total - (contributions already
+// met); at a vertex whose sampled BSDF value f enters every later
+// contribution, d/dtheta of those contributions is L_rem / f * df/dtheta per
+// channel; a light sample at the vertex contributes C / f_light *
+// df_light/dtheta; emission contributes C / P * dP for the emitting light
+// instance's power P.  BSDF derivatives come from dual numbers (dual.cuh).
+// Visibility discontinuities are not differentiated.  Gradients are reduced
+// per block in shared memory and added to the output with atomics.
+// No counterpart in the reference.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dual.cuh"
+#include "path_trace.cuh"
+#include "scene.h"
+#include "zgl_internal.h"
+
+struct zgl_diff {
+    zgl_scene* scene = nullptr;
+    zgl_integrator_params params{};
+    int32_t spp = 0;
+    int32_t nmat = 0, ninst = 0, nparams = 0;
+    float* d_samples = nullptr;   // spp * npix * 3 per-sample radiance
+    int32_t* d_lightInst = nullptr;  // per light triangle: instance index
+    float* d_values = nullptr;       // current parameter values
+    std::vector<uint32_t> lightFirst;
+    std::vector<float> instPower;  // 3 per instance (current)
+    std::vector<float> params_host;
+};
+
+namespace zgl {
+namespace {
+
+constexpr int kMaxDiffParams = 1024;
+
+struct DiffInfo {
+    int32_t nmat;
+    int32_t nparams;
+    const int32_t* lightInst;
+};
+
+// forward: one thread per (pixel, sample); blockIdx.y = sample
+__global__ void __launch_bounds__(kTileX* kTileY)
+diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, float* __restrict__ samples) {
+    __shared__ uint32_t row[256];
+    const int32_t s = blockIdx.y;
+    const uint32_t off = sample_offset(s);
+    load_sobol_row(sc, off, row);
+    const int tile = blockIdx.x;
+    const int px = (tile % tilesX) * kTileX + threadIdx.x;
+    const int py = (tile / tilesX) * kTileY + threadIdx.y;
+    if (px >= sc.filmW || py >= sc.filmH) return;
+    const size_t pix = (size_t)py * sc.filmW + px;
+    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+    Sampler g;
+    g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
+    g.sampleSeed = seed.x * seed.y;
+    g.sampleOffset = off;
+    g.dim = 0;
+    g.mode = sc.sampler;
+    g.rowCache = row;
+    g.mats = sc.sobol;
+    v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    v3 r = pathTrace(sc, pp, ray, g);
+    float* o = samples + 3 * ((size_t)s * sc.filmW * sc.filmH + pix);
+    o[0] = r.x;
+    o[1] = r.y;
+    o[2] = r.z;
+}
+
+// image = (sum over samples in order, NaN samples dropped) / spp
+__global__ void diff_reduce_kernel(const float* __restrict__ samples, int64_t npix, int32_t spp,
+                                   float* __restrict__ image) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    float r = 0.0f, g = 0.0f, b = 0.0f;
+    for (int s = 0; s < spp; s++) {
+        const float* x = samples + 3 * ((size_t)s * npix + p);
+        if (!(zisnan(x[0]) || zisnan(x[1]) || zisnan(x[2]))) {
+            r = r + x[0];
+            g = g + x[1];
+            b = b + x[2];
+        }
+    }
+    float inv = (float)spp;
+    image[3 * p] = r / inv;
+    image[3 * p + 1] = g / inv;
+    image[3 * p + 2] = b / inv;
+}
+
+__device__ __forceinline__ void add_mat_grad(float* sg, int matId, const v3& delta, const v3& scale, const BsdfGrad& bg) {
+    // sum_c delta_c * scale_c * df_c / f_c, channels with f_c == 0 carry no radiance
+    v3 w;
+    w.x = bg.f.x != 0.0f ? delta.x * scale.x / bg.f.x : 0.0f;
+    w.y = bg.f.y != 0.0f ? delta.y * scale.y / bg.f.y : 0.0f;
+    w.z = bg.f.z != 0.0f ? delta.z * scale.z / bg.f.z : 0.0f;
+#pragma unroll
+    for (int i = 0; i < kDiffMatParams; i++) {
+        float gsum = w.x * bg.df[i].x + w.y * bg.df[i].y + w.z * bg.df[i].z;
+        if (gsum != 0.0f) atomicAdd(&sg[kDiffMatParams * matId + i], gsum);
+    }
+}
+__device__ __forceinline__ void add_power_grad(float* sg, const DiffInfo& di, const float* params, int lightId,
+                                               const v3& delta, const v3& C) {
+    int inst = __ldg(&di.lightInst[lightId]);
+    int base = kDiffMatParams * di.nmat + 3 * inst;
+    float P[3] = {__ldg(&params[base]), __ldg(&params[base + 1]), __ldg(&params[base + 2])};
+    float c[3] = {C.x, C.y, C.z}, d[3] = {delta.x, delta.y, delta.z};
+    for (int k = 0; k < 3; k++)
+        if (P[k] != 0.0f && c[k] != 0.0f) atomicAdd(&sg[base + k], d[k] * c[k] / P[k]);
+}
+
+// Replay of pathIntegTrace with adjoint accounting (same sample consumption).
+__device__ void replay_adjoint(const DeviceScene& sc, const PathParams& pp, const DiffInfo& di, const float* params,
+                               Ray ray, Sampler& g, v3 Lrem, v3 delta, float* sg) {
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    v3 pos = rayPoint(ray, primDist);
+    if (id == -1) return;  // environment: no differentiable parameter
+    if (id - sc.objPrimCount >= 0) {
+        int lightId = id - sc.objPrimCount;
+        v3 C = lightLe(sc, lightId, pos, -ray.dir);
+        add_power_grad(sg, di, params, lightId, delta, C);
+        return;
+    }
+    v3 wo = -ray.dir;
+    v3 throughput = mk3(1.0f);
+    for (int bounce = 1; bounce <= pp.maxDepth; bounce++) {
+        TriShade tri = loadTri(sc, id);
+        Surface surf = surfaceInfo(tri, pos);
+        int matId = tri.matTex & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
+            surf.ns = -surf.ns;
+            surf.ng = -surf.ng;
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        if (pp.sampleLight) {
+            float ud = sample1D(g);
+            float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+            // the light pick of sampleLightAndEnv, kept to know which light is sampled
+            float pdfSampleLight = 0.0f;
+            if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
+            bool sampleLight = ud < pdfSampleLight;
+            int lid = sampleLight ? lightSampleOne(sc, mk2(u0, u1)) : -1;
+            LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
+            if (ls.pdf > 0.0f) {
+                v3 f = materialBSDF(matType, mp, wo, ls.wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                float weight = biHeuristic(ls.pdf, fpdf);
+                v3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+                BsdfGrad bg = bsdfGrad(sc, matType, matId, wo, ls.wi, surf.ns);
+                add_mat_grad(sg, matId, delta, C, bg);
+                if (lid >= 0) add_power_grad(sg, di, params, lid, delta, C);
+                Lrem = Lrem - C;
+            }
+        }
+        float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        v3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        // every later contribution carries this vertex's sampled BSDF value
+        {
+            BsdfGrad bg = bsdfGrad(sc, matType, matId, wo, wi, surf.ns);
+            add_mat_grad(sg, matId, delta, Lrem, bg);
+        }
+        throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        ray = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, ray, dist);
+        int lightId = nextId - sc.objPrimCount;
+        v3 nextPos = rayPoint(ray, dist);
+        if (nextId == -1) break;  // environment emission: no parameter
+        if (lightId >= 0) {
+            v3 radiance = lightLe(sc, lightId, nextPos, -wi);
+            float weight = 1.0f;
+            if (pp.sampleLight && !deltaBsdf) {
+                float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, pp, lightId);
+                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
+            }
+            v3 C = radiance * throughput * weight;
+            add_power_grad(sg, di, params, lightId, delta, C);
+            break;
+        }
+        if (pp.rr && bounce >= pp.rrStart) {
+            float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+            if (sample1D(g) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        id = nextId;
+        pos = nextPos;
+        wo = -wi;
+    }
+}
+
+__global__ void __launch_bounds__(kTileX* kTileY)
+diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
+                     int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
+                     float* __restrict__ grad) {
+    __shared__ uint32_t row[256];
+    __shared__ float sg[kMaxDiffParams];
+    for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY) sg[i] = 0.0f;
+    const int32_t s = blockIdx.y;
+    const uint32_t off = sample_offset(s);
+    load_sobol_row(sc, off, row);  // includes the barrier that publishes sg
+    const int tile = blockIdx.x;
+    const int px = (tile % tilesX) * kTileX + threadIdx.x;
+    const int py = (tile / tilesX) * kTileY + threadIdx.y;
+    if (px < sc.filmW && py < sc.filmH) {
+        const size_t npix = (size_t)sc.filmW * sc.filmH;
+        const size_t pix = (size_t)py * sc.filmW + px;
+        const float* L = samples + 3 * ((size_t)s * npix + pix);
+        v3 Ltot = mk3(L[0], L[1], L[2]);
+        // image = sum / spp, NaN samples excluded from the sum
+        if (!hasNan(Ltot)) {
+            const float inv = 1.0f / (float)spp;
+            v3 delta = mk3(dimage[3 * pix] * inv, dimage[3 * pix + 1] * inv, dimage[3 * pix + 2] * inv);
+            if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
+                const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+                Sampler g;
+                g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
+                g.sampleSeed = seed.x * seed.y;
+                g.sampleOffset = off;
+                g.dim = 0;
+                g.mode = sc.sampler;
+                g.rowCache = row;
+                g.mats = sc.sobol;
+                v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+                float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+                Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+                replay_adjoint(sc, pp, di, params, ray, g, Ltot, delta, sg);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY)
+        if (sg[i] != 0.0f) atomicAdd(&grad[i], sg[i]);
+}
+
+}  // namespace
+
+// Rewrites the differentiable parameters of a scene: material records
+// (baseColor, roughness, metallic, specular) and light-instance powers with
+// the light tables that depend on them (Scene.cpp:200-243).
+void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, const std::vector<uint32_t>& first,
+                           std::vector<float>& instPower);
+
+}  // namespace zgl
+
+using namespace zgl;
+
+namespace {
+
+PathParams path_params(const zgl_integrator_params& p) {
+    return PathParams{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
+                      p.light_portion};
+}
+
+bool device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" {
+
+zgl_status zgl_diff_create(zgl_scene* scene, const zgl_integrator_params* params, int32_t spp, zgl_diff** out) {
+    ZGL_API_BEGIN
+    if (!scene || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_create: NULL argument");
+    *out = nullptr;
+    if (scene->host_only) fail(ZGL_ERR_STATE, "zgl_diff_create: scene was created host-only");
+    if (spp < 1 || spp > 4096) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_create: spp %d out of range", spp);
+    auto* d = new zgl_diff();
+    try {
+        d->scene = scene;
+        zgl_integrator_params_default(&d->params);
+        if (params) d->params = *params;
+        d->spp = spp;
+        d->nmat = (int32_t)(scene->materials.size() / 16);
+        d->lightFirst = scene->lightFirst;
+        d->instPower = scene->lightInstPower;
+        d->ninst = (int32_t)(d->instPower.size() / 3);
+        d->nparams = kDiffMatParams * d->nmat + 3 * d->ninst;
+        if (d->nparams > kMaxDiffParams) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_create: %d parameters exceed %d", d->nparams, kMaxDiffParams);
+        size_t npix = (size_t)scene->filmW * scene->filmH;
+        ZGL_CUDA(cudaMalloc(&d->d_samples, sizeof(float) * 3 * npix * (size_t)spp));
+        std::vector<int32_t> inst((size_t)std::max(scene->nLight, 1), 0);
+        for (int k = 0; k < d->ninst; k++)
+            for (uint32_t t = d->lightFirst[(size_t)k]; t < d->lightFirst[(size_t)k + 1]; t++) inst[t] = k;
+        ZGL_CUDA(cudaMalloc(&d->d_lightInst, sizeof(int32_t) * inst.size()));
+        ZGL_CUDA(cudaMemcpy(d->d_lightInst, inst.data(), sizeof(int32_t) * inst.size(), cudaMemcpyHostToDevice));
+        // current parameter values
+        d->params_host.assign((size_t)d->nparams, 0.0f);
+        for (int m = 0; m < d->nmat; m++) {
+            const float* r = &scene->materials[16 * (size_t)m];
+            float v[6] = {r[0], r[1], r[2], r[3], r[5], r[6]};
+            std::memcpy(&d->params_host[(size_t)kDiffMatParams * m], v, sizeof(v));
+        }
+        for (int k = 0; k < 3 * d->ninst; k++) d->params_host[(size_t)kDiffMatParams * d->nmat + k] = d->instPower[(size_t)k];
+        ZGL_CUDA(cudaMalloc(&d->d_values, sizeof(float) * (size_t)std::max(d->nparams, 1)));
+        ZGL_CUDA(cudaMemcpy(d->d_values, d->params_host.data(), sizeof(float) * (size_t)d->nparams, cudaMemcpyHostToDevice));
+    } catch (...) {
+        if (d->d_samples) cudaFree(d->d_samples);
+        if (d->d_lightInst) cudaFree(d->d_lightInst);
+        if (d->d_values) cudaFree(d->d_values);
+        delete d;
+        throw;
+    }
+    *out = d;
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_param_count(const zgl_diff* d, int32_t* n) {
+    ZGL_API_BEGIN
+    if (!d || !n) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_param_count: NULL");
+    *n = d->nparams;
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_get_params(const zgl_diff* d, float* out) {
+    ZGL_API_BEGIN
+    if (!d || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_get_params: NULL");
+    std::memcpy(out, d->params_host.data(), sizeof(float) * d->params_host.size());
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_set_params(zgl_diff* d, const float* params) {
+    ZGL_API_BEGIN
+    if (!d || !params) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: NULL");
+    // work queued on any stream may still read the scene or write `params`
+    ZGL_CUDA(cudaDeviceSynchronize());
+    std::vector<float> p((size_t)d->nparams);
+    if (device_ptr(params)) ZGL_CUDA(cudaMemcpy(p.data(), params, sizeof(float) * p.size(), cudaMemcpyDeviceToHost));
+    else std::memcpy(p.data(), params, sizeof(float) * p.size());
+    for (float v : p)
+        if (!std::isfinite(v)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: non-finite parameter");
+    scene_set_diff_params(d->scene, p.data(), d->nmat, d->lightFirst, d->instPower);
+    d->params_host = p;
+    ZGL_CUDA(cudaMemcpy(d->d_values, p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice));
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_forward(zgl_diff* d, float* image, void* stream) {
+    ZGL_API_BEGIN
+    if (!d || !image) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_forward: NULL");
+    if (!device_ptr(image)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_forward: image must be device memory");
+    const zgl_scene* s = d->scene;
+    cudaStream_t st = (cudaStream_t)stream;
+    int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
+    dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
+    diff_forward_kernel<<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
+    ZGL_CUDA(cudaGetLastError());
+    int64_t npix = (int64_t)s->filmW * s->filmH;
+    diff_reduce_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(d->d_samples, npix, d->spp, image);
+    ZGL_CUDA(cudaGetLastError());
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_backward(zgl_diff* d, const float* d_image, float* d_params, void* stream) {
+    ZGL_API_BEGIN
+    if (!d || !d_image || !d_params) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_backward: NULL");
+    if (!device_ptr(d_image) || !device_ptr(d_params))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_diff_backward: arrays must be device memory");
+    const zgl_scene* s = d->scene;
+    cudaStream_t st = (cudaStream_t)stream;
+    ZGL_CUDA(cudaMemsetAsync(d_params, 0, sizeof(float) * (size_t)d->nparams, st));
+    DiffInfo di{d->nmat, d->nparams, d->d_lightInst};
+    int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
+    dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
+    diff_backward_kernel<<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
+                                                                d->spp, d->d_samples, d_image, d_params);
+    ZGL_CUDA(cudaGetLastError());
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_destroy(zgl_diff* d) {
+    ZGL_API_BEGIN
+    if (!d) return ZGL_OK;
+    if (d->d_samples) cudaFree(d->d_samples);
+    if (d->d_lightInst) cudaFree(d->d_lightInst);
+    if (d->d_values) cudaFree(d->d_values);
+    delete d;
+    ZGL_API_END
+}
+
+}  // extern "C"

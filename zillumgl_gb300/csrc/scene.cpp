@@ -239,6 +239,43 @@ T* upload(const std::vector<T>& v) {
     return d;
 }
 
+// Per-triangle light power (instance power split by area), light areas, the
+// light alias table and the power sum (Scene.cpp:200-243).  Light triangle t
+// is scene triangle objPrimCount + t.
+void light_tables(zgl_scene& s) {
+    std::vector<float> pdf;
+    s.lightPower.clear();
+    s.lightArea.clear();
+    s.lightAlias.clear();
+    s.lightProb.clear();
+    s.lightSum = 0.0f;
+    auto vert = [&](uint32_t t, int j) {
+        const float* p = &s.vertices[3 * (size_t)s.indices[3 * ((size_t)s.objPrimCount + t) + j]];
+        return mk3(p[0], p[1], p[2]);
+    };
+    for (size_t k = 0; k + 1 < s.lightFirst.size(); k++) {
+        uint32_t f0 = s.lightFirst[k], f1 = s.lightFirst[k + 1];
+        v3 P = mk3(s.lightInstPower[3 * k], s.lightInstPower[3 * k + 1], s.lightInstPower[3 * k + 2]);
+        float sumArea = 0.0f;
+        for (uint32_t t = f0; t < f1; t++) sumArea += length(cross(vert(t, 2) - vert(t, 0), vert(t, 1) - vert(t, 0)));
+        for (uint32_t t = f0; t < f1; t++) {
+            v3 a = vert(t, 0), b = vert(t, 1), c = vert(t, 2);
+            float area = length(cross(c - a, b - a));
+            v3 pw = P * area / sumArea;
+            s.lightPower.push_back(pw.x);
+            s.lightPower.push_back(pw.y);
+            s.lightPower.push_back(pw.z);
+            s.lightArea.push_back(0.5f * length(cross(c - a, b - a)));  // triangleArea (math.glsl:147-150)
+            float l = dot(pw, mk3(0.299f, 0.587f, 0.114f));
+            pdf.push_back(l);
+            s.lightSum += l;
+        }
+    }
+    if (!pdf.empty()) alias_build(pdf, s.lightAlias, s.lightProb);
+    if (s.nLight > 0 && !(s.lightSum > 0.0f))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: lights have zero total power or zero area");
+}
+
 void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
     if (d.obj_n_triangles > 0 && (!d.obj_vertices || !d.obj_normals || !d.obj_indices || !d.obj_mat_tex))
         fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: object arrays missing");
@@ -298,40 +335,20 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
         if ((size_t)mat >= d.n_materials) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu material out of range", t);
     }
 
-    // light power split by area and the light alias table (Scene.cpp:200-243)
-    std::vector<float> pdf;
-    s.lightSum = 0.0f;
+    // light instances, then power split by area and the light alias table
     size_t covered = 0;
+    s.lightFirst.assign(1, 0u);
     for (size_t k = 0; k < d.n_light_instances; k++) {
         uint32_t f0 = d.light_first[k], f1 = d.light_first[k + 1];
         if (f0 != covered || f1 < f0 || f1 > d.light_n_triangles)
             fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: light_first must partition the light triangles");
         covered = f1;
-        v3 P = mk3(d.light_power[3 * k], d.light_power[3 * k + 1], d.light_power[3 * k + 2]);
-        auto vert = [&](uint32_t t, int j) {
-            const float* p = d.light_vertices + 3 * (size_t)d.light_indices[3 * t + j];
-            return mk3(p[0], p[1], p[2]);
-        };
-        float sumArea = 0.0f;
-        for (uint32_t t = f0; t < f1; t++) sumArea += length(cross(vert(t, 2) - vert(t, 0), vert(t, 1) - vert(t, 0)));
-        for (uint32_t t = f0; t < f1; t++) {
-            v3 a = vert(t, 0), b = vert(t, 1), c = vert(t, 2);
-            float area = length(cross(c - a, b - a));
-            v3 pw = P * area / sumArea;
-            s.lightPower.push_back(pw.x);
-            s.lightPower.push_back(pw.y);
-            s.lightPower.push_back(pw.z);
-            s.lightArea.push_back(0.5f * length(cross(c - a, b - a)));  // triangleArea (math.glsl:147-150)
-            float l = dot(pw, mk3(0.299f, 0.587f, 0.114f));
-            pdf.push_back(l);
-            s.lightSum += l;
-        }
+        s.lightFirst.push_back(f1);
+        for (int c = 0; c < 3; c++) s.lightInstPower.push_back(d.light_power[3 * k + c]);
     }
     if (covered != d.light_n_triangles)
         fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: light_first does not cover every light triangle");
-    if (!pdf.empty()) alias_build(pdf, s.lightAlias, s.lightProb);
-    if (s.nLight > 0 && !(s.lightSum > 0.0f))
-        fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: lights have zero total power or zero area");
+    light_tables(s);
 
     // environment map (EnvironmentMap.cpp:8-59)
     s.envRotation = d.env_rotation;
@@ -425,6 +442,51 @@ void upload_scene(zgl_scene& s) {
 }
 
 }  // namespace
+
+// Writes new material parameters (per material: baseColor rgb, roughness,
+// metallic, specular into record slots 0-3, 5, 6) and light-instance powers
+// (3 per instance), rebuilds the light tables that depend on the powers and
+// updates the device copies in place.
+void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, const std::vector<uint32_t>& first,
+                           std::vector<float>& instPower) {
+    (void)first;
+    const int ninst = (int)(instPower.size() / 3);
+    for (int k = 0; k < 3 * ninst; k++)
+        if (p[6 * nmat + k] < 0.0f) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: negative light power");
+    std::vector<float> oldInst = s->lightInstPower;
+    for (int k = 0; k < 3 * ninst; k++) s->lightInstPower[(size_t)k] = p[6 * nmat + k];
+    try {
+        light_tables(*s);
+    } catch (...) {
+        s->lightInstPower = oldInst;
+        light_tables(*s);
+        throw;
+    }
+    instPower = s->lightInstPower;
+    for (int m = 0; m < nmat; m++) {
+        float* r = &s->materials[16 * (size_t)m];
+        const float* q = p + 6 * (size_t)m;
+        r[0] = q[0];
+        r[1] = q[1];
+        r[2] = q[2];
+        r[3] = q[3];
+        r[5] = q[4];
+        r[6] = q[5];
+    }
+    if (nmat > 0)
+        ZGL_CUDA(cudaMemcpy(s->d_materials, s->materials.data(), sizeof(float) * s->materials.size(),
+                            cudaMemcpyHostToDevice));
+    if (s->nLight > 0) {
+        std::vector<float4> lp((size_t)s->nLight);
+        for (int i = 0; i < s->nLight; i++)
+            lp[(size_t)i] = make_float4(s->lightPower[3 * i], s->lightPower[3 * i + 1], s->lightPower[3 * i + 2],
+                                        s->lightArea[(size_t)i]);
+        ZGL_CUDA(cudaMemcpy(s->d_lightPower, lp.data(), sizeof(float4) * lp.size(), cudaMemcpyHostToDevice));
+        ZGL_CUDA(cudaMemcpy(s->d_lightAlias, s->lightAlias.data(), 4 * s->lightAlias.size(), cudaMemcpyHostToDevice));
+        ZGL_CUDA(cudaMemcpy(s->d_lightProb, s->lightProb.data(), 4 * s->lightProb.size(), cudaMemcpyHostToDevice));
+    }
+}
+
 }  // namespace zgl
 
 zgl::DeviceScene zgl_scene::view() const {

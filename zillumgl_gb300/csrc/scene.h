@@ -24,7 +24,9 @@ struct zgl_scene {
     int32_t nLight = 0;
     std::vector<float> materials;  // 16 per material
 
-    // lights (Scene.cpp:200-243)
+    // lights (Scene.cpp:200-243): instance ranges and powers, then per triangle
+    std::vector<uint32_t> lightFirst;   // n_instances + 1
+    std::vector<float> lightInstPower;  // 3 per instance
     std::vector<float> lightPower;  // 3 per light triangle
     std::vector<float> lightArea;   // triangleArea of each light triangle
     std::vector<int32_t> lightAlias;

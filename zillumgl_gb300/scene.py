@@ -368,3 +368,76 @@ class BatchRenderer:
             self.close()
         except Exception:
             pass
+
+
+class DiffRenderer:
+    """Differentiable path tracer over a :class:`Scene` (zgl_diff_*).
+
+    :meth:`forward` renders the mean of the path tracer's first ``spp``
+    samples into a CUDA float32 tensor (H, W, 3); :meth:`backward` takes the
+    image adjoint (H, W, 3) and returns the gradient of
+    ``sum(adjoint * image)`` with respect to :meth:`params` by path replay.
+    Parameter layout: per material (baseColor r, g, b, raw roughness,
+    metallic, specular), then per light instance (power r, g, b)."""
+
+    MAT_PARAMS = 6
+
+    def __init__(self, scene: Scene, spp: int, params: IntegratorParams | None = None, **kw):
+        self.scene = scene
+        self.spp = spp
+        self.params_struct = params or default_params(**kw)
+        h = C.c_void_p()
+        call("zgl_diff_create", scene.handle, C.byref(self.params_struct), spp, C.byref(h))
+        self._h = h
+        n = C.c_int32()
+        call("zgl_diff_param_count", self._h, C.byref(n))
+        self.n_params = n.value
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        call("zgl_diff_get_params", self._h, out.ctypes.data)
+        return out
+
+    def set_params(self, values) -> None:
+        from .accel import _ptr
+
+        if getattr(values, "shape", None) != (self.n_params,):
+            raise ValueError(f"expected {self.n_params} parameters")
+        if not hasattr(values, "data_ptr"):
+            values = np.ascontiguousarray(values, np.float32)
+        elif str(values.dtype) != "torch.float32":
+            raise ValueError("parameters must be float32")
+        call("zgl_diff_set_params", self._h, _ptr(values))
+
+    def forward(self, out=None, stream=None):
+        import torch
+
+        from .accel import _ptr, _stream_handle
+
+        W, H = self.scene.film
+        if out is None:
+            out = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+        call("zgl_diff_forward", self._h, _ptr(out), _stream_handle(stream))
+        return out
+
+    def backward(self, d_image, out=None, stream=None):
+        import torch
+
+        from .accel import _ptr, _stream_handle
+
+        d_image = d_image.contiguous()
+        if out is None:
+            out = torch.empty(self.n_params, dtype=torch.float32, device=d_image.device)
+        call("zgl_diff_backward", self._h, _ptr(d_image), _ptr(out), _stream_handle(stream))
+        return out
+
+    def close(self):
+        if self._h:
+            call("zgl_diff_destroy", self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

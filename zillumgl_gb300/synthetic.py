@@ -361,6 +361,35 @@ def sphere_box_scene(seed: int, n_tris: int, width: int, height: int, sampler: i
     return d.normalized()
 
 
+def diff_scene(seed: int = 11, width: int = 512, height: int = 512, sampler: int = 1):
+    """The Cornell-style box of :func:`cornell_scene` with 8 principled
+    materials (5 walls, the two boxes sharing one, the two spheres), each with
+    baseColor U(0.2, 0.8)^3, roughness U(0.1, 0.9), metallic U(0, 1),
+    specular U(0, 1): 8 * 6 material parameters plus the light's power rgb."""
+    from .scene import PRINCIPLED, material, mat_tex
+
+    d = cornell_scene(seed=seed, width=width, height=height, sampler=sampler)
+    rng = np.random.default_rng(seed + 1000)
+    mats = [material(PRINCIPLED, base_color=rng.uniform(0.2, 0.8, 3), roughness=rng.uniform(0.1, 0.9),
+                     metallic=rng.uniform(0.0, 1.0), specular=rng.uniform(0.0, 1.0)) for _ in range(8)]
+    # cornell_scene material order: 5 walls, box, box, principled sphere, sphere
+    remap = np.array([0, 1, 2, 3, 4, 5, 5, 6, 7], np.int32)
+    old = d.obj_mat_tex & 0xFFFF
+    d.obj_mat_tex = np.array([mat_tex(int(m)) for m in remap[old]], np.int32)
+    d.materials = np.stack(mats)
+    return d.normalized()
+
+
+def perturbed_params(p0: np.ndarray, n_materials: int, seed: int = 12, scale: float = 0.3) -> np.ndarray:
+    """Initial guess for inverse rendering: every material parameter moved by
+    U(-scale, scale) and clamped to [0.02, 1]; light power unchanged."""
+    rng = np.random.default_rng(seed)
+    p = np.array(p0, np.float32, copy=True)
+    k = 6 * n_materials
+    p[:k] = np.clip(p[:k] + rng.uniform(-scale, scale, k).astype(np.float32), 0.02, 1.0)
+    return p
+
+
 def batch_requests(seed: int = 3, n: int = 64):
     """Seeded request list of the batched-serving workload: n scenes with
     log-uniform triangle counts in [1k, 500k], log-uniform square films in
