@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--render", default="cornell,city,batch,diff", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
     ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
+    ap.add_argument("--diff-size", type=int, default=512, help="film side of the differentiable workload")
+    ap.add_argument("--diff-spp", type=int, default=32, help="samples per pixel of the differentiable workload")
     return ap.parse_args()
 
 
@@ -144,6 +146,22 @@ def profiled_traffic():
         except Exception:
             return None
     return None
+
+
+def l2_peak(stream):
+    """L2 read bandwidth (GB/s) by the library's own L2-resident read kernel:
+    best of 16/32/64 MiB buffers, 200 passes each."""
+    import ctypes as C
+
+    from zillumgl_gb300._lib import call
+
+    best, per = 0.0, {}
+    for mib in (16, 32, 64):
+        v = C.c_double()
+        call("zgl_measure_l2_read", mib << 20, 200, C.byref(v), stream.cuda_stream)
+        per[f"{mib}MiB"] = round(v.value, 1)
+        best = max(best, v.value)
+    return best, per
 
 
 def run_ours(args):
@@ -282,9 +300,13 @@ def run_ours(args):
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = profiled_traffic()
+    l2, l2_sweep = l2_peak(stream)
     roofline = {"bound": "hbm", "kernel": "trace_closest_kernel" if dom is closest else "trace_any_kernel",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": f"{peak_kind} hbm_gbs (copy bandwidth)",
+                "l2_peak": round(l2, 1), "l2_frac": round(achieved / l2, 4),
+                "l2_peak_source": "zgl_measure_l2_read: L2-resident buffer read by all SMs with 16-byte ld.global.cg, "
+                                  f"best of {l2_sweep} GB/s",
                 "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                 "traffic_note": traffic.get("note") if traffic else "no ncu capture committed yet",
                 "algorithmic_bytes_per_launch": int(dom_bytes),
@@ -295,7 +317,8 @@ def run_ours(args):
         ms = statistics.mean(per_launch[sp["name"]])
         workloads.append({"name": sp["name"], "ms": round(ms, 4), "mrays_s": round(nray / (ms * 1e-3) / 1e6, 1),
                           "visits_per_ray": round(sp["V"] / nray, 2), "tests_per_ray": round(sp["T"] / nray, 3),
-                          "gbs": round(sp["bytes"] / (ms * 1e-3) / 1e9, 1)})
+                          "gbs": round(sp["bytes"] / (ms * 1e-3) / 1e9, 1),
+                          "l2_frac": round(sp["bytes"] / (ms * 1e-3) / 1e9 / l2, 4)})
 
     # end to end through the C ABI with pinned host arrays
     e2e = None
@@ -514,13 +537,14 @@ def run_diff(args, stream, dev):
     from zillumgl_gb300.scene import DiffRenderer, Scene
     from zillumgl_gb300.synthetic import diff_scene, perturbed_params
 
-    data = diff_scene(seed=11, width=512, height=512)
+    data = diff_scene(seed=11, width=args.diff_size, height=args.diff_size)
     W, H = data.film
-    spp, params = 32, dict(max_depth=6)
+    spp, params = args.diff_spp, dict(max_depth=6)
     scene = Scene(data)
     dr = DiffRenderer(scene, spp, **params)
     p_true = dr.params()
-    target = dr.forward(stream=stream).clone()
+    target = dr.forward(stream=stream)
+    stream.synchronize()
     p = torch.tensor(perturbed_params(p_true, 8, seed=12), device=dev, requires_grad=True)
     opt = torch.optim.Adam([p], lr=0.01)
     img = torch.empty((H, W, 3), dtype=torch.float32, device=dev)

@@ -366,6 +366,18 @@ zgl_status zgl_diff_forward(zgl_diff* diff, float* image, void* stream);
 zgl_status zgl_diff_backward(zgl_diff* diff, const float* d_image, float* d_params, void* stream);
 zgl_status zgl_diff_destroy(zgl_diff* diff);
 
+/* ------------------------------------------------------------------------ */
+/* Measurement                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* L2 read bandwidth of the current device in GB/s: a `bytes`-sized buffer
+ * (a multiple of 16 in [1 MiB, 1 GiB]; keep it below the L2 size) is read
+ * `passes` times by all SMs with 16-byte L1-bypassing loads after two
+ * untimed passes; CUDA events time the passes on `stream`.  Synchronous.
+ * The traversal roofline uses it as the L2 peak.  No counterpart in the
+ * reference. */
+zgl_status zgl_measure_l2_read(size_t bytes, int32_t passes, double* gbs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,16 +14,17 @@
 // contribution, d/dtheta of those contributions is L_rem / f * df/dtheta per
 // channel; a light sample at the vertex contributes C / f_light *
 // df_light/dtheta; emission contributes C / P * dP for the emitting light
-// instance's power P.  BSDF derivatives come from dual numbers (dual.cuh).
-// Visibility discontinuities are not differentiated.  Gradients are reduced
-// per block in shared memory and added to the output with atomics.
+// instance's power P.  BSDF derivatives are analytic (bsdf_grad.cuh).
+// Visibility discontinuities are not differentiated.  Gradients are summed
+// across each warp in registers, then per block in shared memory, then added
+// to the output with one global atomic per parameter per block.
 // No counterpart in the reference.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
-#include "dual.cuh"
+#include "bsdf_grad.cuh"
 #include "path_trace.cuh"
 #include "scene.h"
 #include "zgl_internal.h"
@@ -103,113 +104,66 @@ __global__ void diff_reduce_kernel(const float* __restrict__ samples, int64_t np
     image[3 * p + 2] = b / inv;
 }
 
-__device__ __forceinline__ void add_mat_grad(float* sg, int matId, const v3& delta, const v3& scale, const BsdfGrad& bg) {
-    // sum_c delta_c * scale_c * df_c / f_c, channels with f_c == 0 carry no radiance
-    v3 w;
-    w.x = bg.f.x != 0.0f ? delta.x * scale.x / bg.f.x : 0.0f;
-    w.y = bg.f.y != 0.0f ? delta.y * scale.y / bg.f.y : 0.0f;
-    w.z = bg.f.z != 0.0f ? delta.z * scale.z / bg.f.z : 0.0f;
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
-    for (int i = 0; i < kDiffMatParams; i++) {
-        float gsum = w.x * bg.df[i].x + w.y * bg.df[i].y + w.z * bg.df[i].z;
-        if (gsum != 0.0f) atomicAdd(&sg[kDiffMatParams * matId + i], gsum);
-    }
-}
-__device__ __forceinline__ void add_power_grad(float* sg, const DiffInfo& di, const float* params, int lightId,
-                                               const v3& delta, const v3& C) {
-    int inst = __ldg(&di.lightInst[lightId]);
-    int base = kDiffMatParams * di.nmat + 3 * inst;
-    float P[3] = {__ldg(&params[base]), __ldg(&params[base + 1]), __ldg(&params[base + 2])};
-    float c[3] = {C.x, C.y, C.z}, d[3] = {delta.x, delta.y, delta.z};
-    for (int k = 0; k < 3; k++)
-        if (P[k] != 0.0f && c[k] != 0.0f) atomicAdd(&sg[base + k], d[k] * c[k] / P[k]);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+    return v;
 }
 
-// Replay of pathIntegTrace with adjoint accounting (same sample consumption).
-__device__ void replay_adjoint(const DeviceScene& sc, const PathParams& pp, const DiffInfo& di, const float* params,
-                               Ray ray, Sampler& g, v3 Lrem, v3 delta, float* sg) {
-    float primDist;
-    int id = bvhHit(sc, ray, primDist);
-    v3 pos = rayPoint(ray, primDist);
-    if (id == -1) return;  // environment: no differentiable parameter
-    if (id - sc.objPrimCount >= 0) {
-        int lightId = id - sc.objPrimCount;
-        v3 C = lightLe(sc, lightId, pos, -ray.dir);
-        add_power_grad(sg, di, params, lightId, delta, C);
-        return;
-    }
-    v3 wo = -ray.dir;
-    v3 throughput = mk3(1.0f);
-    for (int bounce = 1; bounce <= pp.maxDepth; bounce++) {
-        TriShade tri = loadTri(sc, id);
-        Surface surf = surfaceInfo(tri, pos);
-        int matId = tri.matTex & 0x0000ffff;
-        uint32_t matType = loadMaterialType(sc, matId);
-        if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
-            surf.ns = -surf.ns;
-            surf.ng = -surf.ng;
+// Adds vals[0..K) of every lane to sg[key + j], summing lanes that share a key
+// in registers first: one shared-memory atomic per (distinct key, j) per warp.
+// key < 0: the lane adds nothing.  All 32 lanes must call it together.
+template <int K>
+__device__ __forceinline__ void warp_flush(float* sg, int key, const float* vals) {
+    unsigned pending = __ballot_sync(kFullMask, key >= 0);
+    unsigned lane;  // the hardware lane id (the block is two-dimensional)
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const int k = __shfl_sync(kFullMask, key, leader);
+        const bool mine = key == k;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            float v = warp_sum(mine ? vals[j] : 0.0f);
+            if (lane == (unsigned)leader && v != 0.0f) atomicAdd(&sg[k + j], v);
         }
-        BSDFParam mp = loadMaterial(sc, matType, matId);
-        if (pp.sampleLight) {
-            float ud = sample1D(g);
-            float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
-            // the light pick of sampleLightAndEnv, kept to know which light is sampled
-            float pdfSampleLight = 0.0f;
-            if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
-            bool sampleLight = ud < pdfSampleLight;
-            int lid = sampleLight ? lightSampleOne(sc, mk2(u0, u1)) : -1;
-            LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
-            if (ls.pdf > 0.0f) {
-                v3 f = materialBSDF(matType, mp, wo, ls.wi, surf.ns);
-                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
-                float weight = biHeuristic(ls.pdf, fpdf);
-                v3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
-                BsdfGrad bg = bsdfGrad(sc, matType, matId, wo, ls.wi, surf.ns);
-                add_mat_grad(sg, matId, delta, C, bg);
-                if (lid >= 0) add_power_grad(sg, di, params, lid, delta, C);
-                Lrem = Lrem - C;
-            }
-        }
-        float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
-        v3 wi = bs.wi;
-        float bsdfPdf = bs.pdf;
-        bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
-        if (bsdfPdf < 1e-8f) break;
-        // every later contribution carries this vertex's sampled BSDF value
-        {
-            BsdfGrad bg = bsdfGrad(sc, matType, matId, wo, wi, surf.ns);
-            add_mat_grad(sg, matId, delta, Lrem, bg);
-        }
-        throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
-        ray = rayOffseted(pos, wi);
-        float dist;
-        int nextId = bvhHit(sc, ray, dist);
-        int lightId = nextId - sc.objPrimCount;
-        v3 nextPos = rayPoint(ray, dist);
-        if (nextId == -1) break;  // environment emission: no parameter
-        if (lightId >= 0) {
-            v3 radiance = lightLe(sc, lightId, nextPos, -wi);
-            float weight = 1.0f;
-            if (pp.sampleLight && !deltaBsdf) {
-                float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, pp, lightId);
-                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
-            }
-            v3 C = radiance * throughput * weight;
-            add_power_grad(sg, di, params, lightId, delta, C);
-            break;
-        }
-        if (pp.rr && bounce >= pp.rrStart) {
-            float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
-            if (sample1D(g) >= continueProb) break;
-            throughput = throughput / continueProb;
-        }
-        id = nextId;
-        pos = nextPos;
-        wo = -wi;
+        pending &= ~__ballot_sync(kFullMask, mine);
     }
 }
 
+// sum_c w_c df[i]_c with w_c = delta_c scale_c / f_c (channels with f_c == 0
+// carry no radiance), added to acc[i].
+__device__ __forceinline__ float grad_weight(float delta, float scale, float f) {
+    float w = f > 1e-30f ? delta * scale / f : 0.0f;
+    return isfinite(w) ? w : 0.0f;
+}
+__device__ __forceinline__ void mat_grad(float* acc, const v3& delta, const v3& scale, const BsdfGrad& bg) {
+    const v3 w = mk3(grad_weight(delta.x, scale.x, bg.f.x), grad_weight(delta.y, scale.y, bg.f.y),
+                     grad_weight(delta.z, scale.z, bg.f.z));
+#pragma unroll
+    for (int i = 0; i < kDiffMatParams; i++) acc[i] += w.x * bg.df[i].x + w.y * bg.df[i].y + w.z * bg.df[i].z;
+}
+
+// delta_c C_c / P_c for the power P of light triangle lightId's instance;
+// returns the slot of the instance's first channel.
+__device__ __forceinline__ int power_grad(const DiffInfo& di, const float* params, int lightId, const v3& delta,
+                                          const v3& C, float* out) {
+    const int inst = __ldg(&di.lightInst[lightId]);
+    const int base = kDiffMatParams * di.nmat + 3 * inst;
+    const float P[3] = {__ldg(&params[base]), __ldg(&params[base + 1]), __ldg(&params[base + 2])};
+    const float c[3] = {C.x, C.y, C.z}, d[3] = {delta.x, delta.y, delta.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) out[k] = (P[k] != 0.0f && c[k] != 0.0f) ? d[k] * c[k] / P[k] : 0.0f;
+    return base;
+}
+
+// Backward: one thread per (pixel, sample), blockIdx.y = sample.  The replay
+// of pathIntegTrace (path_integ_naive.glsl:35-143) runs in warp lockstep, one
+// bounce per iteration of a warp-uniform loop, so that each iteration's
+// gradients (one material, up to two light instances per lane) are reduced
+// across the warp before the shared-memory atomics.
 __global__ void __launch_bounds__(kTileX* kTileY)
 diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
                      int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
@@ -223,31 +177,134 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
     const int tile = blockIdx.x;
     const int px = (tile % tilesX) * kTileX + threadIdx.x;
     const int py = (tile / tilesX) * kTileY + threadIdx.y;
-    if (px < sc.filmW && py < sc.filmH) {
+
+    bool alive = px < sc.filmW && py < sc.filmH;
+    v3 Lrem = mk3(0.0f), Ltot = mk3(0.0f), delta = mk3(0.0f);
+    size_t pix = 0;
+    if (alive) {
         const size_t npix = (size_t)sc.filmW * sc.filmH;
-        const size_t pix = (size_t)py * sc.filmW + px;
+        pix = (size_t)py * sc.filmW + px;
         const float* L = samples + 3 * ((size_t)s * npix + pix);
-        v3 Ltot = mk3(L[0], L[1], L[2]);
-        // image = sum / spp, NaN samples excluded from the sum
-        if (!hasNan(Ltot)) {
-            const float inv = 1.0f / (float)spp;
-            v3 delta = mk3(dimage[3 * pix] * inv, dimage[3 * pix + 1] * inv, dimage[3 * pix + 2] * inv);
-            if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
-                const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
-                Sampler g;
-                g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
-                g.sampleSeed = seed.x * seed.y;
-                g.sampleOffset = off;
-                g.dim = 0;
-                g.mode = sc.sampler;
-                g.rowCache = row;
-                g.mats = sc.sobol;
-                v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
-                float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
-                Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-                replay_adjoint(sc, pp, di, params, ray, g, Ltot, delta, sg);
-            }
+        Lrem = mk3(L[0], L[1], L[2]);
+        Ltot = Lrem;
+        const float inv = 1.0f / (float)spp;
+        delta = mk3(dimage[3 * pix] * inv, dimage[3 * pix + 1] * inv, dimage[3 * pix + 2] * inv);
+        // NaN samples are left out of the image; zero adjoints need no replay
+        alive = !hasNan(Lrem) && (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f);
+    }
+    Sampler g;
+    Ray ray;
+    int id = -1;
+    v3 pos = mk3(0.0f), wo = mk3(0.0f), throughput = mk3(1.0f);
+    float pw[3];
+    int pkey = -1;
+    if (alive) {
+        const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+        g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
+        g.sampleSeed = seed.x * seed.y;
+        g.sampleOffset = off;
+        g.dim = 0;
+        g.mode = sc.sampler;
+        g.rowCache = row;
+        g.mats = sc.sobol;
+        v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+        ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+        float primDist;
+        id = bvhHit(sc, ray, primDist);
+        pos = rayPoint(ray, primDist);
+        wo = -ray.dir;
+        if (id == -1) {
+            alive = false;  // environment: no differentiable parameter
+        } else if (id - sc.objPrimCount >= 0) {
+            const int lightId = id - sc.objPrimCount;
+            pkey = power_grad(di, params, lightId, delta, lightLe(sc, lightId, pos, -ray.dir), pw);
+            alive = false;
         }
+    }
+    warp_flush<3>(sg, pkey, pw);
+
+    int bounce = 1;
+    while (__any_sync(kFullMask, alive)) {
+        int mkey = -1, nkey = -1, hkey = -1;
+        float mg[kDiffMatParams], npw[3], hpw[3];
+#pragma unroll
+        for (int i = 0; i < kDiffMatParams; i++) mg[i] = 0.0f;
+        if (alive) {
+            TriShade tri = loadTri(sc, id);
+            Surface surf = surfaceInfo(tri, pos);
+            const int matId = tri.matTex & 0x0000ffff;
+            const uint32_t matType = loadMaterialType(sc, matId);
+            if (matType != kDielectric && matType != kThinDielectric && dot(surf.ns, wo) < 0.0f) {
+                surf.ns = -surf.ns;
+                surf.ng = -surf.ng;
+            }
+            const BSDFParam mp = loadMaterial(sc, matType, matId);
+            mkey = kDiffMatParams * matId;
+            if (pp.sampleLight) {
+                const float ud = sample1D(g);
+                const float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+                float pdfSampleLight = 0.0f;  // the light pick of sampleLightAndEnv
+                if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
+                const int lid = ud < pdfSampleLight ? lightSampleOne(sc, mk2(u0, u1)) : -1;
+                const LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
+                if (ls.pdf > 0.0f) {
+                    const BsdfGrad bg = bsdfGrad(matType, mp, wo, ls.wi, surf.ns);
+                    const float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                    const float weight = biHeuristic(ls.pdf, fpdf);
+                    const v3 C = bg.f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+                    mat_grad(mg, delta, C, bg);
+                    if (lid >= 0) nkey = power_grad(di, params, lid, delta, C, npw);
+                    // what is left below the rounding of the total is no radiance
+                    Lrem = Lrem - C;
+                    Lrem.x = Lrem.x > 1e-6f * Ltot.x ? Lrem.x : 0.0f;
+                    Lrem.y = Lrem.y > 1e-6f * Ltot.y ? Lrem.y : 0.0f;
+                    Lrem.z = Lrem.z > 1e-6f * Ltot.z ? Lrem.z : 0.0f;
+                }
+            }
+            const float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
+            const BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+            const v3 wi = bs.wi;
+            const float bsdfPdf = bs.pdf;
+            const bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
+            if (bsdfPdf < 1e-8f) {
+                alive = false;
+            } else {
+                // every later contribution carries this vertex's sampled BSDF value
+                mat_grad(mg, delta, Lrem, bsdfGrad(matType, mp, wo, wi, surf.ns));
+                throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+                ray = rayOffseted(pos, wi);
+                float dist;
+                const int nextId = bvhHit(sc, ray, dist);
+                const int lightId = nextId - sc.objPrimCount;
+                const v3 nextPos = rayPoint(ray, dist);
+                if (nextId == -1) {
+                    alive = false;  // environment emission: no parameter
+                } else if (lightId >= 0) {
+                    const v3 radiance = lightLe(sc, lightId, nextPos, -wi);
+                    float weight = 1.0f;
+                    if (pp.sampleLight && !deltaBsdf) {
+                        const float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, pp, lightId);
+                        weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
+                    }
+                    hkey = power_grad(di, params, lightId, delta, radiance * throughput * weight, hpw);
+                    alive = false;
+                } else {
+                    if (pp.rr && bounce >= pp.rrStart) {
+                        const float continueProb = zmin(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+                        if (sample1D(g) >= continueProb) alive = false;
+                        throughput = throughput / continueProb;
+                    }
+                    id = nextId;
+                    pos = nextPos;
+                    wo = -wi;
+                }
+            }
+            if (++bounce > pp.maxDepth) alive = false;
+        }
+        warp_flush<kDiffMatParams>(sg, mkey, mg);
+        warp_flush<3>(sg, nkey, npw);
+        warp_flush<3>(sg, hkey, hpw);
     }
     __syncthreads();
     for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY)
