@@ -31,7 +31,7 @@ __device__ __forceinline__ float dSchlickGdk(float c, float k) {
     return -c * (1.0f - c) / (den * den);
 }
 
-__device__ __forceinline__ BsdfGrad principledGrad(v3 wo, v3 wi, v3 n, const BSDFParam& p) {
+static __device__ __noinline__ BsdfGrad principledGrad(v3 wo, v3 wi, v3 n, BSDFParam p) {
     BsdfGrad g;
     g.f = mk3(0.0f);
 #pragma unroll

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <vector>
 
+#define ZGL_INLINE_TRACE 1
 #include "scene.h"
 #include "shading.cuh"
 #include "zgl_internal.h"

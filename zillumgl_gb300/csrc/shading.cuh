@@ -231,7 +231,7 @@ __device__ __forceinline__ v3 principledDiffuse(v3 wo, v3 wi, v3 n, v3 baseColor
     v3 ss = baseColor * kPiInv * 1.25f * (fss * (1.0f / (cosWi + cosWo) - 0.5f) + mk3(0.5f));
     return mix3(baseDiffuse, ss, subsurface);
 }
-__device__ __forceinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :462-490
+static __device__ __noinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :462-490
     float alpha = sq(p.roughness);
     float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
     float lum = luminance(p.baseColor);
@@ -245,7 +245,7 @@ __device__ __forceinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, const BSDFParam
     res = res + mix3(mk3(1.0f), tint, p.sheenTint) * schlickW(hCosWi) * p.sheen * (dot(n, wi) < 0.0f ? 0.0f : 1.0f);
     return res;
 }
-__device__ __forceinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :492-514
+static __device__ __noinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :492-514
     float pdf = 0.0f;
     float alpha = sq(p.roughness);
     float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
@@ -370,16 +370,42 @@ struct Ray {
 __device__ __forceinline__ Ray rayOffseted(v3 o, v3 d) { return Ray{o + d * 1e-4f, d}; }
 __device__ __forceinline__ v3 rayPoint(const Ray& r, float t) { return r.ori + r.dir * t; }
 
-__device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float& dist) {
-    TraceRay tr = make_trace_ray(make_float3(r.ori.x, r.ori.y, r.ori.z), make_float3(r.dir.x, r.dir.y, r.dir.z));
-    dist = 1e8f;
+// The integrators call traversal from several places (camera ray, bounce,
+// light and environment shadow rays); each call goes to one out-of-line copy
+// of the closest-hit and any-hit loops (five ray-mode variants each), which
+// keeps the integrator kernels' instruction footprint small.  A translation
+// unit that defines ZGL_INLINE_TRACE before including this header inlines
+// them instead (the batched renderer, whose one call site per kind is hot).
+struct ClosestHit {
+    int id;
+    float dist;
+};
+#ifdef ZGL_INLINE_TRACE
+#define ZGL_TRACE_CALL __device__ __forceinline__
+#else
+#define ZGL_TRACE_CALL __device__ __noinline__
+#endif
+static ZGL_TRACE_CALL ClosestHit traceClosestCall(DeviceAccel a, float ox, float oy, float oz, float dx, float dy,
+                                                    float dz) {
+    TraceRay tr = make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz));
+    float dist = 1e8f;
     int v = 0, t = 0;
-    return traverse<false, false>(sc.accel, tr, dist, v, t);
+    int id = traverse<false, false>(a, tr, dist, v, t);
+    return ClosestHit{id, dist};
+}
+static ZGL_TRACE_CALL bool traceAnyCall(DeviceAccel a, float ox, float oy, float oz, float dx, float dy, float dz,
+                                          float dist) {
+    TraceRay tr = make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz));
+    int v = 0, t = 0;
+    return traverse<true, false>(a, tr, dist, v, t) != 0;
+}
+__device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float& dist) {
+    ClosestHit h = traceClosestCall(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z);
+    dist = h.dist;
+    return h.id;
 }
 __device__ __forceinline__ bool bvhTest(const DeviceScene& sc, const Ray& r, float dist) {
-    TraceRay tr = make_trace_ray(make_float3(r.ori.x, r.ori.y, r.ori.z), make_float3(r.dir.x, r.dir.y, r.dir.z));
-    int v = 0, t = 0;
-    return traverse<true, false>(sc.accel, tr, dist, v, t) != 0;
+    return traceAnyCall(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z, dist);
 }
 __device__ __forceinline__ bool visible(const DeviceScene& sc, v3 x, v3 y) {  // intersection.glsl:429-433
     float dist = distance(x, y) - 2e-5f;
