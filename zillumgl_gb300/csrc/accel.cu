@@ -79,14 +79,18 @@ trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 // ---------------------------------------------------------------------------
-// Persistent traversal: each warp keeps all 32 lanes busy by refilling a lane
-// with the next ray as soon as its traversal ends.  Idle lanes are counted
-// with __ballot_sync/__popc, one lane grabs that many ray indices with a
-// single atomicAdd on the work counter, and each idle lane takes its rank.
-// Every ray is still traversed by one lane in exactly the reference order, so
-// results are identical to the one-thread-per-ray kernels.
+// Persistent traversal: each warp keeps its lanes busy by refilling a lane
+// with the next ray once its traversal ends.  Idle lanes are counted with
+// __ballot_sync/__popc; once at least kRefillIdle lanes (or all) are idle,
+// one lane grabs that many ray indices with a single atomicAdd on the work
+// counter and each idle lane takes its rank.  The common general ray mode
+// runs a specialised box test; the rare axis-dominant and near-zero modes use
+// the generic one.  Every ray is still traversed by one lane in exactly the
+// reference order, so results are identical to the one-thread-per-ray
+// kernels.
 // ---------------------------------------------------------------------------
 constexpr int kPersistBlock = 128;
+constexpr int kRefillIdle = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
 template <bool ANY>
@@ -107,13 +111,13 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
     int k = 0, closest = -1;
     for (;;) {
         const unsigned idle = __ballot_sync(kFull, !active);
-        if (idle != 0u && !exhausted) {
+        const int nidle = __popc(idle);
+        if (!exhausted && (nidle >= kRefillIdle || nidle == 32)) {
             const int leader = __ffs(idle) - 1;
-            const unsigned cnt = __popc(idle);
             unsigned long long b = 0;
-            if (lane == leader) b = atomicAdd(counter, (unsigned long long)cnt);
+            if (lane == leader) b = atomicAdd(counter, (unsigned long long)nidle);
             b = __shfl_sync(kFull, b, leader);
-            if (b + cnt >= (unsigned long long)n) exhausted = true;
+            if (b + nidle >= (unsigned long long)n) exhausted = true;
             if (!active) {
                 const unsigned long long idx = b + __popc(idle & lt);
                 if (idx < (unsigned long long)n) {
@@ -127,12 +131,16 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
                 }
             }
         }
-        if (__ballot_sync(kFull, active) == 0u) break;
+        if (__ballot_sync(kFull, active) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
         if (active) {
             const float4 lo = __ldg(base + 2 * (size_t)k);
             const float4 hi = __ldg(base + 2 * (size_t)k + 1);
             float tmin;
-            const bool h = box_hit(lo, hi, r, tmin) && !(tmin > dist);
+            const bool bh = r.mode == 3 ? box_hit_m<3>(lo, hi, r, tmin) : box_hit(lo, hi, r, tmin);
+            const bool h = bh && !(tmin > dist);
             const int prim = __float_as_int(lo.w);
             int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
             if (h && prim >= 0) {
