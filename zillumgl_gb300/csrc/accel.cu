@@ -165,16 +165,14 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
     }
 }
 
+// SMs x resident blocks of `kernel` on the current device.
 int persistent_grid(const void* kernel) {
-    static int cached = 0;
-    if (cached) return cached;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistBlock, 0);
     if (per_sm < 1) per_sm = 1;
-    cached = sms * per_sm;
-    return cached;
+    return sms * per_sm;
 }
 
 }  // namespace
