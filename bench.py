@@ -58,6 +58,8 @@ def parse_args():
     ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
     ap.add_argument("--diff-size", type=int, default=512, help="film side of the differentiable workload")
     ap.add_argument("--diff-spp", type=int, default=32, help="samples per pixel of the differentiable workload")
+    ap.add_argument("--batch-requests", type=int, default=64, help="requests of the batched workload")
+    ap.add_argument("--batch-no-autotune", action="store_true", help="batched workload with the default schedule")
     return ap.parse_args()
 
 
@@ -439,6 +441,23 @@ def run_render(args, stream, dev):
                     res[kind]["light_paths_per_pass"] = 64 * 1536
             res[kind]["params"] = params
             integ.close()
+        if name == "cornell":
+            # the configuration's 16 samples per pixel as one multi-pass launch
+            integ = PathIntegrator(scene, **runs[0][2])
+            integ.render_passes(16, stream)  # warm-up (allocates the pass buffer)
+            integ.reset()
+            stream.synchronize()
+            e0.record(stream)
+            for _ in range(args.render_passes):
+                integ.reset()
+                integ.render_passes(16, stream)
+            e1.record(stream)
+            stream.synchronize()
+            ms16 = e0.elapsed_time(e1) / args.render_passes
+            res["path_16spp"] = {"ms_per_render": round(ms16, 3), "samples_per_s": round(W * H * 16 / (ms16 * 1e-3), 1),
+                                 "note": "16 passes in one launch (zgl_integrator_render_passes), frame identical "
+                                         "to 16 single passes"}
+            integ.close()
         # end to end through the C ABI: one pass + the frame read back to pinned host memory
         integ = PathIntegrator(scene, **runs[0][2])
         host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
@@ -470,7 +489,7 @@ def run_batch(args, stream, dev):
     from zillumgl_gb300.synthetic import batch_requests
 
     t0 = time.time()
-    reqs = batch_requests(seed=3, n=64)
+    reqs = batch_requests(seed=3, n=args.batch_requests)
     scenes, frames, total = [], [], 0
     for data, spp, params in reqs:
         scenes.append(Scene(data))
@@ -495,10 +514,25 @@ def run_batch(args, stream, dev):
     stream.synchronize()
     plain_ms = e0.elapsed_time(e1)
     launches_plain = sum(spp for _, spp, _ in reqs)
+    # plain, one multi-pass launch per request (zgl_integrator_render_passes)
+    multi = [PathIntegrator(sc, **params) for sc, (_, _, params) in zip(scenes, reqs)]
+    for it, (_, spp, _) in zip(multi, reqs):
+        it.render_passes(spp, stream)  # warm-up: allocates each pass buffer
+        it.reset()
+    stream.synchronize()
+    e0.record(stream)
+    for it, (_, spp, _) in zip(multi, reqs):
+        it.render_passes(spp, stream)
+    e1.record(stream)
+    stream.synchronize()
+    multi_ms = e0.elapsed_time(e1)
+    for it in multi:
+        it.close()
+    del multi
     # batched
     batch = BatchRenderer([(sc, spp, params, fr) for sc, (_, spp, params), fr in zip(scenes, reqs, frames)])
     t1 = time.time()
-    tuned = batch.autotune(stream)
+    tuned = batch.config() if args.batch_no_autotune else batch.autotune(stream)
     tune_s = time.time() - t1
     batch.render(stream)  # captures the graph
     stream.synchronize()
@@ -520,6 +554,9 @@ def run_batch(args, stream, dev):
     return {"requests": len(reqs), "samples": total,
             "plain": {"ms": round(plain_ms, 2), "samples_per_s": round(total / (plain_ms * 1e-3), 1),
                       "launches": launches_plain},
+            "plain_one_launch_per_request": {"ms": round(multi_ms, 2),
+                                             "samples_per_s": round(total / (multi_ms * 1e-3), 1),
+                                             "launches": 2 * len(reqs)},
             "batched": {"ms": round(batch_ms, 2), "samples_per_s": round(total / (batch_ms * 1e-3), 1),
                         "config": tuned, "autotune_s": round(tune_s, 2)},
             "speedup": round(plain_ms / batch_ms, 3), "frames_bit_identical_checked": f"{same}/4"}

@@ -263,6 +263,15 @@ zgl_status zgl_integrator_render_pass(zgl_integrator* integ, void* stream);
 
 /* Integrator::reset (NaivePath.cpp:107-115): the next pass restarts the
  * progressive sum at sample 0. */
+/* `passes` consecutive calls of zgl_integrator_render_pass in one go: the
+ * frame, sample count and counters end exactly as after those calls.  The
+ * path tracer renders all of them in one launch (per-pass radiance in a
+ * device scratch buffer of filmW*filmH*3*passes floats kept by the
+ * integrator, then added to the frame in pass order), which fills the GPU at
+ * small film sizes; the light and triple integrators run one pass at a time.
+ * No counterpart in the reference (one dispatch per pass). */
+zgl_status zgl_integrator_render_passes(zgl_integrator* integ, int32_t passes, void* stream);
+
 zgl_status zgl_integrator_reset(zgl_integrator* integ);
 
 /* Integrator::getFrame: the frame holds the running SUM of samples, RGBA
@@ -297,15 +306,23 @@ typedef struct zgl_render_request {
 } zgl_render_request;
 
 /* Schedule of the batched renderer; 0 picks the default (or, after
- * zgl_batch_autotune, the tuned value).  block_size: 64, 128 or 256 threads;
- * queue_capacity: work items a warp claims per atomic fetch;
- * regen_threshold: idle lanes a warp waits for before refilling them (1-32).
- * The CUDA graph holds one persistent launch per sample index (per group of
- * up to 64 requests that still need that sample). */
+ * zgl_batch_autotune, the tuned value).  schedule: ZGL_BATCH_FLAT (one grid of
+ * 16x8 pixel tiles over every sample of every request, straight-line path
+ * code per thread; the default) or ZGL_BATCH_PERSISTENT (persistent warps
+ * with per-bounce path state and path regeneration).  For the persistent
+ * schedule: block_size 64, 128 or 256 threads; queue_capacity: work items a
+ * warp claims per atomic fetch; regen_threshold: idle lanes a warp waits for
+ * before refilling them (1-32).  Either schedule renders every sample of a
+ * group of up to 64 requests in one launch (chunks of sample indices when the
+ * per-sample scratch would exceed scratch_mib), followed by the in-order frame
+ * updates; the CUDA graph holds these launches. */
+enum { ZGL_BATCH_DEFAULT = 0, ZGL_BATCH_FLAT = 1, ZGL_BATCH_PERSISTENT = 2 };
 typedef struct zgl_batch_config {
     int32_t block_size;
     int32_t queue_capacity;
     int32_t regen_threshold;
+    int32_t schedule;
+    int32_t scratch_mib;  /* per-sample scratch budget in MiB (0 = 4096); fixed at zgl_batch_create */
 } zgl_batch_config;
 
 typedef struct zgl_batch zgl_batch;
@@ -322,9 +339,10 @@ zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const
  * and later work on `stream` waits for it. */
 zgl_status zgl_batch_render(zgl_batch* batch, void* stream);
 
-/* Times every combination of block size, queue capacity and regeneration
- * threshold on the first samples of the batch, keeps the fastest for later
- * renders and returns it in `chosen` (may be NULL).  Overwrites the frames. */
+/* Times the flat schedule and every combination of block size, queue
+ * capacity and regeneration threshold of the persistent one on the first
+ * samples of the batch, keeps the fastest for later renders and returns it
+ * in `chosen` (may be NULL).  Overwrites the frames. */
 zgl_status zgl_batch_autotune(zgl_batch* batch, void* stream, zgl_batch_config* chosen);
 
 zgl_status zgl_batch_set_config(zgl_batch* batch, const zgl_batch_config* config);

@@ -68,11 +68,18 @@ def _check(reqs, refs):
         assert bad == 0, f"request {i}: {bad} pixels differ from the plain integrator"
 
 
+FLAT, PERSISTENT = 1, 2
+
+
 @pytest.mark.parametrize("cfg", [
     dict(),
-    dict(block_size=64, queue_capacity=8, regen_threshold=1),
-    dict(block_size=256, queue_capacity=128, regen_threshold=32),
-    dict(block_size=128, queue_capacity=1, regen_threshold=8),
+    dict(schedule=FLAT),
+    dict(schedule=PERSISTENT),
+    dict(schedule=PERSISTENT, block_size=64, queue_capacity=8, regen_threshold=1),
+    dict(schedule=PERSISTENT, block_size=256, queue_capacity=128, regen_threshold=32),
+    dict(schedule=PERSISTENT, block_size=128, queue_capacity=1, regen_threshold=8),
+    dict(schedule=FLAT, scratch_mib=1),        # chunks of a few sample indices
+    dict(schedule=PERSISTENT, scratch_mib=1),
 ])
 def test_batch_equals_plain_integrator(batch_setup, cfg):
     reqs, refs = batch_setup
@@ -89,8 +96,31 @@ def test_autotune_then_render(batch_setup):
     reqs, refs = batch_setup
     b = BatchRenderer(reqs)
     chosen = b.autotune()
+    assert chosen["schedule"] in (FLAT, PERSISTENT)
     assert chosen["block_size"] in (64, 128, 256)
-    assert b.config()["block_size"] == chosen["block_size"]
+    assert b.config() == chosen
     b.render()
     _check(reqs, refs)
     b.close()
+
+
+@pytest.mark.parametrize("schedule", [FLAT, PERSISTENT])
+def test_batch_in_sample_chunks(zgl_lib, cuda, schedule):
+    """A 1 MiB scratch budget forces one sample index per launch for a 256^2
+    request; frames still equal the plain integrator's bit for bit."""
+    import torch
+
+    specs = [(cornell_scene(seed=31, width=256, height=256), 6, dict(max_depth=4)),
+             (cornell_scene(seed=32, width=24, height=16), 3, dict(max_depth=5))]
+    reqs = []
+    for data, spp, params in specs:
+        sc = Scene(data)
+        W, H = data.film
+        reqs.append((sc, spp, params, torch.zeros((H, W, 4), dtype=torch.float32, device=cuda)))
+    refs = [_plain(sc, spp, params) for sc, spp, params, _ in reqs]
+    b = BatchRenderer(reqs, schedule=schedule, scratch_mib=1)
+    b.render()
+    _check(reqs, refs)
+    b.close()
+    for sc, *_ in reqs:
+        sc.close()

@@ -130,3 +130,33 @@ def test_xml_loaded_scene_renders_like_the_oracle(zgl_lib, cuda, tmp_path):
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
     integ.close()
     sc.close()
+
+
+def test_render_passes_equals_consecutive_passes(zgl_lib, cuda):
+    """render_passes(n) in one launch == n render_one_pass calls, bit for bit,
+    including a start after earlier passes and a finite sample budget."""
+    d = cornell_scene(seed=12, width=40, height=24)
+    sc = Scene(d)
+    params = dict(max_depth=5, finite_sample=1, max_sample=9)
+    a = PathIntegrator(sc, **params)
+    b = PathIntegrator(sc, **params)
+    for _ in range(3):
+        a.render_one_pass()
+    b.render_passes(3)
+    fa, sa = a.get_frame()
+    fb, sb = b.get_frame()
+    assert sa == sb == 3 and np.array_equal(fa.view(np.uint32), fb.view(np.uint32))
+    for _ in range(12):  # runs into the budget of 10 samples
+        a.render_one_pass()
+    b.render_passes(12)
+    fa, sa = a.get_frame()
+    fb, sb = b.get_frame()
+    assert sa == sb == 10
+    assert np.array_equal(fa.view(np.uint32), fb.view(np.uint32))
+    orc = oracle.OracleScene(d, sc.export("sobol"), dict(max_depth=5))
+    W, H = d.film
+    ref = orc.render_pt(np.arange(W * H), 10, spp0=0, fc0=1).reshape(H, W, 3)
+    assert np.array_equal(fb[..., :3].view(np.uint32), ref.view(np.uint32))
+    a.close()
+    b.close()
+    sc.close()

@@ -66,6 +66,7 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_integrator_params_default": (C.c_int32, [C.c_void_p]),
     "zgl_integrator_create": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "zgl_integrator_render_pass": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_integrator_render_passes": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p]),
     "zgl_integrator_reset": (C.c_int32, [C.c_void_p]),
     "zgl_integrator_frame": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_integrator_result_scale": (C.c_int32, [C.c_void_p, C.c_void_p]),

@@ -5,10 +5,12 @@
 // :145-174).  Pixels are mapped to 16x8 tiles so that a warp's camera rays are
 // neighbours.  The 256 Sobol values of the pass's sample row are computed
 // once per block into shared memory.
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
 
+#include "batch_flat.h"
 #include "path_trace.cuh"
 #include "scene.h"
 #include "shading.cuh"
@@ -25,6 +27,8 @@ struct zgl_integrator {
     float* d_film = nullptr;    // light / triple: RGB sum, filmW * filmH * 3 (the r32f 3W x H film)
     float samplePerPixel = 0.0f;
     int32_t blocks = 0, loops = 1;
+    float* d_passes = nullptr;  // path tracer, several passes per launch: per-pass radiance
+    size_t passesCap = 0;       // floats allocated in d_passes
 };
 
 namespace zgl {
@@ -62,6 +66,102 @@ path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uin
         v3 r = last + result;
         frame[pix] = make_float4(r.x, r.y, r.z, 1.0f);
     }
+}
+
+// Several consecutive passes in one launch: pass j = blockIdx.z renders
+// sample c0 + j with freeCounter f0 + j, exactly as path_kernel would, into
+// out[j][pix] (NaN samples kept, the accumulation drops them).
+__global__ void __launch_bounds__(kTileX* kTileY)
+path_passes_kernel(DeviceScene sc, PathParams pp, int32_t c0, int32_t f0, float* __restrict__ out) {
+    __shared__ uint32_t row[256];
+    const int32_t j = blockIdx.z;
+    const uint32_t off = sample_offset(c0 + j);
+    load_sobol_row(sc, off, row);
+    const int px = blockIdx.x * kTileX + threadIdx.x;
+    const int py = blockIdx.y * kTileY + threadIdx.y;
+    if (px >= sc.filmW || py >= sc.filmH) return;
+    const size_t npix = (size_t)sc.filmW * sc.filmH;
+    const size_t pix = (size_t)py * sc.filmW + px;
+    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+    Sampler g;
+    g.randSeed = seed.x * (uint32_t)(f0 + j) + seed.y;
+    g.sampleSeed = seed.x * seed.y;
+    g.sampleOffset = off;
+    g.dim = 0;
+    g.mode = sc.sampler;
+    g.rowCache = row;
+    g.mats = sc.sobol;
+    v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    v3 r = pathTrace(sc, pp, ray, g);
+    float* o = out + 3 * ((size_t)j * npix + pix);
+    o[0] = r.x;
+    o[1] = r.y;
+    o[2] = r.z;
+}
+
+// The frame updates of those passes in pass order, as consecutive
+// path_kernel launches make them (main(), path_integ_naive.glsl:166-173):
+// a pass with sample index 0 starts from zero, a NaN sample leaves the pixel
+// as it was.
+__global__ void accumulate_passes_kernel(const float* __restrict__ in, int64_t npix, int32_t c0, int32_t n,
+                                         float4* __restrict__ frame) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float4 f = frame[p];
+    v3 acc = mk3(f.x, f.y, f.z);
+    bool written = false;
+    for (int j = 0; j < n; j++) {
+        const float* x = in + 3 * ((size_t)j * npix + p);
+        const v3 r = mk3(x[0], x[1], x[2]);
+        const v3 last = (c0 + j != 0) ? acc : mk3(0.0f);
+        if (!hasNan(r)) {
+            acc = last + r;
+            written = true;
+        }
+    }
+    if (written) frame[p] = make_float4(acc.x, acc.y, acc.z, 1.0f);
+}
+
+// Flat schedule of the batched renderer (batch_flat.h): block b is a 16x8
+// tile of one sample of one request.
+__global__ void __launch_bounds__(kTileX* kTileY) batch_flat_kernel(const __grid_constant__ FlatLaunch L) {
+    const int64_t blk = blockIdx.x;
+    int lo = 0, hi = L.nreq - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (L.req[mid].blockBase <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    const FlatRequest& rq = L.req[lo];
+    const int64_t local = blk - rq.blockBase;
+    const int64_t perSample = (int64_t)rq.tilesX * rq.tilesY;
+    const int j = L.j0 + (int)(local / perSample);
+    const int64_t tile = local % perSample;
+    const DeviceScene& sc = rq.sc;
+    const int px = (int)(tile % rq.tilesX) * kTileX + threadIdx.x;
+    const int py = (int)(tile / rq.tilesX) * kTileY + threadIdx.y;
+    if (px >= sc.filmW || py >= sc.filmH) return;
+    const size_t pix = (size_t)py * sc.filmW + px;
+    const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+    Sampler g;
+    g.randSeed = seed.x * (uint32_t)(j + 1) + seed.y;
+    g.sampleSeed = seed.x * seed.y;
+    g.sampleOffset = sample_offset(j);
+    g.dim = 0;
+    g.mode = sc.sampler;
+    g.rowCache = L.rows + 256 * (size_t)j;
+    g.mats = L.mats;
+    const PathParams pp{rq.maxDepth, rq.rr, rq.rrStart, rq.sampleLight, rq.uniformSel, rq.portion};
+    v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+    Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    v3 r = pathTrace(sc, pp, ray, g);
+    float* o = rq.scratch + 3 * ((size_t)(j - L.j0) * ((size_t)sc.filmW * sc.filmH) + pix);
+    o[0] = r.x;
+    o[1] = r.y;
+    o[2] = r.z;
 }
 
 // Film of the light-tracing passes, float[H][W][3].  int(uv * size) == size
@@ -438,6 +538,26 @@ cudaError_t launch_path_pass(const zgl_scene* s, const zgl_integrator_params& p,
     return cudaGetLastError();
 }
 
+cudaError_t launch_path_passes(const zgl_scene* s, const zgl_integrator_params& p, int32_t c0, int32_t f0, int32_t n,
+                               float* scratch, float4* frame, cudaStream_t st) {
+    PathParams pp{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
+                  p.light_portion};
+    dim3 block(kTileX, kTileY);
+    dim3 grid((unsigned)((s->filmW + kTileX - 1) / kTileX), (unsigned)((s->filmH + kTileY - 1) / kTileY), (unsigned)n);
+    path_passes_kernel<<<grid, block, 0, st>>>(s->view(), pp, c0, f0, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t npix = (int64_t)s->filmW * s->filmH;
+    accumulate_passes_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(scratch, npix, c0, n, frame);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_flat(const FlatLaunch& L, cudaStream_t st) {
+    if (L.nblocks <= 0) return cudaSuccess;
+    batch_flat_kernel<<<(unsigned)L.nblocks, dim3(kTileX, kTileY), 0, st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_light_pass(const zgl_scene* s, const zgl_integrator_params& p, int32_t blocks, int32_t spp,
                               int32_t freeCounter, float* film, cudaStream_t st) {
     PathParams pp{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
@@ -587,6 +707,42 @@ zgl_status zgl_integrator_render_pass(zgl_integrator* it, void* stream) {
     ZGL_API_END
 }
 
+zgl_status zgl_integrator_render_passes(zgl_integrator* it, int32_t passes, void* stream) {
+    ZGL_API_BEGIN
+    if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_passes: NULL");
+    if (passes < 0 || passes > 4096) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_passes: %d passes", passes);
+    if (it->kind != ZGL_INTEGRATOR_PATH) {
+        // light and triple passes splat into one film: one launch per pass
+        for (int32_t k = 0; k < passes; k++) {
+            zgl_status st = zgl_integrator_render_pass(it, stream);
+            if (st != ZGL_OK) return st;
+        }
+        return ZGL_OK;
+    }
+    // passes that render before a finite sample budget stops the integrator;
+    // every call counts in freeCounter, as consecutive render_pass calls do
+    int32_t n = passes;
+    if (it->params.finite_sample) n = std::max(0, std::min(passes, it->params.max_sample + 1 - it->curSample));
+    const int32_t f0 = it->freeCounter + 1;
+    if (n > 0) {
+        const zgl_scene* sc = it->scene;
+        const size_t need = (size_t)3 * sc->filmW * sc->filmH * (size_t)n;
+        if (need > it->passesCap) {
+            if (it->d_passes) ZGL_CUDA(cudaFree(it->d_passes));
+            it->d_passes = nullptr;
+            it->passesCap = 0;
+            ZGL_CUDA(cudaMalloc(&it->d_passes, sizeof(float) * need));
+            it->passesCap = need;
+        }
+        ZGL_CUDA(launch_path_passes(sc, it->params, it->curSample, f0, n, it->d_passes, it->d_frame,
+                                    (cudaStream_t)stream));
+        it->curSample += n;
+    }
+    if (n < passes) it->finished = true;
+    it->freeCounter += passes;
+    ZGL_API_END
+}
+
 zgl_status zgl_integrator_reset(zgl_integrator* it) {
     ZGL_API_BEGIN
     if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_reset: NULL");
@@ -647,6 +803,7 @@ zgl_status zgl_integrator_destroy(zgl_integrator* it) {
     if (!it) return ZGL_OK;
     if (it->d_frame) cudaFree(it->d_frame);
     if (it->d_film) cudaFree(it->d_film);
+    if (it->d_passes) cudaFree(it->d_passes);
     delete it;
     ZGL_API_END
 }

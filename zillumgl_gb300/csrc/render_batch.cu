@@ -1,32 +1,34 @@
 // render_batch.cu — batched wavefront path tracing: many render requests
-// (each its own scene, film, samples per pixel and depth) rendered by
-// persistent launches, one per sample index, captured in one CUDA graph.
+// (each its own scene, film, samples per pixel and depth) rendered by one
+// persistent launch over every (request, sample, pixel), captured in a CUDA
+// graph with the frame updates.
 //
-// A launch renders sample s of every request that still needs it.  Its work
-// items are the pixels of those requests in 8x4 tiles, so a warp's lanes hold
-// neighbouring pixels of one sample.  Persistent warps claim ranges of
-// `queue_capacity` items with one atomicAdd on the launch's work counter and
-// hand them to idle lanes with __ballot_sync/__popc once at least
-// `regen_threshold` lanes are idle (or none is live).  Each lane runs its path
-// as an explicit state machine whose step is one bounce (closest-hit trace,
-// emission/MIS, Russian roulette, then next-event estimation and BSDF
-// sampling at the new vertex); a lane whose path ends takes the next pixel at
-// once (path regeneration).  Request descriptors travel in the kernel
-// parameter block (up to 64 per launch), the sample's Sobol row sits in
-// shared memory.
-//
-// The per-sample arithmetic, RNG streams and sample dimensions are those of
-// path_integ_naive.glsl (pathIntegTrace :35-143, main :145-174), launches run
-// in sample order and each pixel has one owner per launch, so a request's
-// frame is bit for bit the frame of the plain path integrator after `spp`
-// passes from a fresh start (freeCounter = sample + 1).  This batched schedule has no
-// counterpart in the reference; its nearest relatives are the queue
-// experiments pt_global_queue_*.glsl and pt_shared_queue.glsl.
+// Work items are the pixels of every sample of every request, in 8x4 tiles
+// per sample, so a warp's lanes hold neighbouring pixels of one sample.
+// Persistent warps claim ranges of `queue_capacity` items with one atomicAdd
+// on the launch's work counter and hand them to idle lanes with
+// __ballot_sync/__popc once at least `regen_threshold` lanes are idle (or none
+// is live).  Each lane runs its path as an explicit state machine whose step
+// is one bounce (closest-hit trace, emission/MIS, Russian roulette, then
+// next-event estimation and BSDF sampling at the new vertex); a lane whose
+// path ends takes the next item at once (path regeneration), whatever its
+// request or sample.  The Sobol rows of all sample indices sit in a small
+// device table.  Each sample's radiance goes to a per-request scratch array;
+// a second kernel then adds the samples to the frames in sample order
+// (path_integ_naive.glsl main(), :166-173), so a request's frame is bit for
+// bit the frame of the plain path integrator after `spp` passes from a fresh
+// start (sample j uses freeCounter j + 1).  When the scratch of all samples
+// would exceed a memory budget the samples are rendered in chunks of sample
+// indices.  Request descriptors travel in the kernel parameter block (up to
+// 64 per launch).  This schedule has no counterpart in the reference; its
+// nearest relatives are the queue experiments pt_global_queue_*.glsl and
+// pt_shared_queue.glsl.
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
 #define ZGL_INLINE_TRACE 1
+#include "batch_flat.h"
 #include "scene.h"
 #include "shading.cuh"
 #include "zgl_internal.h"
@@ -46,23 +48,27 @@ struct BatchRequest {
     BatchPathParams pp;
     int32_t spp;
     float4* frame;
+    float* scratch;    // per-sample radiance of the current chunk, [sample - j0][npix][3]
     int64_t itemBase;  // first work item of this request in its launch
     int32_t npix;
     int32_t tilesX;    // 8x4 pixel tiles per film row
+    int32_t perSample; // items per sample (whole tiles)
+    int32_t j1;        // samples [j0, j1) of this request in the launch
 };
 
 constexpr int kMaxReqPerLaunch = 64;
+constexpr size_t kScratchBudget = (size_t)4 << 30;  // default per-sample radiance of one launch chunk
 
 struct BatchLaunch {
     BatchRequest req[kMaxReqPerLaunch];
     int32_t nreq;
     int64_t nitems;
-    int32_t s;              // sample index of this launch
-    uint32_t sampleOffset;  // s * 256, wrapped (path_integ_naive.glsl:163-164)
+    int32_t j0;             // first sample index of this launch
     unsigned long long* counter;
     int32_t queueCap;
     int32_t regenThreshold;
     const uint32_t* mats;   // Sobol generator matrices
+    const uint32_t* rows;   // Sobol rows: 256 values per sample index
 };
 static_assert(sizeof(BatchLaunch) <= 32000, "kernel parameter block too large");
 
@@ -100,19 +106,19 @@ __device__ __forceinline__ uint32_t sample_offset_dev(int32_t spp) {
     return (uint32_t)off;
 }
 
-// Starts sample `s` of pixel (px, py): seeds and the camera ray (main(),
+// Starts sample `j` of pixel (px, py): seeds and the camera ray (main(),
 // path_integ_naive.glsl:145-166).
-__device__ __forceinline__ void start_sample(const BatchRequest& rq, const BatchLaunch& L, const uint32_t* row,
-                                             int px, int py, Sampler& g, PathState& st) {
+__device__ __forceinline__ void start_sample(const BatchRequest& rq, const BatchLaunch& L, int j, int px, int py,
+                                             Sampler& g, PathState& st) {
     const DeviceScene& sc = rq.sc;
     const uint2 seed = __ldg(&sc.pixelSeeds[(size_t)py * sc.filmW + px]);
-    const uint32_t freeCounter = (uint32_t)L.s + 1u;
+    const uint32_t freeCounter = (uint32_t)j + 1u;
     g.randSeed = seed.x * freeCounter + seed.y;
     g.sampleSeed = seed.x * seed.y;
-    g.sampleOffset = L.sampleOffset;
+    g.sampleOffset = sample_offset_dev(j);
     g.dim = 0;
     g.mode = sc.sampler;
-    g.rowCache = row;
+    g.rowCache = L.rows + 256 * (size_t)j;
     g.mats = L.mats;
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
@@ -223,16 +229,13 @@ __device__ __forceinline__ int find_request(const BatchLaunch& L, int64_t item) 
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ BatchLaunch L) {
-    __shared__ uint32_t row[256];
-    for (int i = threadIdx.x; i < 256; i += BLOCK) row[i] = sobol_value(L.mats, L.sampleOffset >> 8, (uint32_t)i);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     // warp-uniform: claimed but not yet handed-out work items [qnext, qend)
     int64_t qnext = 0, qend = 0;
     bool exhausted = false;
     bool live = false;
-    int rid = 0, px = 0, py = 0;
+    int rid = 0, px = 0, py = 0, js = 0;
     Sampler g;
     PathState st;
     for (;;) {
@@ -263,13 +266,16 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ Ba
                     rid = find_request(L, item);
                     const BatchRequest& rq = L.req[rid];
                     const int64_t local = item - rq.itemBase;
-                    const int64_t tile = local >> 5;
-                    const int w = (int)(local & 31);
+                    js = (int)(local / rq.perSample);
+                    const int64_t inSample = local - (int64_t)js * rq.perSample;
+                    js += L.j0;
+                    const int64_t tile = inSample >> 5;
+                    const int w = (int)(inSample & 31);
                     px = (int)(tile % rq.tilesX) * 8 + (w & 7);
                     py = (int)(tile / rq.tilesX) * 4 + (w >> 3);
                     if (px < rq.sc.filmW && py < rq.sc.filmH) {
                         live = true;
-                        start_sample(rq, L, row, px, py, g, st);
+                        start_sample(rq, L, js, px, py, g, st);
                     }
                 }
             }
@@ -288,21 +294,44 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ Ba
         if (live) {
             const BatchRequest& rq = L.req[rid];
             if (!path_step(rq, g, st)) {
-                // main(): lastRes + result, NaN samples dropped; one owner per pixel
-                if (!hasNan(st.result)) {
-                    float4* f = rq.frame + (size_t)py * rq.sc.filmW + px;
-                    v3 last = mk3(0.0f);
-                    if (L.s != 0) {
-                        float4 o = *f;
-                        last = mk3(o.x, o.y, o.z);
-                    }
-                    v3 r = last + st.result;
-                    *f = make_float4(r.x, r.y, r.z, 1.0f);
-                }
+                float* o = rq.scratch + 3 * ((size_t)(js - L.j0) * rq.npix + (size_t)py * rq.sc.filmW + px);
+                o[0] = st.result.x;
+                o[1] = st.result.y;
+                o[2] = st.result.z;
                 live = false;
             }
         }
     }
+}
+
+// Adds the chunk's samples [j0, j1) of every request to its frame in sample
+// order, as consecutive path-tracer passes do (main(),
+// path_integ_naive.glsl:166-173): sample 0 starts from zero, a NaN sample
+// leaves the pixel as it was.  One thread per pixel of the launch's requests.
+__global__ void batch_accumulate_kernel(const __grid_constant__ BatchLaunch L) {
+    const int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (item >= L.nitems) return;
+    int lo = 0, hi = L.nreq - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (L.req[mid].itemBase <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchRequest& rq = L.req[lo];
+    const int64_t p = item - rq.itemBase;
+    float4 f = rq.frame[p];
+    v3 acc = mk3(f.x, f.y, f.z);
+    bool written = false;
+    for (int j = L.j0; j < rq.j1; j++) {
+        const float* x = rq.scratch + 3 * ((size_t)(j - L.j0) * rq.npix + (size_t)p);
+        const v3 r = mk3(x[0], x[1], x[2]);
+        const v3 last = (j != 0) ? acc : mk3(0.0f);
+        if (!hasNan(r)) {
+            acc = last + r;
+            written = true;
+        }
+    }
+    if (written) rq.frame[p] = make_float4(acc.x, acc.y, acc.z, 1.0f);
 }
 
 int occupancy_grid(const void* kernel, int block) {
@@ -311,6 +340,11 @@ int occupancy_grid(const void* kernel, int block) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
     return sms * std::max(per_sm, 1);
+}
+
+cudaError_t launch_accumulate(const BatchLaunch& a, cudaStream_t st) {
+    batch_accumulate_kernel<<<(unsigned)((a.nitems + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch(const BatchLaunch& a, int block, cudaStream_t st) {
@@ -336,8 +370,11 @@ struct zgl_batch {
     int32_t nreq = 0;
     int64_t nitems = 0;
     int32_t maxSpp = 0;
+    int32_t chunkLen = 0;  // sample indices per launch (scratch budget)
     std::vector<zgl::BatchRequest> req;
     uint32_t* d_mats = nullptr;
+    uint32_t* d_rows = nullptr;     // maxSpp x 256 Sobol values
+    float* d_scratch = nullptr;     // per request: min(spp, chunkLen) x npix x 3
     unsigned long long* d_counters = nullptr;
     int32_t nchunks_cap = 0;
     zgl_batch_config cfg{};
@@ -357,6 +394,8 @@ void batch_free(zgl_batch* b) {
     if (b->ev_out) cudaEventDestroy(b->ev_out);
     if (b->stream) cudaStreamDestroy(b->stream);
     if (b->d_mats) cudaFree(b->d_mats);
+    if (b->d_rows) cudaFree(b->d_rows);
+    if (b->d_scratch) cudaFree(b->d_scratch);
     if (b->d_counters) cudaFree(b->d_counters);
     delete b;
 }
@@ -366,6 +405,7 @@ zgl_batch_config resolve(const zgl_batch_config& c) {
     if (r.block_size == 0) r.block_size = 128;
     if (r.queue_capacity == 0) r.queue_capacity = 32;
     if (r.regen_threshold == 0) r.regen_threshold = 16;
+    if (r.schedule == ZGL_BATCH_DEFAULT) r.schedule = ZGL_BATCH_FLAT;
     return r;
 }
 
@@ -374,44 +414,83 @@ void check_config(const zgl_batch_config& c) {
         fail(ZGL_ERR_INVALID_ARG, "batch: block_size must be 64, 128 or 256");
     if (c.queue_capacity < 0 || c.queue_capacity > 4096) fail(ZGL_ERR_INVALID_ARG, "batch: queue_capacity out of range");
     if (c.regen_threshold < 0 || c.regen_threshold > 32) fail(ZGL_ERR_INVALID_ARG, "batch: regen_threshold out of range");
+    if (c.scratch_mib < 0) fail(ZGL_ERR_INVALID_ARG, "batch: negative scratch budget");
+    if (c.schedule != ZGL_BATCH_DEFAULT && c.schedule != ZGL_BATCH_FLAT && c.schedule != ZGL_BATCH_PERSISTENT)
+        fail(ZGL_ERR_INVALID_ARG, "batch: unknown schedule %d", c.schedule);
 }
 
-// Enqueues the whole render on `st`: frame clears, then for every sample
-// index one persistent launch per group of up to 64 requests that still need
-// that sample (each with its own counter reset).  `first_samples` > 0 renders
-// only that many sample indices (autotuning).
+// Enqueues the whole render on `st`: frame clears, then per chunk of sample
+// indices one persistent launch per group of up to 64 requests that need
+// samples of the chunk (each with its own counter reset) and the in-order
+// frame updates of that group.  `first_samples` > 0 renders only that many
+// sample indices (autotuning).
 void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, int first_samples) {
     for (const auto& r : b->req)
         ZGL_CUDA(cudaMemsetAsync(r.frame, 0, sizeof(float4) * (size_t)r.npix, st));
-    int nsamples = first_samples > 0 ? std::min(first_samples, b->maxSpp) : b->maxSpp;
+    const int nsamples = first_samples > 0 ? std::min(first_samples, b->maxSpp) : b->maxSpp;
     int k = 0;
-    for (int s = 0; s < nsamples; s++) {
+    for (int j0 = 0; j0 < nsamples; j0 += b->chunkLen) {
+        const int j1 = std::min(j0 + b->chunkLen, nsamples);
         std::vector<int> active;
         for (int i = 0; i < b->nreq; i++)
-            if (b->req[(size_t)i].spp > s) active.push_back(i);
+            if (b->req[(size_t)i].spp > j0) active.push_back(i);
         for (size_t g0 = 0; g0 < active.size(); g0 += kMaxReqPerLaunch) {
             if (k >= b->nchunks_cap) fail(ZGL_ERR_STATE, "batch: launch count exceeds the counter array");
-            BatchLaunch L;
+            BatchLaunch L, A;
             std::memset(&L, 0, sizeof(L));
-            int64_t base = 0;
+            int64_t base = 0, pbase = 0;
             for (size_t j = g0; j < active.size() && (int)(j - g0) < kMaxReqPerLaunch; j++) {
                 BatchRequest q = b->req[(size_t)active[j]];
+                q.j1 = std::min(j1, q.spp);
                 q.itemBase = base;
-                int tilesY = (q.sc.filmH + 3) / 4;
-                base += (int64_t)q.tilesX * tilesY * 32;
+                base += (int64_t)(q.j1 - j0) * q.perSample;
                 L.req[L.nreq++] = q;
             }
             L.nitems = base;
-            L.s = s;
-            int32_t off = (int32_t)((uint32_t)s * 256u);
-            if (off > 131072 * 256) off -= 131072 * 256;
-            L.sampleOffset = (uint32_t)off;
+            L.j0 = j0;
             L.counter = b->d_counters + k;
             L.queueCap = c.queue_capacity;
             L.regenThreshold = c.regen_threshold;
             L.mats = b->d_mats;
-            ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
-            ZGL_CUDA(launch_batch(L, c.block_size, st));
+            L.rows = b->d_rows;
+            A = L;
+            for (int i = 0; i < A.nreq; i++) {
+                A.req[i].itemBase = pbase;
+                pbase += A.req[i].npix;
+            }
+            A.nitems = pbase;
+            if (c.schedule == ZGL_BATCH_PERSISTENT) {
+                ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
+                ZGL_CUDA(launch_batch(L, c.block_size, st));
+            } else {
+                FlatLaunch F;
+                std::memset(&F, 0, sizeof(F));
+                int64_t bb = 0;
+                for (int i = 0; i < L.nreq; i++) {
+                    const BatchRequest& q = L.req[i];
+                    FlatRequest& f = F.req[F.nreq++];
+                    f.sc = q.sc;
+                    f.maxDepth = q.pp.maxDepth;
+                    f.rr = q.pp.rr;
+                    f.rrStart = q.pp.rrStart;
+                    f.sampleLight = q.pp.sampleLight;
+                    f.uniformSel = q.pp.uniformSel;
+                    f.portion = q.pp.portion;
+                    f.scratch = q.scratch;
+                    f.tilesX = (q.sc.filmW + 15) / 16;
+                    f.tilesY = (q.sc.filmH + 7) / 8;
+                    f.j1 = q.j1;
+                    f.blockBase = bb;
+                    bb += (int64_t)f.tilesX * f.tilesY * (q.j1 - j0);
+                }
+                F.nblocks = bb;
+                F.j0 = j0;
+                F.rows = b->d_rows;
+                F.mats = b->d_mats;
+                if (bb > 0x7fffffff) fail(ZGL_ERR_INVALID_ARG, "batch: too many tiles in one launch");
+                ZGL_CUDA(launch_batch_flat(F, st));
+            }
+            ZGL_CUDA(launch_accumulate(A, st));
             k++;
         }
     }
@@ -419,7 +498,7 @@ void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, in
 
 bool same_cfg(const zgl_batch_config& x, const zgl_batch_config& y) {
     return x.block_size == y.block_size && x.queue_capacity == y.queue_capacity &&
-           x.regen_threshold == y.regen_threshold;
+           x.regen_threshold == y.regen_threshold && x.schedule == y.schedule;
 }
 
 }  // namespace
@@ -466,6 +545,7 @@ zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const
             q.frame = reinterpret_cast<float4*>(r.frame);
             q.npix = r.scene->filmW * r.scene->filmH;
             q.tilesX = (r.scene->filmW + 7) / 8;
+            q.perSample = q.tilesX * ((r.scene->filmH + 3) / 4) * 32;
             q.itemBase = base;
             base += q.npix;
             b->maxSpp = std::max(b->maxSpp, r.spp);
@@ -476,7 +556,41 @@ zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const
         sobol_matrices(mats);
         ZGL_CUDA(cudaMalloc(&b->d_mats, sizeof(uint32_t) * mats.size()));
         ZGL_CUDA(cudaMemcpy(b->d_mats, mats.data(), sizeof(uint32_t) * mats.size(), cudaMemcpyHostToDevice));
-        b->nchunks_cap = b->maxSpp * ((n + kMaxReqPerLaunch - 1) / kMaxReqPerLaunch);
+        // Sobol rows of every sample index (sampleOffset wrap of
+        // path_integ_naive.glsl:163-164)
+        std::vector<uint32_t> rows((size_t)b->maxSpp * 256);
+        for (int j = 0; j < b->maxSpp; j++) {
+            int32_t off = (int32_t)((uint32_t)j * 256u);
+            if (off > 131072 * 256) off -= 131072 * 256;
+            const uint32_t rowIndex = (uint32_t)off >> 8;
+            for (uint32_t d = 0; d < 256; d++) {
+                uint32_t v = 0, idx = rowIndex;
+                for (int bit = 0; idx != 0u; idx >>= 1, bit++)
+                    if (idx & 1u) v ^= mats[d * 32u + (uint32_t)bit];
+                rows[(size_t)j * 256 + d] = v;
+            }
+        }
+        ZGL_CUDA(cudaMalloc(&b->d_rows, sizeof(uint32_t) * rows.size()));
+        ZGL_CUDA(cudaMemcpy(b->d_rows, rows.data(), sizeof(uint32_t) * rows.size(), cudaMemcpyHostToDevice));
+        // sample indices per launch: the per-sample scratch of all requests
+        // stays within kScratchBudget bytes
+        auto scratch_floats = [&](int len) {
+            size_t f = 0;
+            for (const auto& q : b->req) f += (size_t)std::min(len, q.spp) * (size_t)q.npix * 3;
+            return f;
+        };
+        const size_t budget = cfg.scratch_mib > 0 ? (size_t)cfg.scratch_mib << 20 : kScratchBudget;
+        b->chunkLen = b->maxSpp;
+        while (b->chunkLen > 1 && scratch_floats(b->chunkLen) * sizeof(float) > budget)
+            b->chunkLen = (b->chunkLen + 1) / 2;
+        ZGL_CUDA(cudaMalloc(&b->d_scratch, sizeof(float) * scratch_floats(b->chunkLen)));
+        size_t off = 0;
+        for (auto& q : b->req) {
+            q.scratch = b->d_scratch + off;
+            off += (size_t)std::min(b->chunkLen, q.spp) * (size_t)q.npix * 3;
+        }
+        const int nChunks = (b->maxSpp + b->chunkLen - 1) / b->chunkLen;
+        b->nchunks_cap = nChunks * ((n + kMaxReqPerLaunch - 1) / kMaxReqPerLaunch);
         ZGL_CUDA(cudaMalloc(&b->d_counters, sizeof(unsigned long long) * (size_t)b->nchunks_cap));
         ZGL_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
         ZGL_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming));
@@ -553,24 +667,31 @@ zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chos
     const int thresholds[] = {4, 16, 32};
     zgl_batch_config best = b->cfg;
     float bestMs = 1e30f;
+    auto trial = [&](const zgl_batch_config& c) {
+        ZGL_CUDA(cudaEventRecord(e0, st));
+        enqueue_render(b, c, st, 2);
+        ZGL_CUDA(cudaEventRecord(e1, st));
+        ZGL_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        ZGL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < bestMs) {
+            bestMs = ms;
+            best = c;
+        }
+    };
     try {
+        zgl_batch_config flat = b->cfg;
+        flat.schedule = ZGL_BATCH_FLAT;
+        trial(flat);
         for (int bs : blocks)
             for (int cap : caps)
                 for (int th : thresholds) {
                     zgl_batch_config c = b->cfg;
+                    c.schedule = ZGL_BATCH_PERSISTENT;
                     c.block_size = bs;
                     c.queue_capacity = cap;
                     c.regen_threshold = th;
-                    ZGL_CUDA(cudaEventRecord(e0, st));
-                    enqueue_render(b, c, st, 2);
-                    ZGL_CUDA(cudaEventRecord(e1, st));
-                    ZGL_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.0f;
-                    ZGL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                    if (ms < bestMs) {
-                        bestMs = ms;
-                        best = c;
-                    }
+                    trial(c);
                 }
     } catch (...) {
         cudaEventDestroy(e0);

@@ -252,6 +252,12 @@ class PathIntegrator:
 
         call("zgl_integrator_render_pass", self._h, _stream_handle(stream))
 
+    def render_passes(self, passes: int, stream=None) -> None:
+        """`passes` consecutive passes (one launch for the path tracer)."""
+        from .accel import _stream_handle
+
+        call("zgl_integrator_render_passes", self._h, int(passes), _stream_handle(stream))
+
     def reset(self) -> None:
         call("zgl_integrator_reset", self._h)
 
@@ -302,7 +308,8 @@ class RenderRequest(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("block_size", C.c_int32), ("queue_capacity", C.c_int32), ("regen_threshold", C.c_int32)]
+    _fields_ = [("block_size", C.c_int32), ("queue_capacity", C.c_int32), ("regen_threshold", C.c_int32),
+                ("schedule", C.c_int32), ("scratch_mib", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
