@@ -322,7 +322,7 @@ typedef struct zgl_batch_config {
     int32_t queue_capacity;
     int32_t regen_threshold;
     int32_t schedule;
-    int32_t scratch_mib;  /* per-sample scratch budget in MiB (0 = 4096); fixed at zgl_batch_create */
+    int32_t scratch_mib;  /* per-sample scratch budget in MiB (0 = 8192); fixed at zgl_batch_create */
 } zgl_batch_config;
 
 typedef struct zgl_batch zgl_batch;

@@ -57,7 +57,7 @@ struct BatchRequest {
 };
 
 constexpr int kMaxReqPerLaunch = 64;
-constexpr size_t kScratchBudget = (size_t)4 << 30;  // default per-sample radiance of one launch chunk
+constexpr size_t kScratchBudget = (size_t)8 << 30;  // default per-sample radiance of one launch chunk
 
 struct BatchLaunch {
     BatchRequest req[kMaxReqPerLaunch];
@@ -434,6 +434,12 @@ void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, in
         std::vector<int> active;
         for (int i = 0; i < b->nreq; i++)
             if (b->req[(size_t)i].spp > j0) active.push_back(i);
+        // largest work first, so that small requests fill the launch's tail
+        auto work = [&](int i) {
+            const BatchRequest& q = b->req[(size_t)i];
+            return (double)q.npix * (double)(std::min(j1, q.spp) - j0) * (double)std::max(q.pp.maxDepth, 1);
+        };
+        std::stable_sort(active.begin(), active.end(), [&](int x, int y) { return work(x) > work(y); });
         for (size_t g0 = 0; g0 < active.size(); g0 += kMaxReqPerLaunch) {
             if (k >= b->nchunks_cap) fail(ZGL_ERR_STATE, "batch: launch count exceeds the counter array");
             BatchLaunch L, A;
