@@ -124,3 +124,27 @@ def test_batch_in_sample_chunks(zgl_lib, cuda, schedule):
     b.close()
     for sc, *_ in reqs:
         sc.close()
+
+
+def test_batch_and_multipass_argument_errors(zgl_lib, cuda):
+    import torch
+
+    from zillumgl_gb300 import ZglError
+    from zillumgl_gb300.scene import PathIntegrator
+
+    sc = Scene(cornell_scene(seed=33, width=8, height=8))
+    frame = torch.zeros((8, 8, 4), dtype=torch.float32, device=cuda)
+    for bad in (dict(schedule=7), dict(scratch_mib=-1), dict(schedule=PERSISTENT, block_size=96),
+                dict(schedule=PERSISTENT, regen_threshold=33)):
+        with pytest.raises(ZglError):
+            BatchRenderer([(sc, 2, dict(max_depth=3), frame)], **bad)
+    with pytest.raises(ZglError):
+        BatchRenderer([(sc, 0, dict(max_depth=3), frame)])
+    it = PathIntegrator(sc, max_depth=3)
+    with pytest.raises(ZglError):
+        it.render_passes(-1)
+    it.render_passes(0)  # no-op
+    _, spp = it.get_frame()
+    assert spp == 0
+    it.close()
+    sc.close()
