@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--diff-spp", type=int, default=32, help="samples per pixel of the differentiable workload")
     ap.add_argument("--batch-requests", type=int, default=64, help="requests of the batched workload")
     ap.add_argument("--batch-no-autotune", action="store_true", help="batched workload with the default schedule")
+    ap.add_argument("--batch-schedule", default="", choices=["", "flat", "persistent"],
+                    help="batched workload with this schedule instead of the autotuned one")
     return ap.parse_args()
 
 
@@ -530,9 +532,11 @@ def run_batch(args, stream, dev):
         it.close()
     del multi
     # batched
-    batch = BatchRenderer([(sc, spp, params, fr) for sc, (_, spp, params), fr in zip(scenes, reqs, frames)])
+    sched = {"": {}, "flat": {"schedule": 1}, "persistent": {"schedule": 2}}[args.batch_schedule]
+    batch = BatchRenderer([(sc, spp, params, fr) for sc, (_, spp, params), fr in zip(scenes, reqs, frames)],
+                          **sched)
     t1 = time.time()
-    tuned = batch.config() if args.batch_no_autotune else batch.autotune(stream)
+    tuned = batch.config() if (args.batch_no_autotune or sched) else batch.autotune(stream)
     tune_s = time.time() - t1
     batch.render(stream)  # captures the graph
     stream.synchronize()

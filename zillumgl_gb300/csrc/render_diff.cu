@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#define ZGL_INLINE_MATH 1
 #include "bsdf_grad.cuh"
 #include "path_trace.cuh"
 #include "scene.h"
