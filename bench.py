@@ -359,8 +359,9 @@ def run_ours(args):
         e2e_s = time.perf_counter() - t0
         e2e = {"value": round(rays_per_step * args.steps * world / e2e_s / 1e6, 1), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "note": "C-ABI calls on pinned host arrays; each call stages H2D, traces, copies results back and "
-                       "synchronises"}
+               "note": "C-ABI calls on pinned host arrays: the trace kernels read the rays from and write the hits "
+                       "to page-locked host memory over the host link (NVLink-C2C), each call synchronises; "
+                       "h2d/d2h bytes are the bytes that cross it"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

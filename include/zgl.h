@@ -9,8 +9,11 @@
  *     matching *_destroy call.  One handle is used by one host thread at a time.
  *   - Array arguments of trace calls may be host or device pointers (the
  *     library asks the driver which).  Device arrays are used in place and the
- *     call is asynchronous on `stream`; when any array is host memory the call
- *     stages through device memory and returns after the results are back.
+ *     call is asynchronous on `stream`.  Page-locked (pinned) host arrays are
+ *     used in place too: the kernels read and write them over the host link
+ *     (NVLink-C2C on Grace-Blackwell); pageable host arrays are staged through
+ *     device memory.  A call with any host array returns after the results
+ *     are in host memory.
  *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
  *
  * Each entry point names the reference interface it replaces (paths are

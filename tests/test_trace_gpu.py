@@ -153,3 +153,33 @@ def test_full_scale_scene_sampled_rays(zgl_lib, cuda):
     oocc, _, _, _ = oracle.trace(p.bounds, p.hitTable, v, idx, o2, d2, tmax=tmax, any_hit=True)
     assert np.array_equal(occ.astype(np.int32), oocc)
     acc.close()
+
+
+def test_host_arrays_equal_device_arrays(soup, cuda):
+    """Pinned host arrays are read and written in place by the kernels,
+    pageable ones are staged; results equal the device-array call bit for
+    bit either way."""
+    import torch
+
+    acc, packed, v, idx = soup
+    rng = np.random.default_rng(17)
+    n = (1 << 21) + 12345
+    o, d = _rays_mixed(rng, n)
+    tm = rng.random(n).astype(np.float32)
+    to, td, tt = (torch.from_numpy(x).to(cuda) for x in (o, d, tm))
+    ref_id, ref_t = acc.trace_closest(to, td)
+    ref_occ = acc.trace_any(to, td, tt)
+    torch.cuda.synchronize()
+    ref_id, ref_t, ref_occ = ref_id.cpu().numpy(), ref_t.cpu().numpy(), ref_occ.cpu().numpy()
+    for pinned in (False, True):
+        ho, hd, ht_ = (torch.from_numpy(x) for x in (o, d, tm))
+        hid = torch.empty(n, dtype=torch.int32)
+        hdist = torch.empty(n, dtype=torch.float32)
+        hocc = torch.empty(n, dtype=torch.uint8)
+        if pinned:
+            ho, hd, ht_, hid, hdist, hocc = (x.pin_memory() for x in (ho, hd, ht_, hid, hdist, hocc))
+        acc.trace_closest(ho, hd, hid, hdist)
+        acc.trace_any(ho, hd, ht_, hocc)
+        assert np.array_equal(hid.numpy(), ref_id)
+        assert np.array_equal(hdist.numpy().view(np.uint32), ref_t.view(np.uint32))
+        assert np.array_equal(hocc.numpy(), ref_occ)

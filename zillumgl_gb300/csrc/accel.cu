@@ -243,8 +243,29 @@ bool is_device_ptr(const void* p) {
     return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
-// Moves the arguments of one trace call to device memory when they are host
-// arrays and copies outputs back.  Device arrays pass through untouched.
+// Where a kernel reaches p: device and managed memory in place; page-locked
+// host memory through its mapping in the device address space (the kernel
+// reads and writes it over the host link, so no staging copy is needed; on
+// Grace-Blackwell that link is NVLink-C2C).  nullptr for pageable host
+// memory, which has to be staged.  `host` tells whether p is host memory.
+void* device_address(const void* p, bool& host) {
+    host = false;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        host = true;
+        return nullptr;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+    host = true;
+    if (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr) return attr.devicePointer;
+    return nullptr;
+}
+
+// Moves the arguments of one trace call to device memory when they are
+// pageable host arrays and copies outputs back.  Device arrays and mapped
+// page-locked host arrays are used in place; a call with any host array
+// returns after its results are in host memory.
 class Staging {
 public:
     Staging(const zgl_accel* a, cudaStream_t s) : a_(a), s_(s) {}
@@ -256,7 +277,12 @@ public:
         sl.bytes = bytes;
         sl.in = in;
         sl.out = out;
-        sl.staged = p != nullptr && bytes > 0 && !is_device_ptr(p);
+        if (p != nullptr && bytes > 0) {
+            bool host = false;
+            sl.direct = device_address(p, host);
+            sl.staged = sl.direct == nullptr;
+            anyHost_ = anyHost_ || host;
+        }
         if (sl.staged) {
             sl.off = offset_;
             offset_ += (bytes + 255) & ~size_t(255);
@@ -282,21 +308,22 @@ public:
 
     void* ptr(int slot) const {
         const Slot& sl = slots_[(size_t)slot];
-        return sl.staged ? dev(sl) : sl.user;
+        return sl.staged ? dev(sl) : (sl.direct ? sl.direct : sl.user);
     }
 
-    // Copies staged outputs back and waits for them.
+    // Copies staged outputs back and, when any array is host memory, waits
+    // until the results are there.
     void finish() {
-        if (offset_ == 0) return;
         for (auto& sl : slots_)
             if (sl.staged && sl.out)
                 ZGL_CUDA(cudaMemcpyAsync(sl.user, dev(sl), sl.bytes, cudaMemcpyDeviceToHost, s_));
-        ZGL_CUDA(cudaStreamSynchronize(s_));
+        if (anyHost_) ZGL_CUDA(cudaStreamSynchronize(s_));
     }
 
 private:
     struct Slot {
         void* user = nullptr;
+        void* direct = nullptr;  // device-visible address when used in place
         size_t bytes = 0;
         bool in = false, out = false, staged = false;
         size_t off = 0;
@@ -306,6 +333,7 @@ private:
     cudaStream_t s_;
     std::vector<Slot> slots_;
     size_t offset_ = 0;
+    bool anyHost_ = false;
 };
 
 class DeviceGuard {
