@@ -314,12 +314,6 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
 
 }  // namespace
 
-// Rewrites the differentiable parameters of a scene: material records
-// (baseColor, roughness, metallic, specular) and light-instance powers with
-// the light tables that depend on them (Scene.cpp:200-243).
-void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, const std::vector<uint32_t>& first,
-                           std::vector<float>& instPower);
-
 }  // namespace zgl
 
 using namespace zgl;
@@ -414,7 +408,7 @@ zgl_status zgl_diff_set_params(zgl_diff* d, const float* params) {
     else std::memcpy(p.data(), params, sizeof(float) * p.size());
     for (float v : p)
         if (!std::isfinite(v)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: non-finite parameter");
-    scene_set_diff_params(d->scene, p.data(), d->nmat, d->lightFirst, d->instPower);
+    scene_set_diff_params(d->scene, p.data(), d->nmat, d->instPower);
     d->params_host = p;
     ZGL_CUDA(cudaMemcpy(d->d_values, p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice));
     ZGL_API_END

@@ -447,9 +447,7 @@ void upload_scene(zgl_scene& s) {
 // metallic, specular into record slots 0-3, 5, 6) and light-instance powers
 // (3 per instance), rebuilds the light tables that depend on the powers and
 // updates the device copies in place.
-void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, const std::vector<uint32_t>& first,
-                           std::vector<float>& instPower) {
-    (void)first;
+void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, std::vector<float>& instPower) {
     const int ninst = (int)(instPower.size() / 3);
     for (int k = 0; k < 3 * ninst; k++)
         if (p[6 * nmat + k] < 0.0f) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: negative light power");

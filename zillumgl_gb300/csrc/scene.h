@@ -76,4 +76,11 @@ namespace zgl {
 void sobol_matrices(std::vector<uint32_t>& out);
 float half_round(float x);  // float -> IEEE binary16 (round to nearest even) -> float
 
+// Writes the differentiable parameters into a scene (scene.cpp): per material
+// baseColor rgb, raw roughness, metallic, specular (record slots 0-3, 5, 6),
+// then per light instance power rgb; rebuilds the light tables that depend on
+// the powers (Scene.cpp:200-243) and updates the device copies.  instPower
+// receives the new instance powers.
+void scene_set_diff_params(zgl_scene* s, const float* p, int nmat, std::vector<float>& instPower);
+
 }  // namespace zgl
