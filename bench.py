@@ -72,6 +72,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest of every rank's x (the job's time is its slowest rank's);
+    x itself outside a process group or with one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -282,14 +296,7 @@ def run_ours(args):
                 tot += ms
             step_ms.append(tot)
     torch.cuda.synchronize(dev)
-    total_ms = sum(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), dev)
     rays_per_step = len(specs) * nray
     value = rays_per_step * args.steps * world / (total_ms * 1e-3) / 1e6
 
@@ -356,7 +363,7 @@ def run_ours(args):
         for _ in range(args.steps):
             e2e_step()
         stream.synchronize()
-        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
         e2e = {"value": round(rays_per_step * args.steps * world / e2e_s / 1e6, 1), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "note": "C-ABI calls on pinned host arrays: the trace kernels read the rays from and write the hits "
