@@ -468,6 +468,44 @@ def run_render(args, stream, dev):
                                  "note": "16 passes in one launch (zgl_integrator_render_passes), frame identical "
                                          "to 16 single passes"}
             integ.close()
+        if name == "city":
+            # the display pass (tone map + gamma) on the 1080p frame: 16 B in, 16 B out per pixel
+            from zillumgl_gb300.image import TONE_FILMIC, postprocess
+
+            integ = PathIntegrator(scene, **runs[0][2])
+            integ.render_one_pass(stream)
+            dframe = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+            integ.get_frame(dframe, stream)
+            img = torch.empty_like(dframe)
+            postprocess(dframe, W, H, 1.0, TONE_FILMIC, out=img, stream=stream)
+            stream.synchronize()
+            reps = 20
+            e0.record(stream)
+            for _ in range(reps):
+                postprocess(dframe, W, H, 1.0, TONE_FILMIC, out=img, stream=stream)
+            e1.record(stream)
+            stream.synchronize()
+            pms = e0.elapsed_time(e1) / reps
+            peak, _ = measured_peaks()
+            # the same pass on an 8192 x 4096 film (1 GiB moved per pass, beyond L2): the HBM roofline
+            BW, BH = 8192, 4096
+            big = torch.rand((BH, BW, 4), dtype=torch.float32, device=dev)
+            bimg = torch.empty_like(big)
+            postprocess(big, BW, BH, 1.0, TONE_FILMIC, out=bimg, stream=stream)
+            stream.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                postprocess(big, BW, BH, 1.0, TONE_FILMIC, out=bimg, stream=stream)
+            e1.record(stream)
+            stream.synchronize()
+            bms = e0.elapsed_time(e1) / reps
+            bgbs = BW * BH * 32 / (bms * 1e-3) / 1e9
+            res["postprocess"] = {"ms_1080p": round(pms, 4), "ms_8192x4096": round(bms, 3),
+                                  "gbs_8192x4096": round(bgbs, 1), "hbm_frac": round(bgbs / peak, 3),
+                                  "note": "filmic tone map + pow(1/2.2), 16 B in + 16 B out per pixel; the 1080p "
+                                          "frame stays in L2, the 8192x4096 film (1 GiB per pass) does not"}
+            del big, bimg
+            integ.close()
         # end to end through the C ABI: one pass + the frame read back to pinned host memory
         integ = PathIntegrator(scene, **runs[0][2])
         host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()

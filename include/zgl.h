@@ -388,6 +388,21 @@ zgl_status zgl_diff_backward(zgl_diff* diff, const float* d_image, float* d_para
 zgl_status zgl_diff_destroy(zgl_diff* diff);
 
 /* ------------------------------------------------------------------------ */
+/* Display                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* The reference's display pass (src/shader/post_proc.glsl, set up in
+ * Application.cpp:361-363, 652-660): out = pow(tone(clamp(frame * result_scale,
+ * 0, 1e30)), 1/2.2) per channel, alpha 1.  tone_mapper: 0 none, 1 filmic,
+ * 2 ACES.  `frame` is a DEVICE RGBA32F film of (width / preview_scale) x
+ * (height / preview_scale) texels (preview_scale 1 = full size; the reference's
+ * preview frame); `out` a DEVICE RGBA32F image of width x height.  Output
+ * pixel (x, y) reads texel (x / s, y / s); a texel past the film reads as 0.
+ * Asynchronous on `stream`. */
+zgl_status zgl_postprocess(const float* frame, int32_t width, int32_t height, int32_t preview_scale,
+                           float result_scale, int32_t tone_mapper, float* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Measurement                                                               */
 /* ------------------------------------------------------------------------ */
 

@@ -146,6 +146,8 @@ def _render_lib():
         L.orc_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.orc_transc.restype = None
         L.orc_transc.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L.orc_postprocess.restype = None
+        L.orc_postprocess.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p]
         L.orc_diff_grad.restype = None
         L.orc_diff_grad.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                     C.c_int32, C.c_void_p, C.c_int32]
@@ -207,6 +209,14 @@ def camera(angle, fov):
     out = np.zeros(19, np.float32)
     a = np.ascontiguousarray(angle, np.float32)
     _render_lib().orc_camera(_p(a), float(min(max(fov, 0.1), 90.0)), _p(out))
+    return out
+
+
+def postprocess(frame, width, height, preview_scale, result_scale, tone_mapper):
+    """post_proc.glsl's display pass on a (H/s, W/s, 4) RGBA sum -> (H, W, 4)."""
+    frame = np.ascontiguousarray(frame, np.float32)
+    out = np.zeros((height, width, 4), np.float32)
+    _render_lib().orc_postprocess(_p(frame), width, height, preview_scale, float(result_scale), tone_mapper, _p(out))
     return out
 
 

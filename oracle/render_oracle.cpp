@@ -1761,4 +1761,29 @@ void orc_diff_grad(const OrcScene* sc, int32_t spp, const float* dimage, const i
     }
 }
 
+// The display pass of post_proc.glsl:11-59 (the tone mappers reinhard and CE
+// are defined there but never selected): frame RGBA32F of (W/s) x (H/s)
+// texels, out RGBA32F of W x H; texels past the film read as zero.
+void orc_postprocess(const float* frame, int32_t W, int32_t H, int32_t s, float scale, int32_t mapper, float* out) {
+    const int inW = W / s, inH = H / s;
+    auto calc = [](float x) {
+        const float A = 0.22f, B = 0.3f, C = 0.1f, D = 0.2f, E = 0.01f, F = 0.3f;
+        return (x * (x * A + B * C) + D * E) / (x * (x * A + B) + D * F) - E / F;
+    };
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const int sx = x / s, sy = y / s;
+            const float* c = (sx < inW && sy < inH) ? frame + 4 * ((size_t)sy * inW + sx) : nullptr;
+            float* o = out + 4 * ((size_t)y * W + x);
+            for (int k = 0; k < 3; k++) {
+                float v = (c ? c[k] : 0.0f) * scale;
+                v = fmin_(fmax_(v, 0.0f), 1e30f);
+                if (mapper == 1) v = calc(v * 1.6f) / calc(11.2f);
+                else if (mapper == 2) v = (v * (v * 2.51f + 0.03f)) / (v * (v * 2.43f + 0.59f) + 0.14f);
+                o[k] = zpow(v, 1.0f / 2.2f);
+            }
+            o[3] = 1.0f;
+        }
+}
+
 }  // extern "C"

@@ -85,6 +85,8 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_diff_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_diff_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_diff_destroy": (C.c_int32, [C.c_void_p]),
+    "zgl_postprocess": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
+                                    C.c_void_p]),
     "zgl_measure_l2_read": (C.c_int32, [C.c_size_t, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
 }
 
