@@ -413,6 +413,170 @@ inline BSDFSample principledBRDFSample(vec3 n, vec3 wo, const BSDFParam& p, vec3
     return BSDFSample{wi, pdf, bsdf, 1.0f, Diffuse};
 }
 
+// metalWorkflow / dielectric / thinDielectric (material.glsl:85-355)
+enum : uint32_t { Radiance = 0, Importance = 1 };
+inline bool approximateDelta(float r) { return r < 0.02f; }
+inline vec3 schlickFRough(float c, vec3 F0, float r) {  // microfacet.glsl:14-17
+    vec3 m(fmax_(1.0f - r, F0.x), fmax_(1.0f - r, F0.y), fmax_(1.0f - r, F0.z));
+    return F0 + (m - F0) * pow5(1.0f - c);
+}
+inline vec3 ggxSampleWm(vec3 n, vec3 wo, float alpha, vec2 u) {  // microfacet.glsl:57-64
+    (void)wo;
+    vec2 xi = toConcentricDisk(u);
+    vec3 h(xi.x, xi.y, std::sqrt(fmax_(0.0f, 1.0f - xi.x * xi.x - xi.y * xi.y)));
+    h = normalize(h * vec3(alpha, alpha, 1.0f));
+    return normalToWorld(n, h);
+}
+inline vec3 metalWorkflow(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p) {
+    float alpha = square(p.roughness);
+    vec3 h = normalize(wi + wo);
+    if (!sameHemisphere(n, wo, wi)) return vec3(0.0f);
+    float cosWi = dot(n, wi), cosWo = dot(n, wo);
+    vec3 f0 = mix3(vec3(0.04f), p.baseColor, p.metallic);
+    vec3 f = schlickFRough(satDot(h, wo), f0, p.roughness);
+    float d = ggxD(n, h, alpha);
+    float g = smithG(n, wo, wi, alpha);
+    vec3 kd = vec3(1.0f) - f;
+    kd = kd * (1.0f - p.metallic);
+    float denom = 4.0f * cosWo * cosWi;
+    if (denom < 1e-7f) return vec3(0.0f);
+    return kd * p.baseColor * PiInv + f * d * g / denom;
+}
+inline float metalWorkflowPdf(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p) {
+    float alpha = square(p.roughness);
+    vec3 h = normalize(wo + wi);
+    float pdfDiff = satDot(n, wi) * PiInv;
+    float pdfSpec = ggxPdfVisibleWm(n, h, wo, alpha) / (4.0f * absDot(h, wo));
+    float spec = 1.0f / (2.0f - p.metallic);
+    return mixf(pdfDiff, pdfSpec, spec);
+}
+inline BSDFSample metalWorkflowSample(vec3 n, vec3 wo, const BSDFParam& p, vec3 u) {
+    float alpha = square(p.roughness);
+    float spec = 1.0f / (2.0f - p.metallic);
+    uint32_t type = u.x > spec ? Diffuse : GlosRefl;
+    vec3 wi = type == Diffuse ? sampleCosineWeighted(n, vec2(u.y, u.z)).v
+                              : reflect(-wo, ggxSampleVisibleWm(n, wo, alpha, vec2(u.y, u.z)));
+    if (dot(n, wi) < 0.0f) return invalidSample();
+    return BSDFSample{wi, metalWorkflowPdf(wo, wi, n, p), metalWorkflow(wo, wi, n, p), 1.0f, type};
+}
+inline bool refractDir(vec3& wt, vec3 wi, vec3 n, float eta) {
+    float cosTi = dot(n, wi);
+    if (cosTi < 0.0f) eta = 1.0f / eta;
+    float sin2Ti = fmax_(0.0f, 1.0f - cosTi * cosTi);
+    float sin2Tt = sin2Ti / (eta * eta);
+    if (sin2Tt >= 1.0f) return false;
+    float cosTt = std::sqrt(1.0f - sin2Tt);
+    if (cosTi < 0.0f) cosTt = -cosTt;
+    wt = normalize(-wi / eta + n * (cosTi / eta - cosTt));
+    return true;
+}
+inline float fresnelDielectric(float cosTi, float eta) {
+    cosTi = fmin_(fmax_(cosTi, -1.0f), 1.0f);
+    if (cosTi < 0.0f) {
+        eta = 1.0f / eta;
+        cosTi = -cosTi;
+    }
+    float sinTi = std::sqrt(1.0f - cosTi * cosTi);
+    float sinTt = sinTi / eta;
+    if (sinTt >= 1.0f) return 1.0f;
+    float cosTt = std::sqrt(1.0f - sinTt * sinTt);
+    float rPa = (cosTi - eta * cosTt) / (cosTi + eta * cosTt);
+    float rPe = (eta * cosTi - cosTt) / (eta * cosTi + cosTt);
+    return (rPa * rPa + rPe * rPe) * 0.5f;
+}
+inline vec3 dielectric(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p, uint32_t mode) {
+    if (approximateDelta(p.roughness)) return vec3(0.0f);
+    vec3 h = normalize(wo + wi);
+    float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+    float alpha = p.roughness * p.roughness;
+    if (sameHemisphere(n, wo, wi)) {
+        float refl = fresnelDielectric(absDot(h, wi), p.ior);
+        return (hCosWo * hCosWi < 1e-7f) ? vec3(0.0f)
+                                         : p.baseColor * ggxD(n, h, alpha) * smithG(n, wo, wi, alpha) /
+                                               (4.0f * hCosWo * hCosWi) * refl;
+    }
+    float eta = dot(n, wi) > 0.0f ? p.ior : 1.0f / p.ior;
+    float sqrtDenom = dot(h, wo) + eta * dot(h, wi);
+    float denom = sqrtDenom * sqrtDenom;
+    denom *= absDot(n, wi) * absDot(n, wo);
+    float refl = fresnelDielectric(dot(h, wi), eta);
+    float factor = (mode == Radiance) ? square(1.0f / eta) : 1.0f;
+    return (denom < 1e-7f) ? vec3(0.0f)
+                           : p.baseColor * std::fabs(ggxD(n, h, alpha) * smithG(n, wo, wi, alpha) * hCosWo * hCosWi) /
+                                 denom * (1.0f - refl) * factor;
+}
+inline float dielectricPdf(vec3 wo, vec3 wi, vec3 n, const BSDFParam& p) {
+    if (approximateDelta(p.roughness)) return 0.0f;
+    float alpha = p.roughness * p.roughness;
+    if (sameHemisphere(n, wo, wi)) {
+        vec3 h = normalize(wo + wi);
+        if (dot(wo, h) < 0.0f) return 0.0f;
+        float refl = fresnelDielectric(absDot(h, wi), p.ior);
+        return ggxD(n, h, alpha) / (4.0f * absDot(h, wo)) * refl;
+    }
+    float eta = dot(n, wo) > 0.0f ? p.ior : 1.0f / p.ior;
+    vec3 h = normalize(wo + wi * eta);
+    if (sameHemisphere(h, wo, wi)) return 0.0f;
+    float trans = 1.0f - fresnelDielectric(absDot(h, wo), eta);
+    float dHdWi = absDot(h, wi) / square(dot(h, wo) + eta * dot(h, wi));
+    return ggxD(n, h, alpha) * dHdWi * trans;
+}
+inline BSDFSample dielectricSample(vec3 n, vec3 wo, const BSDFParam& p, uint32_t mode, vec3 u) {
+    float ior = p.ior;
+    if (approximateDelta(p.roughness)) {
+        float refl = fresnelDielectric(dot(n, wo), ior);
+        if (u.x < refl) return BSDFSample{reflect(-wo, n), 1.0f, p.baseColor, 1.0f, SpecRefl};
+        vec3 wi;
+        if (!refractDir(wi, wo, n, ior)) return invalidSample();
+        if (dot(n, wo) < 0.0f) ior = 1.0f / ior;
+        float factor = (mode == Radiance) ? square(1.0f / ior) : 1.0f;
+        return BSDFSample{wi, 1.0f, p.baseColor * factor, ior, SpecTrans};
+    }
+    float alpha = p.roughness * p.roughness;
+    vec3 h = ggxSampleWm(n, wo, alpha, vec2(u.y, u.z));
+    if (dot(n, h) < 0.0f) h = -h;
+    float refl = fresnelDielectric(dot(h, wo), ior);
+    if (u.x < refl) {
+        vec3 wi = -reflect(wo, h);
+        if (!sameHemisphere(n, wo, wi)) return invalidSample();
+        float pdf = ggxD(n, h, alpha) / (4.0f * absDot(h, wo));
+        float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+        vec3 r = (hCosWo * hCosWi < 1e-7f) ? vec3(0.0f)
+                                           : p.baseColor * ggxD(n, h, alpha) * smithG(n, wo, wi, alpha) /
+                                                 (4.0f * hCosWo * hCosWi);
+        if (std::isnan(pdf)) pdf = 0.0f;
+        return BSDFSample{wi, pdf, r, 1.0f, GlosRefl};
+    }
+    vec3 wi;
+    if (!refractDir(wi, wo, h, ior)) return invalidSample();
+    if (sameHemisphere(n, wo, wi)) return invalidSample();
+    if (absDot(n, wi) < 1e-10f) return invalidSample();
+    float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+    if (dot(h, wo) < 0.0f) ior = 1.0f / ior;
+    float sqrtDenom = dot(h, wo) + ior * dot(h, wi);
+    float denom = sqrtDenom * sqrtDenom;
+    float dHdWi = hCosWi / denom;
+    float factor = (mode == Radiance) ? square(1.0f / ior) : 1.0f;
+    denom *= absDot(n, wi) * absDot(n, wo);
+    vec3 t = (denom < 1e-7f) ? vec3(0.0f)
+                             : p.baseColor * std::fabs(ggxD(n, h, alpha) * smithG(n, wo, wi, alpha) * hCosWo * hCosWi) /
+                                   denom;
+    float pdf = ggxD(n, h, alpha) * dHdWi;
+    if (std::isnan(pdf)) pdf = 0.0f;
+    return BSDFSample{wi, pdf, t * factor, ior, GlosTrans};
+}
+inline BSDFSample thinDielectricSample(vec3 n, vec3 wo, const BSDFParam& p, vec3 u) {
+    if (dot(n, wo) < 0.0f) n = -n;
+    float refl = fresnelDielectric(dot(n, wo), p.ior);
+    float trans = 1.0f - refl;
+    if (refl < 1.0f) {
+        refl += trans * trans * refl / (1.0f - refl * refl);
+        trans = 1.0f - refl;
+    }
+    return (u.x < refl) ? BSDFSample{reflect(-wo, n), 1.0f, p.baseColor, 1.0f, SpecRefl}
+                        : BSDFSample{-wo, 1.0f, p.baseColor, 1.0f, SpecTrans};
+}
+
 // ---------------------------------------------------- material_loader.glsl
 inline uint32_t loadMaterialType(const OrcScene& sc, int matId) {
     int32_t t;
@@ -423,7 +587,15 @@ inline BSDFParam loadMaterial(const OrcScene& sc, uint32_t type, int matId) {  /
     const float* m = sc.materials + 16 * matId;
     BSDFParam p;
     p.baseColor = vec3(m[0], m[1], m[2]);
-    if (type == PrincipledBRDF) {
+    if (type == MetalWorkflow) {  // loadMetalWorkflow :26-35
+        p.roughness = mixf(0.0134f, 1.0f, m[3]);
+        p.metallic = m[5];
+    } else if (type == Dielectric) {  // loadDielectric :60-69
+        p.roughness = m[3];
+        p.ior = m[12];
+    } else if (type == ThinDielectric) {  // loadThinDielectric :71-79
+        p.ior = m[12];
+    } else if (type == PrincipledBRDF) {
         p.roughness = mixf(0.0134f, 1.0f, m[3]);
         p.subsurface = m[4];
         p.metallic = m[5];
@@ -436,16 +608,26 @@ inline BSDFParam loadMaterial(const OrcScene& sc, uint32_t type, int matId) {  /
     }
     return p;
 }
-inline vec3 materialBSDF(uint32_t type, const BSDFParam& p, vec3 wo, vec3 wi, vec3 n) {
+inline vec3 materialBSDF(uint32_t type, const BSDFParam& p, vec3 wo, vec3 wi, vec3 n, uint32_t mode = Radiance) {
     if (type == PrincipledBRDF) return principledBRDF(wo, wi, n, p);
+    if (type == MetalWorkflow) return metalWorkflow(wo, wi, n, p);
+    if (type == Dielectric) return dielectric(wo, wi, n, p, mode);
+    if (type == ThinDielectric) return vec3(0.0f);
     return lambertian(p);
 }
 inline float materialPdf(uint32_t type, const BSDFParam& p, vec3 wo, vec3 wi, vec3 n) {
     if (type == PrincipledBRDF) return principledBRDFPdf(wo, wi, n, p);
+    if (type == MetalWorkflow) return metalWorkflowPdf(wo, wi, n, p);
+    if (type == Dielectric) return dielectricPdf(wo, wi, n, p);
+    if (type == ThinDielectric) return 0.0f;
     return lambertianPdf(wi, n);
 }
-inline BSDFSample materialSample(uint32_t type, const BSDFParam& p, vec3 n, vec3 wo, vec3 u, Rng& g) {
+inline BSDFSample materialSample(uint32_t type, const BSDFParam& p, vec3 n, vec3 wo, vec3 u, Rng& g,
+                                 uint32_t mode = Radiance) {
     if (type == PrincipledBRDF) return principledBRDFSample(n, wo, p, u, g);
+    if (type == MetalWorkflow) return metalWorkflowSample(n, wo, p, u);
+    if (type == Dielectric) return dielectricSample(n, wo, p, mode, u);
+    if (type == ThinDielectric) return thinDielectricSample(n, wo, p, u);
     return lambertianSample(n, p, u);
 }
 
@@ -900,7 +1082,7 @@ void lightIntegTrace(const OrcScene& sc, Rng& g, float* film) {
             if (ci.pdf > 0.0f) {
                 vec3 pCam = pos + ci.wi * ci.dist;
                 if (visibleOrc(sc, pos, pCam)) {
-                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, Importance);  // light_path_integ.glsl:113
                     float cosWi = satDot(surf.ng, ci.wi) * std::fabs(dot(surf.ns, wo) / dot(surf.ng, wo));
                     vec3 res = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     if (!hasNan(res) && !std::isnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
@@ -909,7 +1091,7 @@ void lightIntegTrace(const OrcScene& sc, Rng& g, float* film) {
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g, Importance);
         vec3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
@@ -1072,7 +1254,7 @@ void traceLightPath(const OrcScene& sc, Rng& g, float* film, float uScale) {
                 vec3 pCam = pos + ci.wi * ci.dist;
                 if (visibleOrc(sc, pos, pCam)) {
                     float cosWi = satDot(surf.ng, ci.wi) * std::fabs(dot(surf.ns, wo) / dot(surf.ng, wo));
-                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    vec3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, Importance);  // triple_path_pass_lpt.glsl:129
                     vec3 contrib = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     float coefToSurf = remap(thinLensCameraPdfIe(sc, Ray{pCam, -ci.wi}).pdfDir * satDot(surf.ns, ci.wi));
                     float coefToPrev = remap(materialPdf(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
@@ -1087,7 +1269,7 @@ void traceLightPath(const OrcScene& sc, Rng& g, float* film, float uScale) {
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g, Importance);
         vec3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
@@ -1239,7 +1421,9 @@ D3 principledD(const float* m, const double* q, D3 wo, D3 wi, D3 n) {
 void bsdfLogGrad(const OrcScene& sc, int matId, vec3 wo, vec3 wi, vec3 n, double out[6][3]) {
     const float* m = sc.materials + 16 * matId;
     for (int i = 0; i < 6; i++) out[i][0] = out[i][1] = out[i][2] = 0.0;
-    if (loadMaterialType(sc, matId) != PrincipledBRDF) {
+    const uint32_t type = loadMaterialType(sc, matId);
+    if (type != PrincipledBRDF && type != Lambertian) return;  // no differentiable parameters
+    if (type == Lambertian) {
         for (int c = 0; c < 3; c++) out[c][c] = m[c] != 0.0f ? 1.0 / (double)m[c] : 0.0;
         return;
     }

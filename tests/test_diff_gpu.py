@@ -153,7 +153,7 @@ def test_autograd_inverse_rendering_reduces_the_loss(zgl_lib, cuda):
         opt.step()
         with torch.no_grad():
             p.clamp_(0.01, 100.0)
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < 0.5 * losses[0], losses
     err0 = np.abs(perturbed_params(p_true, 8, seed=26) - p_true)[:48].mean()
     err1 = np.abs(p.detach().cpu().numpy() - p_true)[:48].mean()

@@ -140,7 +140,7 @@ def test_env_sum_truncation_and_leftover_probabilities():
     assert s > 0 and np.float32(int(s)) <= s
 
 
-@pytest.mark.parametrize("bad", ["texture", "type", "nan", "index", "power", "film"])
+@pytest.mark.parametrize("bad", ["texture", "type", "ior", "nan", "index", "power", "film"])
 def test_scene_rejects_invalid_input(zgl_lib, bad):
     from zillumgl_gb300 import ZglError
 
@@ -148,7 +148,9 @@ def test_scene_rejects_invalid_input(zgl_lib, bad):
     if bad == "texture":
         d.obj_mat_tex[0] = mat_tex(0, 2)
     elif bad == "type":
-        d.materials[0] = material(3)
+        d.materials[0] = material(7)
+    elif bad == "ior":
+        d.materials[0] = material(3, ior=0.0)
     elif bad == "nan":
         d.materials[0, 0] = np.nan
     elif bad == "index":

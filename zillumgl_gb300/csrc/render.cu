@@ -246,7 +246,7 @@ __device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler&
             if (ci.pdf > 0.0f) {
                 v3 pCam = pos + ci.wi * ci.dist;
                 if (visible(sc, pos, pCam)) {
-                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, kImportance);
                     float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
                     v3 res = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     if (!hasNan(res) && !zisnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
@@ -255,7 +255,7 @@ __device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler&
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
@@ -423,7 +423,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
                 v3 pCam = pos + ci.wi * ci.dist;
                 if (visible(sc, pos, pCam)) {
                     float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
-                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns);
+                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, kImportance);
                     v3 contrib = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     float coefToSurf = remap(thinLensCameraPdfIe(sc, Ray{pCam, -ci.wi}).pdfDir * satDot(surf.ns, ci.wi));
                     float coefToPrev = remap(materialPdf(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
@@ -438,7 +438,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);

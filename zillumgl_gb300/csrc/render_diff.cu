@@ -241,7 +241,10 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 surf.ng = -surf.ng;
             }
             const BSDFParam mp = loadMaterial(sc, matType, matId);
-            mkey = kDiffMatParams * matId;
+            // metal-workflow and dielectric materials have no differentiable
+            // parameters; their vertices only carry the paths
+            const bool diffMat = matType == kLambertian || matType == kPrincipled;
+            mkey = diffMat ? kDiffMatParams * matId : -1;
             if (pp.sampleLight) {
                 const float ud = sample1D(g);
                 const float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
@@ -250,11 +253,13 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 const int lid = ud < pdfSampleLight ? lightSampleOne(sc, mk2(u0, u1)) : -1;
                 const LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
                 if (ls.pdf > 0.0f) {
-                    const BsdfGrad bg = bsdfGrad(matType, mp, wo, ls.wi, surf.ns);
+                    BsdfGrad bg;
+                    if (diffMat) bg = bsdfGrad(matType, mp, wo, ls.wi, surf.ns);
+                    const v3 f = diffMat ? bg.f : materialBSDF(matType, mp, wo, ls.wi, surf.ns);
                     const float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
                     const float weight = biHeuristic(ls.pdf, fpdf);
-                    const v3 C = bg.f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
-                    mat_grad(mg, delta, C, bg);
+                    const v3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+                    if (diffMat) mat_grad(mg, delta, C, bg);
                     if (lid >= 0) nkey = power_grad(di, params, lid, delta, C, npw);
                     // what is left below the rounding of the total is no radiance
                     Lrem = Lrem - C;
@@ -272,7 +277,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 alive = false;
             } else {
                 // every later contribution carries this vertex's sampled BSDF value
-                mat_grad(mg, delta, Lrem, bsdfGrad(matType, mp, wo, wi, surf.ns));
+                if (diffMat) mat_grad(mg, delta, Lrem, bsdfGrad(matType, mp, wo, wi, surf.ns));
                 throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
                 ray = rayOffseted(pos, wi);
                 float dist;

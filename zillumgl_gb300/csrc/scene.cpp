@@ -319,10 +319,12 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
     for (size_t m = 0; m < d.n_materials; m++) {
         int32_t type;
         std::memcpy(&type, &s.materials[16 * m + 13], 4);
-        if (type != 0 && type != 1)
+        if (type < 0 || type > 4)
             fail(ZGL_ERR_INVALID_ARG,
-                 "zgl_scene_create: material %zu has type %d; lambertian (0) and principled (1) are supported", m,
-                 type);
+                 "zgl_scene_create: material %zu has type %d; the types are lambertian (0), principled (1), "
+                 "metal workflow (2), dielectric (3) and thin dielectric (4)", m, type);
+        if ((type == 3 || type == 4) && !(s.materials[16 * m + 12] > 0.0f))
+            fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: dielectric material %zu needs ior > 0", m);
         for (int k = 0; k < 13; k++)
             if (!std::isfinite(s.materials[16 * m + k]))
                 fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: material %zu parameter %d is not finite", m, k);

@@ -173,7 +173,11 @@ struct BSDFParam {
     v3 baseColor;
     float subsurface, metallic, roughness, specular, specularTint;
     float sheen, sheenTint, clearcoat, clearcoatGloss;
+    float ior;
 };
+// TransportMode (material.glsl:19-21): the dielectric's refraction scales
+// radiance by 1/eta^2 but not importance.
+enum : uint32_t { kRadiance = 0, kImportance = 1 };
 struct BSDFSample {
     v3 wi;
     float pdf;
@@ -282,6 +286,191 @@ __device__ __forceinline__ BSDFSample principledBRDFSample(v3 n, v3 wo, const BS
     return r;
 }
 
+// metalWorkflow, dielectric and thinDielectric (material.glsl:85-355).  Used
+// only by scenes with those materials, so they stay out of line.
+__device__ __forceinline__ BSDFSample invalidSample() {
+    BSDFSample r;
+    r.wi = mk3(0.0f);
+    r.pdf = 0.0f;
+    r.bsdf = mk3(0.0f);
+    r.flag = kInvalid;
+    return r;
+}
+__device__ __forceinline__ BSDFSample makeSample(v3 wi, float pdf, v3 bsdf, uint32_t flag) {
+    BSDFSample r;
+    r.wi = wi;
+    r.pdf = pdf;
+    r.bsdf = bsdf;
+    r.flag = flag;
+    return r;
+}
+__device__ __forceinline__ bool approximateDelta(float roughness) { return roughness < 0.02f; }
+__device__ __forceinline__ v3 schlickFR(float c, v3 F0, float roughness) {  // microfacet.glsl:14-17
+    const float r1 = 1.0f - roughness;
+    return F0 + (mk3(zmax(r1, F0.x), zmax(r1, F0.y), zmax(r1, F0.z)) - F0) * pow5(1.0f - c);
+}
+__device__ __forceinline__ v3 ggxSampleWm(v3 n, v3 wo, float alpha, v2 u) {  // microfacet.glsl:57-64
+    v2 xi = toConcentricDisk(u);
+    v3 h = mk3(xi.x, xi.y, zsqrt(zmax(0.0f, 1.0f - xi.x * xi.x - xi.y * xi.y)));
+    h = normalize(h * mk3(alpha, alpha, 1.0f));
+    return normalToWorld(n, h);
+}
+static __device__ __noinline__ v3 metalWorkflowBSDF(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :85-113
+    const float alpha = sq(p.roughness);
+    const v3 h = normalize(wi + wo);
+    if (!sameHemisphere(n, wo, wi)) return mk3(0.0f);
+    const float cosWi = dot(n, wi), cosWo = dot(n, wo);
+    const v3 f0 = mix3(mk3(0.04f), p.baseColor, p.metallic);
+    const v3 f = schlickFR(satDot(h, wo), f0, p.roughness);
+    const float d = ggx(dot(n, h), alpha);
+    const float g = smithG(n, wo, wi, alpha);
+    v3 kd = mk3(1.0f) - f;
+    kd = kd * (1.0f - p.metallic);
+    const float denom = 4.0f * cosWo * cosWi;
+    if (denom < 1e-7f) return mk3(0.0f);
+    return kd * p.baseColor * kPiInv + f * d * g / denom;
+}
+static __device__ __noinline__ float metalWorkflowPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :115-123
+    const float alpha = sq(p.roughness);
+    const v3 h = normalize(wo + wi);
+    const float pdfDiff = satDot(n, wi) * kPiInv;
+    const float pdfSpec = ggxPdfVisibleWm(n, h, wo, alpha) / (4.0f * absDot(h, wo));
+    const float spec = 1.0f / (2.0f - p.metallic);
+    return mixf(pdfDiff, pdfSpec, spec);
+}
+static __device__ __noinline__ BSDFSample metalWorkflowSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :125-145
+    const float alpha = sq(p.roughness);
+    const float spec = 1.0f / (2.0f - p.metallic);
+    const uint32_t type = u.x > spec ? kDiffuse : kGlosRefl;
+    v3 wi;
+    if (type == kDiffuse) {
+        float pdf;
+        wi = sampleCosineWeighted(n, mk2(u.y, u.z), pdf);
+    } else {
+        wi = reflect(-wo, ggxSampleVisibleWm(n, wo, alpha, mk2(u.y, u.z)));
+    }
+    if (dot(n, wi) < 0.0f) return invalidSample();
+    return makeSample(wi, metalWorkflowPdf(wo, wi, n, p), metalWorkflowBSDF(wo, wi, n, p), type);
+}
+__device__ __forceinline__ bool refractDir(v3& wt, v3 wi, v3 n, float eta) {  // :147-161
+    const float cosTi = dot(n, wi);
+    if (cosTi < 0.0f) eta = 1.0f / eta;
+    const float sin2Ti = zmax(0.0f, 1.0f - cosTi * cosTi);
+    const float sin2Tt = sin2Ti / (eta * eta);
+    if (sin2Tt >= 1.0f) return false;
+    float cosTt = zsqrt(1.0f - sin2Tt);
+    if (cosTi < 0.0f) cosTt = -cosTt;
+    wt = normalize(-wi / eta + n * (cosTi / eta - cosTt));
+    return true;
+}
+__device__ __forceinline__ float fresnelDielectric(float cosTi, float eta) {  // :163-182
+    cosTi = zmin(zmax(cosTi, -1.0f), 1.0f);
+    if (cosTi < 0.0f) {
+        eta = 1.0f / eta;
+        cosTi = -cosTi;
+    }
+    const float sinTi = zsqrt(1.0f - cosTi * cosTi);
+    const float sinTt = sinTi / eta;
+    if (sinTt >= 1.0f) return 1.0f;
+    const float cosTt = zsqrt(1.0f - sinTt * sinTt);
+    const float rPa = (cosTi - eta * cosTt) / (cosTi + eta * cosTt);
+    const float rPe = (eta * cosTi - cosTt) / (eta * cosTi + cosTt);
+    return (rPa * rPa + rPe * rPe) * 0.5f;
+}
+static __device__ __noinline__ v3 dielectricBSDF(v3 wo, v3 wi, v3 n, BSDFParam p, uint32_t mode) {  // :184-217
+    if (approximateDelta(p.roughness)) return mk3(0.0f);
+    const v3 h = normalize(wo + wi);
+    const float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+    const float alpha = p.roughness * p.roughness;
+    if (sameHemisphere(n, wo, wi)) {
+        const float refl = fresnelDielectric(absDot(h, wi), p.ior);
+        return (hCosWo * hCosWi < 1e-7f)
+                   ? mk3(0.0f)
+                   : p.baseColor * ggx(dot(n, h), alpha) * smithG(n, wo, wi, alpha) / (4.0f * hCosWo * hCosWi) * refl;
+    }
+    const float eta = dot(n, wi) > 0.0f ? p.ior : 1.0f / p.ior;
+    const float sqrtDenom = dot(h, wo) + eta * dot(h, wi);
+    float denom = sqrtDenom * sqrtDenom;
+    denom *= absDot(n, wi) * absDot(n, wo);
+    const float refl = fresnelDielectric(dot(h, wi), eta);
+    const float factor = (mode == kRadiance) ? sq(1.0f / eta) : 1.0f;
+    return (denom < 1e-7f) ? mk3(0.0f)
+                           : p.baseColor * fabsf(ggx(dot(n, h), alpha) * smithG(n, wo, wi, alpha) * hCosWo * hCosWi) /
+                                 denom * (1.0f - refl) * factor;
+}
+static __device__ __noinline__ float dielectricPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :219-243
+    if (approximateDelta(p.roughness)) return 0.0f;
+    const float alpha = p.roughness * p.roughness;
+    if (sameHemisphere(n, wo, wi)) {
+        const v3 h = normalize(wo + wi);
+        if (dot(wo, h) < 0.0f) return 0.0f;
+        const float refl = fresnelDielectric(absDot(h, wi), p.ior);
+        return ggx(dot(n, h), alpha) / (4.0f * absDot(h, wo)) * refl;
+    }
+    const float eta = dot(n, wo) > 0.0f ? p.ior : 1.0f / p.ior;
+    const v3 h = normalize(wo + wi * eta);
+    if (sameHemisphere(h, wo, wi)) return 0.0f;
+    const float trans = 1.0f - fresnelDielectric(absDot(h, wo), eta);
+    const float dHdWi = absDot(h, wi) / sq(dot(h, wo) + eta * dot(h, wi));
+    return ggx(dot(n, h), alpha) * dHdWi * trans;
+}
+static __device__ __noinline__ BSDFSample dielectricSample(v3 n, v3 wo, BSDFParam p, uint32_t mode, v3 u) {  // :245-325
+    float ior = p.ior;
+    if (approximateDelta(p.roughness)) {
+        const float refl = fresnelDielectric(dot(n, wo), ior);
+        if (u.x < refl) return makeSample(reflect(-wo, n), 1.0f, p.baseColor, kSpecRefl);
+        v3 wi;
+        if (!refractDir(wi, wo, n, ior)) return invalidSample();
+        if (dot(n, wo) < 0.0f) ior = 1.0f / ior;
+        const float factor = (mode == kRadiance) ? sq(1.0f / ior) : 1.0f;
+        return makeSample(wi, 1.0f, p.baseColor * factor, kSpecTrans);
+    }
+    const float alpha = p.roughness * p.roughness;
+    v3 h = ggxSampleWm(n, wo, alpha, mk2(u.y, u.z));
+    if (dot(n, h) < 0.0f) h = -h;
+    const float refl = fresnelDielectric(dot(h, wo), ior);
+    if (u.x < refl) {
+        const v3 wi = -reflect(wo, h);
+        if (!sameHemisphere(n, wo, wi)) return invalidSample();
+        float pdf = ggx(dot(n, h), alpha) / (4.0f * absDot(h, wo));
+        const float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+        const v3 r = (hCosWo * hCosWi < 1e-7f)
+                         ? mk3(0.0f)
+                         : p.baseColor * ggx(dot(n, h), alpha) * smithG(n, wo, wi, alpha) / (4.0f * hCosWo * hCosWi);
+        if (zisnan(pdf)) pdf = 0.0f;
+        return makeSample(wi, pdf, r, kGlosRefl);
+    }
+    v3 wi;
+    if (!refractDir(wi, wo, h, ior)) return invalidSample();
+    if (sameHemisphere(n, wo, wi)) return invalidSample();
+    if (absDot(n, wi) < 1e-10f) return invalidSample();
+    const float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
+    if (dot(h, wo) < 0.0f) ior = 1.0f / ior;
+    const float sqrtDenom = dot(h, wo) + ior * dot(h, wi);
+    float denom = sqrtDenom * sqrtDenom;
+    const float dHdWi = hCosWi / denom;
+    const float factor = (mode == kRadiance) ? sq(1.0f / ior) : 1.0f;
+    denom *= absDot(n, wi) * absDot(n, wo);
+    const v3 t = (denom < 1e-7f) ? mk3(0.0f)
+                                 : p.baseColor *
+                                       fabsf(ggx(dot(n, h), alpha) * smithG(n, wo, wi, alpha) * hCosWo * hCosWi) /
+                                       denom;
+    float pdf = ggx(dot(n, h), alpha) * dHdWi;
+    if (zisnan(pdf)) pdf = 0.0f;
+    return makeSample(wi, pdf, t * factor, kGlosTrans);
+}
+static __device__ __noinline__ BSDFSample thinDielectricSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :327-340
+    if (dot(n, wo) < 0.0f) n = -n;
+    float refl = fresnelDielectric(dot(n, wo), p.ior);
+    float trans = 1.0f - refl;
+    if (refl < 1.0f) {
+        refl += trans * trans * refl / (1.0f - refl * refl);
+        trans = 1.0f - refl;
+    }
+    return (u.x < refl) ? makeSample(reflect(-wo, n), 1.0f, p.baseColor, kSpecRefl)
+                        : makeSample(-wo, 1.0f, p.baseColor, kSpecTrans);
+}
+
 // ----------------------------------------------------- material_loader.glsl
 __device__ __forceinline__ uint32_t loadMaterialType(const DeviceScene& sc, int matId) {
     return (uint32_t)__float_as_int(__ldg(&sc.materials[4 * matId + 3]).y);
@@ -292,7 +481,16 @@ __device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_
     p.baseColor = mk3(m0.x, m0.y, m0.z);
     p.subsurface = p.metallic = p.roughness = p.specular = p.specularTint = 0.0f;
     p.sheen = p.sheenTint = p.clearcoat = p.clearcoatGloss = 0.0f;
-    if (type == kPrincipled) {  // loadPrincipledBRDF (material_loader.glsl:37-58)
+    p.ior = 0.0f;
+    if (type == kMetalWorkflow) {  // loadMetalWorkflow (material_loader.glsl:26-35)
+        p.roughness = mixf(0.0134f, 1.0f, m0.w);
+        p.metallic = __ldg(&sc.materials[4 * matId + 1]).y;
+    } else if (type == kDielectric) {  // loadDielectric (:60-69): roughness not remapped
+        p.roughness = m0.w;
+        p.ior = __ldg(&sc.materials[4 * matId + 3]).x;
+    } else if (type == kThinDielectric) {  // loadThinDielectric (:71-79)
+        p.ior = __ldg(&sc.materials[4 * matId + 3]).x;
+    } else if (type == kPrincipled) {  // loadPrincipledBRDF (material_loader.glsl:37-58)
         const float4 m1 = __ldg(&sc.materials[4 * matId + 1]);
         const float4 m2 = __ldg(&sc.materials[4 * matId + 2]);
         p.roughness = mixf(0.0134f, 1.0f, m0.w);
@@ -307,17 +505,29 @@ __device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_
     }
     return p;
 }
-__device__ __forceinline__ v3 materialBSDF(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n) {
+// materialBSDF / materialPdf / materialSample (material_loader.glsl:97-170);
+// `mode` is kRadiance for camera paths and kImportance for light paths.
+__device__ __forceinline__ v3 materialBSDF(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n,
+                                           uint32_t mode = kRadiance) {
     if (type == kPrincipled) return principledBRDF(wo, wi, n, p);
+    if (type == kMetalWorkflow) return metalWorkflowBSDF(wo, wi, n, p);
+    if (type == kDielectric) return dielectricBSDF(wo, wi, n, p, mode);
+    if (type == kThinDielectric) return mk3(0.0f);
     return p.baseColor * kPiInv;
 }
 __device__ __forceinline__ float materialPdf(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n) {
     if (type == kPrincipled) return principledBRDFPdf(wo, wi, n, p);
+    if (type == kMetalWorkflow) return metalWorkflowPdf(wo, wi, n, p);
+    if (type == kDielectric) return dielectricPdf(wo, wi, n, p);
+    if (type == kThinDielectric) return 0.0f;
     return satDot(wi, n) * kPiInv;
 }
 __device__ __forceinline__ BSDFSample materialSample(uint32_t type, const BSDFParam& p, v3 n, v3 wo, v3 u,
-                                                     Sampler& g) {
+                                                     Sampler& g, uint32_t mode = kRadiance) {
     if (type == kPrincipled) return principledBRDFSample(n, wo, p, u, g);
+    if (type == kMetalWorkflow) return metalWorkflowSample(n, wo, p, u);
+    if (type == kDielectric) return dielectricSample(n, wo, p, mode, u);
+    if (type == kThinDielectric) return thinDielectricSample(n, wo, p, u);
     BSDFSample r;  // lambertianSample (material.glsl:78-83)
     float pdf;
     r.wi = sampleCosineWeighted(n, mk2(u.y, u.z), pdf);

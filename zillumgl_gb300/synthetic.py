@@ -361,6 +361,24 @@ def sphere_box_scene(seed: int, n_tris: int, width: int, height: int, sampler: i
     return d.normalized()
 
 
+def material_zoo_scene(seed: int = 41, width: int = 64, height: int = 64, sampler: int = 1):
+    """The Cornell-style box of :func:`cornell_scene` with every material type:
+    Lambertian walls, a metal-workflow tall box (metallic 0.7, roughness 0.4),
+    a thin-dielectric short box (ior 1.5), a smooth glass sphere (roughness
+    0, ior 1.5) and a rough dielectric sphere (roughness 0.35, ior 1.33)."""
+    from .scene import DIELECTRIC, METAL_WORKFLOW, THIN_DIELECTRIC, material
+
+    d = cornell_scene(seed=seed, width=width, height=height, sampler=sampler)
+    mats = np.array(d.materials, np.float32, copy=True)
+    # cornell_scene material order: 5 walls, tall box, short box, principled sphere, sphere
+    mats[5] = material(METAL_WORKFLOW, base_color=(0.9, 0.7, 0.4), roughness=0.4, metallic=0.7)
+    mats[6] = material(THIN_DIELECTRIC, base_color=(0.95, 0.95, 0.9), ior=1.5)
+    mats[7] = material(DIELECTRIC, base_color=(1.0, 1.0, 1.0), roughness=0.0, ior=1.5)
+    mats[8] = material(DIELECTRIC, base_color=(0.9, 1.0, 0.95), roughness=0.35, ior=1.33)
+    d.materials = mats
+    return d.normalized()
+
+
 def diff_scene(seed: int = 11, width: int = 512, height: int = 512, sampler: int = 1):
     """The Cornell-style box of :func:`cornell_scene` with 8 principled
     materials (5 walls, the two boxes sharing one, the two spheres), each with
