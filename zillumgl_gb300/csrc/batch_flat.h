@@ -34,6 +34,7 @@ struct FlatLaunch {
     int32_t j0;
     const uint32_t* rows;  // Sobol rows, 256 values per sample index
     const uint32_t* mats;  // Sobol generator matrices (dimensions past 256)
+    bool full;             // some request uses metal-workflow or dielectric materials
 };
 
 cudaError_t launch_batch_flat(const FlatLaunch& L, cudaStream_t st);

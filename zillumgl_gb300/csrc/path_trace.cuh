@@ -48,6 +48,7 @@ __device__ __forceinline__ float pdfSelectEnv(const DeviceScene& sc, const PathP
 }
 
 // pathIntegTrace (path_integ_naive.glsl:35-143)
+template <bool FULL>
 __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g) {
     float primDist;
     int id = bvhHit(sc, ray, primDist);
@@ -67,20 +68,20 @@ __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sa
                 surf.ng = -surf.ng;
             }
         }
-        BSDFParam mp = loadMaterial(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
         if (pp.sampleLight) {
             float ud = sample1D(g);
             float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
             LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
             if (ls.pdf > 0.0f) {
-                v3 f = materialBSDF(matType, mp, wo, ls.wi, surf.ns);
-                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                v3 f = materialBSDF<FULL>(matType, mp, wo, ls.wi, surf.ns);
+                float fpdf = materialPdf<FULL>(matType, mp, wo, ls.wi, surf.ns);
                 float weight = biHeuristic(ls.pdf, fpdf);
                 result = result + f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
             }
         }
         float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);

@@ -35,6 +35,7 @@ namespace zgl {
 namespace {
 
 // main() of path_integ_naive.glsl:145-174
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY)
 path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uint32_t sampleOffset,
             float4* __restrict__ frame) {
@@ -56,7 +57,7 @@ path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uin
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 result = pathTrace(sc, pp, ray, g);
+    v3 result = pathTrace<FULL>(sc, pp, ray, g);
     v3 last = mk3(0.0f);
     if (spp != 0) {
         float4 f = frame[pix];
@@ -73,6 +74,7 @@ path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uin
 // Several consecutive passes in one launch: pass j = blockIdx.z renders
 // sample c0 + j with freeCounter f0 + j, exactly as path_kernel would, into
 // out[j][pix] (NaN samples kept, the accumulation drops them).
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY, 5)
 path_passes_kernel(DeviceScene sc, PathParams pp, int32_t c0, int32_t f0, float* __restrict__ out) {
     __shared__ uint32_t row[256];
@@ -96,7 +98,7 @@ path_passes_kernel(DeviceScene sc, PathParams pp, int32_t c0, int32_t f0, float*
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 r = pathTrace(sc, pp, ray, g);
+    v3 r = pathTrace<FULL>(sc, pp, ray, g);
     float* o = out + 3 * ((size_t)j * npix + pix);
     o[0] = r.x;
     o[1] = r.y;
@@ -128,6 +130,7 @@ __global__ void accumulate_passes_kernel(const float* __restrict__ in, int64_t n
 
 // Flat schedule of the batched renderer (batch_flat.h): block b is a 16x8
 // tile of one sample of one request.
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY, 5) batch_flat_kernel(const __grid_constant__ FlatLaunch L) {
     const int64_t blk = blockIdx.x;
     int lo = 0, hi = L.nreq - 1;
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(kTileX* kTileY, 5) batch_flat_kernel(const __g
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 r = pathTrace(sc, pp, ray, g);
+    v3 r = pathTrace<FULL>(sc, pp, ray, g);
     float* o = rq.scratch + 3 * ((size_t)(j - L.j0) * ((size_t)sc.filmW * sc.filmH) + pix);
     o[0] = r.x;
     o[1] = r.y;
@@ -184,6 +187,7 @@ __device__ __forceinline__ void accumulateFilm(const DeviceScene& sc, float* fil
     atomicAdd(p + 2, res.z);
 }
 
+template <bool FULL>
 __device__ __forceinline__ void shadeSurface(const DeviceScene& sc, int id, v3 pos, v3 wo, Surface& surf,
                                              uint32_t& matType, BSDFParam& mp) {
     TriShade tri = loadTri(sc, id);
@@ -194,11 +198,12 @@ __device__ __forceinline__ void shadeSurface(const DeviceScene& sc, int id, v3 p
         surf.ns = -surf.ns;
         surf.ng = -surf.ng;
     }
-    mp = loadMaterial(sc, matType, matId);
+    mp = loadMaterial<FULL>(sc, matType, matId);
 }
 
 // lightIntegTrace (light_path_integ.glsl:45-146); the light tracer forces the
 // independent sampler (LightPath.cpp:49), so every dimension is rand().
+template <bool FULL>
 __device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler& g, float* film) {
     float a0 = rand01(g), a1 = rand01(g);
     int light = lightSampleOne(sc, mk2(a0, a1));
@@ -239,14 +244,14 @@ __device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler&
         Surface surf;
         uint32_t matType;
         BSDFParam mp;
-        shadeSurface(sc, id, pos, wo, surf, matType, mp);
+        shadeSurface<FULL>(sc, id, pos, wo, surf, matType, mp);
         {
             float c0 = rand01(g), c1 = rand01(g);
             CameraIiSample ci = thinLensCameraSampleIi(sc, pos, mk2(c0, c1));
             if (ci.pdf > 0.0f) {
                 v3 pCam = pos + ci.wi * ci.dist;
                 if (visible(sc, pos, pCam)) {
-                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, kImportance);
+                    v3 bsdf = materialBSDF<FULL>(matType, mp, wo, ci.wi, surf.ns, kImportance);
                     float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
                     v3 res = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     if (!hasNan(res) && !zisnan(ci.pdf) && ci.pdf > 1e-8f && !isBlack(res))
@@ -255,7 +260,7 @@ __device__ void lightTrace(const DeviceScene& sc, const PathParams& pp, Sampler&
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
+        BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
@@ -277,6 +282,7 @@ __device__ __forceinline__ float weightS1(float s1s0, float t1s1) { return s1s0 
 __device__ __forceinline__ float weightT1(float s0t1, float s1t1) { return 1.0f / (s0t1 + s1t1 + 1.0f); }
 
 // traceCameraPath (triple_path_pass_pt.glsl:59-195)
+template <bool FULL>
 __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g) {
     float primDist;
     int id = bvhHit(sc, ray, primDist);
@@ -299,7 +305,7 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
             surf.ns = -surf.ns;
             surf.ng = -surf.ng;
         }
-        BSDFParam mp = loadMaterial(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
         {
             float a0 = sample1D(g), a1 = sample1D(g);
             int light = lightSampleOne(sc, mk2(a0, a1));
@@ -317,9 +323,9 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
                 float pA = pdfSource / area;
                 float dist2 = distSquare(pos, pLit);
                 float pS = pA * dist2 / absDot(nLit, wi);
-                v3 f = materialBSDF(matType, mp, wo, wi, surf.ns);
-                float fpdf = materialPdf(matType, mp, wo, wi, surf.ns);
-                float pdfRev = materialPdf(matType, mp, wi, wo, surf.ns);
+                v3 f = materialBSDF<FULL>(matType, mp, wo, wi, surf.ns);
+                float fpdf = materialPdf<FULL>(matType, mp, wo, wi, surf.ns);
+                float pdfRev = materialPdf<FULL>(matType, mp, wi, wo, surf.ns);
                 float pdfPLit = remap(pA);
                 float coefToSurf = remap(0.5f * kPiInv * absDot(surf.ns, wi));
                 float coefToLight = remap(fpdf * satDot(nLit, -wi));
@@ -330,7 +336,7 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
             }
         }
         float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+        BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
@@ -341,8 +347,8 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
         int nextId = bvhHit(sc, nextRay, dist);
         int lightId = nextId - sc.objPrimCount;
         v3 nextPos = rayPoint(nextRay, dist);
-        float pdfDirToNext = materialPdf(matType, mp, wo, wi, surf.ns);
-        float pdfDirToPrev = materialPdf(matType, mp, wi, wo, surf.ns);
+        float pdfDirToNext = materialPdf<FULL>(matType, mp, wo, wi, surf.ns);
+        float pdfDirToPrev = materialPdf<FULL>(matType, mp, wi, wo, surf.ns);
         if (nextId == -1) break;
         if (lightId >= 0) {
             v3 nLit = geomNormal(sc, nextId, nextPos);
@@ -376,6 +382,7 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
 }
 
 // traceLightPath (triple_path_pass_lpt.glsl:58-182)
+template <bool FULL>
 __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sampler& g, float* film, float uScale) {
     float a0 = rand01(g), a1 = rand01(g);
     int light = lightSampleOne(sc, mk2(a0, a1));
@@ -415,7 +422,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
         float coefToPos = remap(prevPdfDir * absDot(surf.ns, wo));
         s0t1 /= coefToPos;
         s1t1 /= coefToPos / (bounce == 1 ? remap(dist * dist) : 1.0f);
-        BSDFParam mp = loadMaterial(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
         {
             float c0 = rand01(g), c1 = rand01(g);
             CameraIiSample ci = thinLensCameraSampleIi(sc, pos, mk2(c0, c1));
@@ -423,10 +430,10 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
                 v3 pCam = pos + ci.wi * ci.dist;
                 if (visible(sc, pos, pCam)) {
                     float cosWi = satDot(surf.ng, ci.wi) * fabsf(dot(surf.ns, wo) / dot(surf.ng, wo));
-                    v3 bsdf = materialBSDF(matType, mp, wo, ci.wi, surf.ns, kImportance);
+                    v3 bsdf = materialBSDF<FULL>(matType, mp, wo, ci.wi, surf.ns, kImportance);
                     v3 contrib = ci.Ii * bsdf * throughput * cosWi / ci.pdf;
                     float coefToSurf = remap(thinLensCameraPdfIe(sc, Ray{pCam, -ci.wi}).pdfDir * satDot(surf.ns, ci.wi));
-                    float coefToPrev = remap(materialPdf(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
+                    float coefToPrev = remap(materialPdf<FULL>(matType, mp, ci.wi, wo, surf.ns) * absDot(prevNorm, wo));
                     float coefDist = remap(ci.dist * ci.dist);
                     float coef0 = coefToSurf * coefToPrev / coefDist;
                     float coef1 = ((bounce == 1) ? 1.0f : coefToPrev) * coefToSurf / coefDist;
@@ -438,7 +445,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
             }
         }
         float b0 = rand01(g), b1 = rand01(g), b2 = rand01(g);
-        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
+        BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g, kImportance);
         v3 wi = bs.wi;
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
@@ -448,10 +455,10 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
             if (rand01(g) >= continueProb) break;
             throughput = throughput / continueProb;
         }
-        float coefToPrev = remap(materialPdf(matType, mp, wi, wo, surf.ns) * absDot(prevNorm, wo));
+        float coefToPrev = remap(materialPdf<FULL>(matType, mp, wi, wo, surf.ns) * absDot(prevNorm, wo));
         s0t1 *= coefToPrev;
         s1t1 *= (bounce == 1) ? 1.0f : coefToPrev;
-        prevPdfDir = materialPdf(matType, mp, wo, wi, surf.ns);
+        prevPdfDir = materialPdf<FULL>(matType, mp, wo, wi, surf.ns);
         prevNorm = surf.ns;
         float cosWi = deltaBsdf ? 1.0f : fabsf(dot(surf.ng, wi) * dot(surf.ns, wo) / dot(surf.ng, wo));
         throughput = throughput * (bs.bsdf * cosWi / bsdfPdf);
@@ -463,6 +470,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
 constexpr int kLightBlock = 256;
 
 // main() of light_path_integ.glsl:148-158: logical group 1536 x blocks
+template <bool FULL>
 __global__ void __launch_bounds__(kLightBlock)
 light_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCounter, uint32_t nPaths, float* film) {
     uint32_t gid = blockIdx.x * kLightBlock + threadIdx.x;
@@ -475,10 +483,11 @@ light_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCounter, 
     g.mode = 0;
     g.rowCache = nullptr;
     g.mats = sc.sobol;
-    lightTrace(sc, pp, g, film);
+    lightTrace<FULL>(sc, pp, g, film);
 }
 
 // main() of triple_path_pass_pt.glsl:197-224 (addFilm: one owner per pixel)
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY)
 triple_pt_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uint32_t sampleOffset,
                  float* __restrict__ film) {
@@ -500,7 +509,7 @@ triple_pt_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 r = tripleCameraTrace(sc, pp, ray, g);
+    v3 r = tripleCameraTrace<FULL>(sc, pp, ray, g);
     if (!hasNan(r)) {
         float* p = film + 3 * pix;
         p[0] = p[0] + r.x;
@@ -510,6 +519,7 @@ triple_pt_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter
 }
 
 // main() of triple_path_pass_lpt.glsl:184-191
+template <bool FULL>
 __global__ void __launch_bounds__(kLightBlock)
 triple_lpt_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCounter, uint32_t nThreads,
                   uint32_t loops, float uScale, float* film) {
@@ -523,7 +533,7 @@ triple_lpt_kernel(DeviceScene sc, PathParams pp, uint32_t spp, uint32_t freeCoun
     g.mode = 0;
     g.rowCache = nullptr;
     g.mats = sc.sobol;
-    for (uint32_t i = 0; i < loops; i++) tripleLightTrace(sc, pp, g, film, uScale);
+    for (uint32_t i = 0; i < loops; i++) tripleLightTrace<FULL>(sc, pp, g, film, uScale);
 }
 
 // img_copy_1x32f_4x32f.glsl: film (r, g, b) -> frame (r, g, b, 1)
@@ -541,7 +551,10 @@ cudaError_t launch_path_pass(const zgl_scene* s, const zgl_integrator_params& p,
                   p.light_portion};
     dim3 block(kTileX, kTileY);
     dim3 grid((unsigned)((s->filmW + kTileX - 1) / kTileX), (unsigned)((s->filmH + kTileY - 1) / kTileY));
-    path_kernel<<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), frame);
+    if (s->fullMaterials)
+        path_kernel<true><<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), frame);
+    else
+        path_kernel<false><<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), frame);
     return cudaGetLastError();
 }
 
@@ -551,7 +564,10 @@ cudaError_t launch_path_passes(const zgl_scene* s, const zgl_integrator_params& 
                   p.light_portion};
     dim3 block(kTileX, kTileY);
     dim3 grid((unsigned)((s->filmW + kTileX - 1) / kTileX), (unsigned)((s->filmH + kTileY - 1) / kTileY), (unsigned)n);
-    path_passes_kernel<<<grid, block, 0, st>>>(s->view(), pp, c0, f0, scratch);
+    if (s->fullMaterials)
+        path_passes_kernel<true><<<grid, block, 0, st>>>(s->view(), pp, c0, f0, scratch);
+    else
+        path_passes_kernel<false><<<grid, block, 0, st>>>(s->view(), pp, c0, f0, scratch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t npix = (int64_t)s->filmW * s->filmH;
@@ -561,7 +577,10 @@ cudaError_t launch_path_passes(const zgl_scene* s, const zgl_integrator_params& 
 
 cudaError_t launch_batch_flat(const FlatLaunch& L, cudaStream_t st) {
     if (L.nblocks <= 0) return cudaSuccess;
-    batch_flat_kernel<<<(unsigned)L.nblocks, dim3(kTileX, kTileY), 0, st>>>(L);
+    if (L.full)
+        batch_flat_kernel<true><<<(unsigned)L.nblocks, dim3(kTileX, kTileY), 0, st>>>(L);
+    else
+        batch_flat_kernel<false><<<(unsigned)L.nblocks, dim3(kTileX, kTileY), 0, st>>>(L);
     return cudaGetLastError();
 }
 
@@ -570,7 +589,11 @@ cudaError_t launch_light_pass(const zgl_scene* s, const zgl_integrator_params& p
     PathParams pp{p.max_depth, p.russian_roulette, p.rr_start_depth, p.sample_light, p.light_env_uniform_sample,
                   p.light_portion};
     uint32_t n = 1536u * (uint32_t)blocks;
-    light_kernel<<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(s->view(), pp, (uint32_t)spp,
+    if (s->fullMaterials)
+        light_kernel<true><<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(s->view(), pp, (uint32_t)spp,
+                                                                             (uint32_t)freeCounter, n, film);
+    else
+        light_kernel<false><<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(s->view(), pp, (uint32_t)spp,
                                                                              (uint32_t)freeCounter, n, film);
     return cudaGetLastError();
 }
@@ -581,12 +604,19 @@ cudaError_t launch_triple_pass(const zgl_scene* s, const zgl_integrator_params& 
                   p.light_portion};
     dim3 block(kTileX, kTileY);
     dim3 grid((unsigned)((s->filmW + kTileX - 1) / kTileX), (unsigned)((s->filmH + kTileY - 1) / kTileY));
-    triple_pt_kernel<<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), film);
+    if (s->fullMaterials)
+        triple_pt_kernel<true><<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), film);
+    else
+        triple_pt_kernel<false><<<grid, block, 0, st>>>(s->view(), pp, spp, freeCounter, sample_offset(spp), film);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     uint32_t n = 1536u * (uint32_t)blocks;
     float uScale = (float)(s->filmW * s->filmH) / (float)(blocks * loops * 1536);
-    triple_lpt_kernel<<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(
+    if (s->fullMaterials)
+        triple_lpt_kernel<true><<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(
+        s->view(), pp, (uint32_t)spp, (uint32_t)freeCounter, n, (uint32_t)loops, uScale, film);
+    else
+        triple_lpt_kernel<false><<<(n + kLightBlock - 1) / kLightBlock, kLightBlock, 0, st>>>(
         s->view(), pp, (uint32_t)spp, (uint32_t)freeCounter, n, (uint32_t)loops, uScale, film);
     return cudaGetLastError();
 }

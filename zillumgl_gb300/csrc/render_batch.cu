@@ -131,6 +131,7 @@ __device__ __forceinline__ void start_sample(const BatchRequest& rq, const Batch
 // One step of pathIntegTrace: trace the pending ray, account for what it hits,
 // and, if the path continues, shade the new vertex (light sample + BSDF
 // sample) to produce the next pending ray.  Returns false when the path ends.
+template <bool FULL>
 __device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, PathState& st) {
     const DeviceScene& sc = rq.sc;
     const BatchPathParams& pp = rq.pp;
@@ -193,21 +194,21 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, Pa
         surf.ns = -surf.ns;
         surf.ng = -surf.ng;
     }
-    BSDFParam mp = loadMaterial(sc, matType, matId);
+    BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
     if (pp.sampleLight) {
         float ud = sample1D(g);
         float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g),
               u3 = sample1D(g);
         LiSample ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3);
         if (ls.pdf > 0.0f) {
-            v3 f = materialBSDF(matType, mp, st.wo, ls.wi, surf.ns);
-            float fpdf = materialPdf(matType, mp, st.wo, ls.wi, surf.ns);
+            v3 f = materialBSDF<FULL>(matType, mp, st.wo, ls.wi, surf.ns);
+            float fpdf = materialPdf<FULL>(matType, mp, st.wo, ls.wi, surf.ns);
             float weight = biHeuristic(ls.pdf, fpdf);
             st.result = st.result + f * st.throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
         }
     }
     float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
-    BSDFSample bs = materialSample(matType, mp, surf.ns, st.wo, mk3(b0, b1, b2), g);
+    BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, st.wo, mk3(b0, b1, b2), g);
     st.delta = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
     if (bs.pdf < 1e-8f) return false;
     st.throughput = st.throughput * (bs.bsdf / bs.pdf * (st.delta ? 1.0f : absDot(surf.ns, bs.wi)));
@@ -227,7 +228,7 @@ __device__ __forceinline__ int find_request(const BatchLaunch& L, int64_t item) 
     return lo;
 }
 
-template <int BLOCK>
+template <int BLOCK, bool FULL>
 __global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ BatchLaunch L) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ Ba
         }
         if (live) {
             const BatchRequest& rq = L.req[rid];
-            if (!path_step(rq, g, st)) {
+            if (!path_step<FULL>(rq, g, st)) {
                 float* o = rq.scratch + 3 * ((size_t)(js - L.j0) * rq.npix + (size_t)py * rq.sc.filmW + px);
                 o[0] = st.result.x;
                 o[1] = st.result.y;
@@ -347,18 +348,24 @@ cudaError_t launch_accumulate(const BatchLaunch& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchLaunch& a, int block, cudaStream_t st) {
+template <bool FULL>
+void launch_batch_t(const BatchLaunch& a, int block, cudaStream_t st) {
     switch (block) {
         case 64:
-            batch_kernel<64><<<occupancy_grid((const void*)batch_kernel<64>, 64), 64, 0, st>>>(a);
+            batch_kernel<64, FULL><<<occupancy_grid((const void*)batch_kernel<64, FULL>, 64), 64, 0, st>>>(a);
             break;
         case 256:
-            batch_kernel<256><<<occupancy_grid((const void*)batch_kernel<256>, 256), 256, 0, st>>>(a);
+            batch_kernel<256, FULL><<<occupancy_grid((const void*)batch_kernel<256, FULL>, 256), 256, 0, st>>>(a);
             break;
         default:
-            batch_kernel<128><<<occupancy_grid((const void*)batch_kernel<128>, 128), 128, 0, st>>>(a);
+            batch_kernel<128, FULL><<<occupancy_grid((const void*)batch_kernel<128, FULL>, 128), 128, 0, st>>>(a);
             break;
     }
+}
+
+cudaError_t launch_batch(const BatchLaunch& a, int block, bool full, cudaStream_t st) {
+    if (full) launch_batch_t<true>(a, block, st);
+    else launch_batch_t<false>(a, block, st);
     return cudaGetLastError();
 }
 
@@ -371,6 +378,7 @@ struct zgl_batch {
     int64_t nitems = 0;
     int32_t maxSpp = 0;
     int32_t chunkLen = 0;  // sample indices per launch (scratch budget)
+    bool fullMaterials = false;  // some request's scene has metal-workflow or dielectric materials
     std::vector<zgl::BatchRequest> req;
     uint32_t* d_mats = nullptr;
     uint32_t* d_rows = nullptr;     // maxSpp x 256 Sobol values
@@ -467,7 +475,7 @@ void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, in
             A.nitems = pbase;
             if (c.schedule == ZGL_BATCH_PERSISTENT) {
                 ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
-                ZGL_CUDA(launch_batch(L, c.block_size, st));
+                ZGL_CUDA(launch_batch(L, c.block_size, b->fullMaterials, st));
             } else {
                 FlatLaunch F;
                 std::memset(&F, 0, sizeof(F));
@@ -493,6 +501,7 @@ void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, in
                 F.j0 = j0;
                 F.rows = b->d_rows;
                 F.mats = b->d_mats;
+                F.full = b->fullMaterials;
                 if (bb > 0x7fffffff) fail(ZGL_ERR_INVALID_ARG, "batch: too many tiles in one launch");
                 ZGL_CUDA(launch_batch_flat(F, st));
             }
@@ -555,6 +564,7 @@ zgl_status zgl_batch_create(const zgl_render_request* requests, int32_t n, const
             q.itemBase = base;
             base += q.npix;
             b->maxSpp = std::max(b->maxSpp, r.spp);
+            b->fullMaterials = b->fullMaterials || r.scene->fullMaterials;
             b->req.push_back(q);
         }
         b->nitems = base;

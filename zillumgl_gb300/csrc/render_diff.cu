@@ -55,6 +55,7 @@ struct DiffInfo {
 };
 
 // forward: one thread per (pixel, sample); blockIdx.y = sample
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY)
 diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, float* __restrict__ samples) {
     __shared__ uint32_t row[256];
@@ -78,7 +79,7 @@ diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, float* __rest
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 r = pathTrace(sc, pp, ray, g);
+    v3 r = pathTrace<FULL>(sc, pp, ray, g);
     float* o = samples + 3 * ((size_t)s * sc.filmW * sc.filmH + pix);
     o[0] = r.x;
     o[1] = r.y;
@@ -165,6 +166,7 @@ __device__ __forceinline__ int power_grad(const DiffInfo& di, const float* param
 // bounce per iteration of a warp-uniform loop, so that each iteration's
 // gradients (one material, up to two light instances per lane) are reduced
 // across the warp before the shared-memory atomics.
+template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY)
 diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
                      int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
@@ -240,10 +242,10 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 surf.ns = -surf.ns;
                 surf.ng = -surf.ng;
             }
-            const BSDFParam mp = loadMaterial(sc, matType, matId);
+            const BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
             // metal-workflow and dielectric materials have no differentiable
             // parameters; their vertices only carry the paths
-            const bool diffMat = matType == kLambertian || matType == kPrincipled;
+            const bool diffMat = !FULL || matType == kLambertian || matType == kPrincipled;
             mkey = diffMat ? kDiffMatParams * matId : -1;
             if (pp.sampleLight) {
                 const float ud = sample1D(g);
@@ -255,8 +257,8 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 if (ls.pdf > 0.0f) {
                     BsdfGrad bg;
                     if (diffMat) bg = bsdfGrad(matType, mp, wo, ls.wi, surf.ns);
-                    const v3 f = diffMat ? bg.f : materialBSDF(matType, mp, wo, ls.wi, surf.ns);
-                    const float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                    const v3 f = diffMat ? bg.f : materialBSDF<FULL>(matType, mp, wo, ls.wi, surf.ns);
+                    const float fpdf = materialPdf<FULL>(matType, mp, wo, ls.wi, surf.ns);
                     const float weight = biHeuristic(ls.pdf, fpdf);
                     const v3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
                     if (diffMat) mat_grad(mg, delta, C, bg);
@@ -269,7 +271,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 }
             }
             const float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
-            const BSDFSample bs = materialSample(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
+            const BSDFSample bs = materialSample<FULL>(matType, mp, surf.ns, wo, mk3(b0, b1, b2), g);
             const v3 wi = bs.wi;
             const float bsdfPdf = bs.pdf;
             const bool deltaBsdf = (bs.flag == kSpecRefl || bs.flag == kSpecTrans);
@@ -427,7 +429,10 @@ zgl_status zgl_diff_forward(zgl_diff* d, float* image, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
     dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
-    diff_forward_kernel<<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
+    if (s->fullMaterials)
+        diff_forward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
+    else
+        diff_forward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
     ZGL_CUDA(cudaGetLastError());
     int64_t npix = (int64_t)s->filmW * s->filmH;
     diff_reduce_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(d->d_samples, npix, d->spp, image);
@@ -446,7 +451,11 @@ zgl_status zgl_diff_backward(zgl_diff* d, const float* d_image, float* d_params,
     DiffInfo di{d->nmat, d->nparams, d->d_lightInst};
     int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
     dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
-    diff_backward_kernel<<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
+    if (s->fullMaterials)
+        diff_backward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
+                                                                d->spp, d->d_samples, d_image, d_params);
+    else
+        diff_backward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
                                                                 d->spp, d->d_samples, d_image, d_params);
     ZGL_CUDA(cudaGetLastError());
     ZGL_API_END

@@ -325,6 +325,7 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
                  "metal workflow (2), dielectric (3) and thin dielectric (4)", m, type);
         if ((type == 3 || type == 4) && !(s.materials[16 * m + 12] > 0.0f))
             fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: dielectric material %zu needs ior > 0", m);
+        if (type >= 2) s.fullMaterials = true;
         for (int k = 0; k < 13; k++)
             if (!std::isfinite(s.materials[16 * m + k]))
                 fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: material %zu parameter %d is not finite", m, k);

@@ -23,6 +23,7 @@ struct zgl_scene {
     int64_t nObjVertices = 0;
     int32_t nLight = 0;
     std::vector<float> materials;  // 16 per material
+    bool fullMaterials = false;    // some material is metal workflow, dielectric or thin dielectric
 
     // lights (Scene.cpp:200-243): instance ranges and powers, then per triangle
     std::vector<uint32_t> lightFirst;   // n_instances + 1

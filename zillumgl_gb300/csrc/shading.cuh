@@ -171,9 +171,13 @@ __device__ __forceinline__ v3 gtr1SampleWm(v3 n, v3 wo, float alpha, v2 u) {  //
 // ------------------------------------------------------------ material.glsl
 struct BSDFParam {
     v3 baseColor;
-    float subsurface, metallic, roughness, specular, specularTint;
+    float subsurface, metallic, roughness;
+    union {
+        float specular;  // principled
+        float ior;       // dielectric and thin dielectric (they have no specular)
+    };
+    float specularTint;
     float sheen, sheenTint, clearcoat, clearcoatGloss;
-    float ior;
 };
 // TransportMode (material.glsl:19-21): the dielectric's refraction scales
 // radiance by 1/eta^2 but not importance.
@@ -235,7 +239,7 @@ __device__ __forceinline__ v3 principledDiffuse(v3 wo, v3 wi, v3 n, v3 baseColor
     v3 ss = baseColor * kPiInv * 1.25f * (fss * (1.0f / (cosWi + cosWo) - 0.5f) + mk3(0.5f));
     return mix3(baseDiffuse, ss, subsurface);
 }
-static __device__ __noinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :462-490
+__device__ __forceinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :462-490
     float alpha = sq(p.roughness);
     float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
     float lum = luminance(p.baseColor);
@@ -249,7 +253,7 @@ static __device__ __noinline__ v3 principledBRDF(v3 wo, v3 wi, v3 n, BSDFParam p
     res = res + mix3(mk3(1.0f), tint, p.sheenTint) * schlickW(hCosWi) * p.sheen * (dot(n, wi) < 0.0f ? 0.0f : 1.0f);
     return res;
 }
-static __device__ __noinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :492-514
+__device__ __forceinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, const BSDFParam& p) {  // :492-514
     float pdf = 0.0f;
     float alpha = sq(p.roughness);
     float ccAlpha = mixf(0.1f, 0.001f, p.clearcoatGloss);
@@ -260,11 +264,21 @@ static __device__ __noinline__ float principledBRDFPdf(v3 wo, v3 wi, v3 n, BSDFP
     pdf += principledClearcoatPdf(wo, wi, n, ccAlpha) * 0.25f * p.clearcoat;
     return pdf / (1.0f + 0.25f * p.clearcoat);
 }
-__device__ __forceinline__ BSDFSample principledBRDFSample(v3 n, v3 wo, const BSDFParam& p, v3 u, Sampler& g) {
+// One out-of-line copy of the principled evaluation and pdf per translation
+// unit, called from the sampling routine and the light-sample evaluation.
+static __device__ __noinline__ v3 principledBRDFCall(v3 wo, v3 wi, v3 n, BSDFParam p) {
+    return principledBRDF(wo, wi, n, p);
+}
+static __device__ __noinline__ float principledBRDFPdfCall(v3 wo, v3 wi, v3 n, BSDFParam p) {
+    return principledBRDFPdf(wo, wi, n, p);
+}
+// `ur` is the lobe pick's draw from the rand() stream (material.glsl:539),
+// taken by the caller.
+__device__ __forceinline__ BSDFSample principledBRDFSample(v3 n, v3 wo, const BSDFParam& p, v3 u, float ur) {
     float alpha = sq(p.roughness);  // material.glsl:516-555
     float spec = 1.0f / (2.0f - p.metallic);
     float cdf0 = 1.0f - spec, cdf1 = 1.0f, cdf2 = 1.0f + p.clearcoat * 0.25f;
-    float s = rand01(g) * cdf2;  // the lobe pick draws from the rand() stream
+    float s = ur * cdf2;
     v3 wi;
     if (s <= cdf0) {
         float pdf;
@@ -280,14 +294,13 @@ __device__ __forceinline__ BSDFSample principledBRDFSample(v3 n, v3 wo, const BS
     }
     BSDFSample r;
     r.wi = wi;
-    r.bsdf = principledBRDF(wo, wi, n, p);
-    r.pdf = principledBRDFPdf(wo, wi, n, p);
+    r.bsdf = principledBRDFCall(wo, wi, n, p);
+    r.pdf = principledBRDFPdfCall(wo, wi, n, p);
     r.flag = kDiffuse;
     return r;
 }
 
-// metalWorkflow, dielectric and thinDielectric (material.glsl:85-355).  Used
-// only by scenes with those materials, so they stay out of line.
+// metalWorkflow, dielectric and thinDielectric (material.glsl:85-355).
 __device__ __forceinline__ BSDFSample invalidSample() {
     BSDFSample r;
     r.wi = mk3(0.0f);
@@ -315,7 +328,7 @@ __device__ __forceinline__ v3 ggxSampleWm(v3 n, v3 wo, float alpha, v2 u) {  // 
     h = normalize(h * mk3(alpha, alpha, 1.0f));
     return normalToWorld(n, h);
 }
-static __device__ __noinline__ v3 metalWorkflowBSDF(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :85-113
+__device__ __forceinline__ v3 metalWorkflowBSDF(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :85-113
     const float alpha = sq(p.roughness);
     const v3 h = normalize(wi + wo);
     if (!sameHemisphere(n, wo, wi)) return mk3(0.0f);
@@ -330,7 +343,7 @@ static __device__ __noinline__ v3 metalWorkflowBSDF(v3 wo, v3 wi, v3 n, BSDFPara
     if (denom < 1e-7f) return mk3(0.0f);
     return kd * p.baseColor * kPiInv + f * d * g / denom;
 }
-static __device__ __noinline__ float metalWorkflowPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :115-123
+__device__ __forceinline__ float metalWorkflowPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :115-123
     const float alpha = sq(p.roughness);
     const v3 h = normalize(wo + wi);
     const float pdfDiff = satDot(n, wi) * kPiInv;
@@ -338,7 +351,7 @@ static __device__ __noinline__ float metalWorkflowPdf(v3 wo, v3 wi, v3 n, BSDFPa
     const float spec = 1.0f / (2.0f - p.metallic);
     return mixf(pdfDiff, pdfSpec, spec);
 }
-static __device__ __noinline__ BSDFSample metalWorkflowSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :125-145
+__device__ __forceinline__ BSDFSample metalWorkflowSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :125-145
     const float alpha = sq(p.roughness);
     const float spec = 1.0f / (2.0f - p.metallic);
     const uint32_t type = u.x > spec ? kDiffuse : kGlosRefl;
@@ -377,7 +390,7 @@ __device__ __forceinline__ float fresnelDielectric(float cosTi, float eta) {  //
     const float rPe = (eta * cosTi - cosTt) / (eta * cosTi + cosTt);
     return (rPa * rPa + rPe * rPe) * 0.5f;
 }
-static __device__ __noinline__ v3 dielectricBSDF(v3 wo, v3 wi, v3 n, BSDFParam p, uint32_t mode) {  // :184-217
+__device__ __forceinline__ v3 dielectricBSDF(v3 wo, v3 wi, v3 n, BSDFParam p, uint32_t mode) {  // :184-217
     if (approximateDelta(p.roughness)) return mk3(0.0f);
     const v3 h = normalize(wo + wi);
     const float hCosWo = absDot(h, wo), hCosWi = absDot(h, wi);
@@ -398,7 +411,7 @@ static __device__ __noinline__ v3 dielectricBSDF(v3 wo, v3 wi, v3 n, BSDFParam p
                            : p.baseColor * fabsf(ggx(dot(n, h), alpha) * smithG(n, wo, wi, alpha) * hCosWo * hCosWi) /
                                  denom * (1.0f - refl) * factor;
 }
-static __device__ __noinline__ float dielectricPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :219-243
+__device__ __forceinline__ float dielectricPdf(v3 wo, v3 wi, v3 n, BSDFParam p) {  // :219-243
     if (approximateDelta(p.roughness)) return 0.0f;
     const float alpha = p.roughness * p.roughness;
     if (sameHemisphere(n, wo, wi)) {
@@ -414,7 +427,7 @@ static __device__ __noinline__ float dielectricPdf(v3 wo, v3 wi, v3 n, BSDFParam
     const float dHdWi = absDot(h, wi) / sq(dot(h, wo) + eta * dot(h, wi));
     return ggx(dot(n, h), alpha) * dHdWi * trans;
 }
-static __device__ __noinline__ BSDFSample dielectricSample(v3 n, v3 wo, BSDFParam p, uint32_t mode, v3 u) {  // :245-325
+__device__ __forceinline__ BSDFSample dielectricSample(v3 n, v3 wo, BSDFParam p, uint32_t mode, v3 u) {  // :245-325
     float ior = p.ior;
     if (approximateDelta(p.roughness)) {
         const float refl = fresnelDielectric(dot(n, wo), ior);
@@ -459,7 +472,7 @@ static __device__ __noinline__ BSDFSample dielectricSample(v3 n, v3 wo, BSDFPara
     if (zisnan(pdf)) pdf = 0.0f;
     return makeSample(wi, pdf, t * factor, kGlosTrans);
 }
-static __device__ __noinline__ BSDFSample thinDielectricSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :327-340
+__device__ __forceinline__ BSDFSample thinDielectricSample(v3 n, v3 wo, BSDFParam p, v3 u) {  // :327-340
     if (dot(n, wo) < 0.0f) n = -n;
     float refl = fresnelDielectric(dot(n, wo), p.ior);
     float trans = 1.0f - refl;
@@ -471,18 +484,48 @@ static __device__ __noinline__ BSDFSample thinDielectricSample(v3 n, v3 wo, BSDF
                         : makeSample(-wo, 1.0f, p.baseColor, kSpecTrans);
 }
 
+// One out-of-line entry per query for every material type but Lambertian
+// (principled, metal workflow, dielectric, thin dielectric): each integrator
+// call site holds one call, which keeps the kernels' instruction footprint
+// small.
+static __device__ __noinline__ v3 bsdfCall(uint32_t type, v3 wo, v3 wi, v3 n, BSDFParam p, uint32_t mode) {
+    if (type == kPrincipled) return principledBRDF(wo, wi, n, p);
+    if (type == kMetalWorkflow) return metalWorkflowBSDF(wo, wi, n, p);
+    if (type == kDielectric) return dielectricBSDF(wo, wi, n, p, mode);
+    return mk3(0.0f);  // thin dielectric: delta lobes only
+}
+static __device__ __noinline__ float pdfCall(uint32_t type, v3 wo, v3 wi, v3 n, BSDFParam p) {
+    if (type == kPrincipled) return principledBRDFPdf(wo, wi, n, p);
+    if (type == kMetalWorkflow) return metalWorkflowPdf(wo, wi, n, p);
+    if (type == kDielectric) return dielectricPdf(wo, wi, n, p);
+    return 0.0f;
+}
+static __device__ __noinline__ BSDFSample sampleCall(uint32_t type, v3 n, v3 wo, BSDFParam p, uint32_t mode, v3 u,
+                                                     float ur) {
+    if (type == kPrincipled) return principledBRDFSample(n, wo, p, u, ur);
+    if (type == kMetalWorkflow) return metalWorkflowSample(n, wo, p, u);
+    if (type == kDielectric) return dielectricSample(n, wo, p, mode, u);
+    return thinDielectricSample(n, wo, p, u);
+}
+
 // ----------------------------------------------------- material_loader.glsl
 __device__ __forceinline__ uint32_t loadMaterialType(const DeviceScene& sc, int matId) {
     return (uint32_t)__float_as_int(__ldg(&sc.materials[4 * matId + 3]).y);
 }
+// FULL = false: the scene holds Lambertian and principled materials only (the
+// integrator kernels are instantiated for both cases and the host picks the
+// lean one when it can; the dispatch for the other three types costs the
+// lean scenes 6-16% otherwise).
+template <bool FULL>
 __device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_t type, int matId) {
     const float4 m0 = __ldg(&sc.materials[4 * matId + 0]);
     BSDFParam p;
     p.baseColor = mk3(m0.x, m0.y, m0.z);
     p.subsurface = p.metallic = p.roughness = p.specular = p.specularTint = 0.0f;
     p.sheen = p.sheenTint = p.clearcoat = p.clearcoatGloss = 0.0f;
-    p.ior = 0.0f;
-    if (type == kMetalWorkflow) {  // loadMetalWorkflow (material_loader.glsl:26-35)
+    if (!FULL) {
+        // (the principled branch below)
+    } else if (type == kMetalWorkflow) {  // loadMetalWorkflow (material_loader.glsl:26-35)
         p.roughness = mixf(0.0134f, 1.0f, m0.w);
         p.metallic = __ldg(&sc.materials[4 * matId + 1]).y;
     } else if (type == kDielectric) {  // loadDielectric (:60-69): roughness not remapped
@@ -490,7 +533,8 @@ __device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_
         p.ior = __ldg(&sc.materials[4 * matId + 3]).x;
     } else if (type == kThinDielectric) {  // loadThinDielectric (:71-79)
         p.ior = __ldg(&sc.materials[4 * matId + 3]).x;
-    } else if (type == kPrincipled) {  // loadPrincipledBRDF (material_loader.glsl:37-58)
+    }
+    if (type == kPrincipled) {  // loadPrincipledBRDF (material_loader.glsl:37-58)
         const float4 m1 = __ldg(&sc.materials[4 * matId + 1]);
         const float4 m2 = __ldg(&sc.materials[4 * matId + 2]);
         p.roughness = mixf(0.0134f, 1.0f, m0.w);
@@ -507,27 +551,37 @@ __device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_
 }
 // materialBSDF / materialPdf / materialSample (material_loader.glsl:97-170);
 // `mode` is kRadiance for camera paths and kImportance for light paths.
+template <bool FULL>
 __device__ __forceinline__ v3 materialBSDF(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n,
                                            uint32_t mode = kRadiance) {
-    if (type == kPrincipled) return principledBRDF(wo, wi, n, p);
-    if (type == kMetalWorkflow) return metalWorkflowBSDF(wo, wi, n, p);
-    if (type == kDielectric) return dielectricBSDF(wo, wi, n, p, mode);
-    if (type == kThinDielectric) return mk3(0.0f);
+    if (FULL) {
+        if (type != kLambertian) return bsdfCall(type, wo, wi, n, p, mode);
+    } else if (type == kPrincipled) {
+        return principledBRDFCall(wo, wi, n, p);
+    }
     return p.baseColor * kPiInv;
 }
+template <bool FULL>
 __device__ __forceinline__ float materialPdf(uint32_t type, const BSDFParam& p, v3 wo, v3 wi, v3 n) {
-    if (type == kPrincipled) return principledBRDFPdf(wo, wi, n, p);
-    if (type == kMetalWorkflow) return metalWorkflowPdf(wo, wi, n, p);
-    if (type == kDielectric) return dielectricPdf(wo, wi, n, p);
-    if (type == kThinDielectric) return 0.0f;
+    if (FULL) {
+        if (type != kLambertian) return pdfCall(type, wo, wi, n, p);
+    } else if (type == kPrincipled) {
+        return principledBRDFPdfCall(wo, wi, n, p);
+    }
     return satDot(wi, n) * kPiInv;
 }
+template <bool FULL>
 __device__ __forceinline__ BSDFSample materialSample(uint32_t type, const BSDFParam& p, v3 n, v3 wo, v3 u,
                                                      Sampler& g, uint32_t mode = kRadiance) {
-    if (type == kPrincipled) return principledBRDFSample(n, wo, p, u, g);
-    if (type == kMetalWorkflow) return metalWorkflowSample(n, wo, p, u);
-    if (type == kDielectric) return dielectricSample(n, wo, p, mode, u);
-    if (type == kThinDielectric) return thinDielectricSample(n, wo, p, u);
+    if (FULL) {
+        if (type != kLambertian) {
+            // only the principled lobe pick draws from the rand() stream
+            const float ur = (type == kPrincipled) ? rand01(g) : 0.0f;
+            return sampleCall(type, n, wo, p, mode, u, ur);
+        }
+    } else if (type == kPrincipled) {
+        return principledBRDFSample(n, wo, p, u, rand01(g));
+    }
     BSDFSample r;  // lambertianSample (material.glsl:78-83)
     float pdf;
     r.wi = sampleCosineWeighted(n, mk2(u.y, u.z), pdf);
