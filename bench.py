@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--render", default="cornell,city,batch,diff", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
     ap.add_argument("--no-traversal", action="store_true", help="skip the traversal workload (profiling)")
+    ap.add_argument("--no-host-build", action="store_true", help="skip timing the host MTBVH builder")
     ap.add_argument("--diff-size", type=int, default=512, help="film side of the differentiable workload")
     ap.add_argument("--diff-spp", type=int, default=32, help="samples per pixel of the differentiable workload")
     ap.add_argument("--batch-requests", type=int, default=64, help="requests of the batched workload")
@@ -207,12 +208,12 @@ def run_ours(args):
     specs = []  # (name, acc, o, d, tmax, query)
     scenes = []
     t_setup = time.time()
+    bvh_build = {}
     for N in sizes:
         v, idx = build_scene(N)
-        t0 = time.time()
-        acc = BVH(v, idx).build()
+        acc, bvh_build[f"{N >> 20}M"] = time_bvh_build(v, idx, dev, stream, host=not args.no_host_build)
         acc.set_trace_schedule(args.schedule)
-        log(f"[bench] N={N}: build+upload {time.time() - t0:.1f}s, {acc.node_count} nodes")
+        log(f"[bench] N={N}: {bvh_build[f'{N >> 20}M']}")
         to = torch.from_numpy(o_p).to(dev)
         td = torch.from_numpy(d_p).to(dev)
         hid, ht = acc.trace_closest(to, td, stream=stream)
@@ -385,7 +386,7 @@ def run_ours(args):
                        "triangles": sizes, "rays_per_launch": nray, "launches_per_step": len(specs),
                        "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write); inputs > L2"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": len(specs) * args.steps,
-            "clocks": clk.summary(), "workloads": workloads, "render": render}
+            "clocks": clk.summary(), "workloads": workloads, "bvh_build": bvh_build, "render": render}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -397,6 +398,40 @@ def run_ours(args):
 # --------------------------------------------------------------------------
 # render workloads (secondary metrics): samples/s of the integrators
 # --------------------------------------------------------------------------
+def time_bvh_build(v, idx, dev, stream, host=True):
+    """MTBVH construction of one traversal mesh: the CUDA builder from
+    device-resident arrays (best of 3 after a warm-up build), from pageable
+    host arrays (copies included), and the host builder on every core.  The
+    accelerator returned for tracing is a device-built one (bit-identical)."""
+    import torch
+
+    from zillumgl_gb300 import BVH
+
+    tv = torch.from_numpy(v).to(dev)
+    ti = torch.from_numpy(idx.view(np.int32)).to(dev)
+    torch.cuda.synchronize(dev)
+    BVH(tv, ti).build_device(stream=stream).close()
+    dev_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        a = BVH(tv, ti).build_device(stream=stream)
+        dev_ms.append((time.perf_counter() - t0) * 1e3)
+        a.close()
+    del tv, ti
+    t0 = time.perf_counter()
+    acc = BVH(v, idx).build_device(stream=stream)
+    from_host = (time.perf_counter() - t0) * 1e3
+    out = {"triangles": int(idx.size // 3), "device_ms": round(min(dev_ms), 2),
+           "device_from_host_arrays_ms": round(from_host, 2)}
+    if host:
+        t0 = time.perf_counter()
+        BVH(v, idx).build_host()
+        out["host_ms"] = round((time.perf_counter() - t0) * 1e3, 1)
+        out["host_threads"] = os.cpu_count()
+        out["device_speedup"] = round(out["host_ms"] / out["device_ms"], 1)
+    return acc, out
+
+
 def run_render(args, stream, dev):
     """samples/s of one progressive pass of each integrator (CUDA events over
     `--render-passes` passes after one warm-up pass)."""

@@ -65,6 +65,22 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices,
                            const uint32_t* indices, size_t n_triangles,
                            zgl_accel** out);
 
+/* The same accelerator built by CUDA kernels on the current device: tree,
+ * threaded tables and triangle records are bit-identical to
+ * zgl_accel_build's (BVH::quickBuild + BVH::buildHitTable,
+ * src/accelerator/BVH.cpp:217-345).  `vertices` / `indices` may be device
+ * pointers, page-locked host pointers (read in place) or pageable host
+ * memory (copied first).  Nodes with fewer than `small_threshold` triangles
+ * are built one warp per subtree (0 = default 512; valid 0..4096, values
+ * below 8 act as 8); the result does not depend on it.  Synchronous; the
+ * work is ordered on `stream`.  Out-of-range indices and vertex components
+ * that are NaN, infinite or beyond +-1e8 give ZGL_ERR_INVALID_ARG (the same
+ * checks as zgl_accel_build). */
+zgl_status zgl_accel_build_device(const float* vertices, size_t n_vertices,
+                                  const uint32_t* indices, size_t n_triangles,
+                                  int32_t small_threshold, void* stream,
+                                  zgl_accel** out);
+
 /* Number of BVH nodes M = 2*n_triangles - 1 (0 for an empty accelerator).
  * The reference keeps it as Scene::boxCount / uBvhSize
  * (src/core/Scene.cpp:267, src/integrator/NaivePath.cpp:43). */

@@ -19,6 +19,22 @@ def _both(v, idx):
     return pb, (ob, oh, osz)
 
 
+def _signed_zero_grid(n=40, seed=3):
+    """A height field whose coordinates hold many -0.0 / +0.0 values."""
+    rng = np.random.default_rng(seed)
+    xs, ys = np.meshgrid(np.linspace(-1, 1, n), np.linspace(-1, 1, n))
+    z = np.where(rng.random(xs.shape) < 0.5, 0.0, 0.3 * rng.random(xs.shape))
+    v = np.stack([xs.ravel(), ys.ravel(), z.ravel()], 1).astype(np.float32)
+    zero = v == 0
+    v[zero & (rng.random(v.shape) < 0.5)] = np.float32(-0.0)
+    q = []
+    for j in range(n - 1):
+        for i in range(n - 1):
+            a = j * n + i
+            q += [a, a + 1, a + n, a + 1, a + n + 1, a + n]
+    return v, np.array(q, np.uint32)
+
+
 def _cases():
     rng = np.random.default_rng(7)
     yield "soup_2k", *triangle_soup(2000, 11)
@@ -46,6 +62,7 @@ def _cases():
     # negative zeros and coincident coordinates
     v = np.array([[-0.0, 0, 0], [0.0, 1, 0], [1, -0.0, 0], [0, 0, -0.0], [0, 0, 0.0], [1, 1, 1]], np.float32)
     yield "signed_zero", v, np.array([0, 1, 2, 3, 4, 5, 1, 2, 3, 0, 4, 5], np.uint32)
+    yield ("signed_zero_grid", *_signed_zero_grid())
 
 
 @pytest.mark.parametrize("name,v,idx", list(_cases()), ids=lambda x: x if isinstance(x, str) else "")
@@ -91,3 +108,11 @@ def test_face_order_follows_centroid_comparison():
     v = np.array([[0, 0, 0], [0.1, 0, 0], [0, 0.1, 0], [5, 0, 0], [5.1, 0, 0], [5, 0.1, 0]], np.float32)
     _, hit, _ = oracle.bvh_build(v, np.arange(6, dtype=np.uint32))
     assert hit[0, 1, 1] == 1 and hit[1, 1, 1] == 0
+
+
+def test_signed_zero_bounds_are_exercised():
+    v, idx = _signed_zero_grid()
+    ob, _, _ = oracle.bvh_build(v, idx)
+    neg = np.signbit(ob) & (ob == 0)
+    pos = ~np.signbit(ob) & (ob == 0)
+    assert neg.sum() > 10 and pos.sum() > 10

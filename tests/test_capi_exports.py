@@ -51,3 +51,13 @@ def test_invalid_arguments_return_status_not_abort(zgl_lib):
     bad[1, 1] = np.nan
     with pytest.raises(ZglError):
         BVH(bad, np.array([0, 1, 2], np.uint32)).build_host()
+    # beyond quickBuild's default box (+-1e8) and infinite coordinates
+    for x in (2e8, -np.inf):
+        bad = v.copy()
+        bad[2, 0] = x
+        with pytest.raises(ZglError) as e:
+            BVH(bad, np.array([0, 1, 2], np.uint32)).build_host()
+        assert "1e8" in str(e.value)
+    edge = v.copy()
+    edge[2] = (1e8, -1e8, 0.5)
+    assert BVH(edge, np.array([0, 1, 2], np.uint32)).build_host().bounds.shape == (1, 6)

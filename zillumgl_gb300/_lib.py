@@ -45,6 +45,8 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_version": (C.c_int32, []),
     "zgl_last_error": (C.c_char_p, []),
     "zgl_accel_build": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "zgl_accel_build_device": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int32, C.c_void_p,
+                                           C.POINTER(C.c_void_p)]),
     "zgl_accel_node_count": (C.c_int32, [C.c_void_p, c_size_t_p]),
     "zgl_accel_export": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_accel_destroy": (C.c_int32, [C.c_void_p]),

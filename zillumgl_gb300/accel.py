@@ -166,13 +166,53 @@ class Accelerator:
 
 
 class BVH:
-    """``BVH(vertices, indices).build()`` (src/accelerator/BVH.h:26-47)."""
+    """``BVH(vertices, indices).build()`` (src/accelerator/BVH.h:26-47).
+
+    ``build()`` constructs the tree on the host, ``build_device()`` with CUDA
+    kernels; both give the identical PackedBVH.  Vertices and indices may be
+    numpy arrays or (for ``build_device``) CUDA tensors: float32 (n, 3) and
+    int32/uint32 (m*3,)."""
 
     def __init__(self, vertices, indices):
-        self.vertices = np.ascontiguousarray(np.asarray(vertices, dtype=np.float32).reshape(-1, 3))
-        self.indices = np.ascontiguousarray(np.asarray(indices, dtype=np.uint32).reshape(-1))
-        if self.indices.size % 3:
+        if _is_torch(vertices) and vertices.is_cuda:
+            self._dev = (vertices.reshape(-1, 3).contiguous(), indices.reshape(-1).contiguous())
+            index_types = {torch.int32, getattr(torch, "uint32", torch.int32)}
+            if self._dev[0].dtype != torch.float32 or self._dev[1].dtype not in index_types:
+                raise ValueError("device vertices must be float32 and indices int32/uint32")
+            if self._dev[1].numel() % 3:
+                raise ValueError("indices must hold 3 entries per triangle")
+            self._vertices = None
+            self._indices = None
+            return
+        self._dev = None
+        self._vertices = np.ascontiguousarray(np.asarray(vertices, dtype=np.float32).reshape(-1, 3))
+        self._indices = np.ascontiguousarray(np.asarray(indices, dtype=np.uint32).reshape(-1))
+        if self._indices.size % 3:
             raise ValueError("indices must hold 3 entries per triangle")
+
+    @property
+    def vertices(self) -> np.ndarray:
+        if self._vertices is None:
+            self._vertices = self._dev[0].cpu().numpy()
+        return self._vertices
+
+    @property
+    def indices(self) -> np.ndarray:
+        if self._indices is None:
+            self._indices = self._dev[1].cpu().numpy().view(np.uint32)
+        return self._indices
+
+    def build_device(self, small_threshold: int = 0, stream=None) -> Accelerator:
+        """The accelerator built by CUDA kernels on the current device
+        (zgl_accel_build_device); bit-identical to ``build()``."""
+        h = C.c_void_p()
+        lib()
+        v, idx = self._dev if self._dev is not None else (self._vertices, self._indices)
+        nv = v.shape[0]
+        ntri = (idx.numel() if _is_torch(idx) else idx.size) // 3
+        call("zgl_accel_build_device", _ptr(v), nv, _ptr(idx), ntri, int(small_threshold),
+             _stream_handle(stream), C.byref(h))
+        return Accelerator(h.value, ntri)
 
     def build_host(self) -> PackedBVH:
         """The PackedBVH built on the host only (no device upload)."""

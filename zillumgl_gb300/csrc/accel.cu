@@ -1,6 +1,7 @@
 // accel.cu — MTBVH upload and the closest-hit / any-hit trace kernels, plus
 // the zgl_accel_* and zgl_trace_* entry points.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -407,8 +408,53 @@ zgl_accel* accel_create(const float* vertices, const uint32_t* indices, int64_t 
     return a;
 }
 
+zgl_accel* accel_create_device(const float* vertices, int64_t nv, const uint32_t* indices, int64_t ntri,
+                               int small, cudaStream_t s) {
+    auto* a = new zgl_accel();
+    float* d_v = nullptr;
+    uint32_t* d_i = nullptr;
+    try {
+        ZGL_CUDA(cudaGetDevice(&a->device));
+        ZGL_CUDA(cudaMalloc(&a->d_counter, 256));
+        a->ntri = ntri;
+        a->M = ntri > 0 ? 2 * ntri - 1 : 0;
+        a->device_built = true;
+        if (ntri > 0) {
+            bool host = false;
+            const float* v = static_cast<const float*>(device_address(vertices, host));
+            const uint32_t* idx = static_cast<const uint32_t*>(device_address(indices, host));
+            if (!v) {
+                ZGL_CUDA(cudaMalloc(&d_v, sizeof(float) * 3 * std::max<int64_t>(nv, 1)));
+                ZGL_CUDA(cudaMemcpyAsync(d_v, vertices, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice, s));
+                v = d_v;
+            }
+            if (!idx) {
+                ZGL_CUDA(cudaMalloc(&d_i, sizeof(uint32_t) * 3 * ntri));
+                ZGL_CUDA(cudaMemcpyAsync(d_i, indices, sizeof(uint32_t) * 3 * ntri, cudaMemcpyHostToDevice, s));
+                idx = d_i;
+            }
+            ZGL_CUDA(cudaMalloc(&a->d_nodes, sizeof(float4) * 12 * a->M));
+            ZGL_CUDA(cudaMalloc(&a->d_tris, sizeof(float4) * 3 * a->ntri));
+            ZGL_CUDA(cudaMalloc(&a->d_bounds, sizeof(float) * 6 * a->M));
+            ZGL_CUDA(cudaMalloc(&a->d_hit, sizeof(int32_t) * 18 * a->M));
+            build_bvh_device(v, nv, idx, ntri, small, a->d_nodes, a->d_tris, a->d_bounds, a->d_hit, s);
+        }
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        if (d_v) cudaFree(d_v);
+        if (d_i) cudaFree(d_i);
+        accel_free(a);
+        throw;
+    }
+    if (d_v) cudaFree(d_v);
+    if (d_i) cudaFree(d_i);
+    return a;
+}
+
 void accel_free(zgl_accel* a) {
     if (!a) return;
+    if (a->d_bounds) cudaFree(a->d_bounds);
+    if (a->d_hit) cudaFree(a->d_hit);
     if (a->d_counter) cudaFree(a->d_counter);
     if (a->d_nodes) cudaFree(a->d_nodes);
     if (a->d_tris) cudaFree(a->d_tris);
@@ -432,8 +478,12 @@ static void validate_mesh(const char* fn, const float* vertices, size_t n_vertic
         if (indices[i] >= n_vertices)
             fail(ZGL_ERR_INVALID_ARG, "%s: index %zu = %u out of range (%zu vertices)", fn, i, indices[i],
                  n_vertices);
+    // NaN, infinite and |x| > 1e8 are rejected: quickBuild's default box is
+    // +-1e8 (src/accelerator/AABB.h:13) and a centroid outside it can give an
+    // empty split
     for (size_t i = 0; i < 3 * n_vertices; i++)
-        if (!(vertices[i] == vertices[i])) fail(ZGL_ERR_INVALID_ARG, "%s: vertex component %zu is NaN", fn, i);
+        if (!(std::fabs(vertices[i]) <= 1e8f))
+            fail(ZGL_ERR_INVALID_ARG, "%s: vertex component %zu is NaN, infinite or beyond +-1e8", fn, i);
 }
 
 zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices, const uint32_t* indices,
@@ -461,6 +511,25 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint3
     ZGL_API_END
 }
 
+zgl_status zgl_accel_build_device(const float* vertices, size_t n_vertices, const uint32_t* indices,
+                                  size_t n_triangles, int32_t small_threshold, void* stream, zgl_accel** out) {
+    ZGL_API_BEGIN
+    if (!out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: out is NULL");
+    *out = nullptr;
+    if (n_triangles > 0 && (!vertices || !indices))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: NULL vertex or index array");
+    if (n_triangles > (size_t)0x3fffffff)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: %zu triangles exceed the 2^30 limit", n_triangles);
+    if (n_vertices > (size_t)0x3fffffffffffll)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: too many vertices");
+    if (small_threshold < 0 || small_threshold > gpu_build_max_small())
+        fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: small_threshold %d outside [0, %d]", small_threshold,
+             gpu_build_max_small());
+    *out = accel_create_device(vertices, (int64_t)n_vertices, indices, (int64_t)n_triangles, small_threshold,
+                               static_cast<cudaStream_t>(stream));
+    ZGL_API_END
+}
+
 zgl_status zgl_accel_node_count(const zgl_accel* accel, size_t* out) {
     ZGL_API_BEGIN
     if (!accel || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_node_count: NULL argument");
@@ -473,7 +542,10 @@ zgl_status zgl_accel_export(const zgl_accel* accel, float* bounds, int32_t* hit_
     if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_export: NULL accel");
     if (accel->M > 0 && (!bounds || !hit_table))
         fail(ZGL_ERR_INVALID_ARG, "zgl_accel_export: NULL output array");
-    if (accel->M > 0) {
+    if (accel->M > 0 && accel->device_built) {
+        ZGL_CUDA(cudaMemcpy(bounds, accel->d_bounds, sizeof(float) * accel->M * 6, cudaMemcpyDeviceToHost));
+        ZGL_CUDA(cudaMemcpy(hit_table, accel->d_hit, sizeof(int32_t) * accel->M * 18, cudaMemcpyDeviceToHost));
+    } else if (accel->M > 0) {
         std::memcpy(bounds, accel->host.bounds.data(), sizeof(float) * accel->M * 6);
         std::memcpy(hit_table, accel->host.hitTable.data(), sizeof(int32_t) * accel->M * 18);
     }

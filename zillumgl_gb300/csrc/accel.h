@@ -29,6 +29,12 @@ struct zgl_accel {
     zgl::HostBVH host;
     float4* d_nodes = nullptr;  // 6*M*2
     float4* d_tris = nullptr;   // ntri*3
+    // set when the tree was built on the device: the PackedBVH arrays stay
+    // in device memory (bounds float[M*6], hit table int32[6*M*3]) and
+    // `host` is empty
+    bool device_built = false;
+    float* d_bounds = nullptr;
+    int32_t* d_hit = nullptr;
     // work counter of the persistent trace kernels (reset before each launch;
     // launches of one handle are serialised on its caller's stream)
     unsigned long long* d_counter = nullptr;
@@ -64,6 +70,18 @@ cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir
 
 // Host build + upload (throws zgl::Error) and release of an accelerator.
 zgl_accel* accel_create(const float* vertices, const uint32_t* indices, int64_t ntri);
+// Device build (bvh_build_gpu.cu); inputs may be device, page-locked or
+// pageable host arrays.  `small` = 0 selects the default subtree threshold.
+zgl_accel* accel_create_device(const float* vertices, int64_t nv, const uint32_t* indices, int64_t ntri,
+                               int small, cudaStream_t s);
+void build_bvh_device(const float* v, int64_t nv, const uint32_t* idx, int64_t ntri, int small, float4* nodes,
+                      float4* tris, float* bounds, int32_t* hit, cudaStream_t s);
+int gpu_build_default_small();
+int gpu_build_max_small();
+// Device address of p (itself for device/managed memory, the mapped address
+// of page-locked host memory) or nullptr for pageable host memory; `host`
+// tells whether p is host memory.
+void* device_address(const void* p, bool& host);
 void accel_free(zgl_accel* a);
 int host_threads();
 

@@ -404,7 +404,9 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
 
 void upload_scene(zgl_scene& s) {
     ZGL_CUDA(cudaGetDevice(&s.device));
-    s.accel = accel_create(s.vertices.data(), s.indices.data(), s.ntri);
+    // the CUDA builder: the same PackedBVH as the host builder, bit for bit
+    s.accel = accel_create_device(s.vertices.data(), (int64_t)s.vertices.size() / 3, s.indices.data(), s.ntri, 0,
+                                  0);
     std::vector<float4> shade((size_t)s.ntri * 5);
     for (int64_t t = 0; t < s.ntri; t++) {
         auto P = [&](int j) { return &s.vertices[3 * (size_t)s.indices[3 * t + j]]; };
