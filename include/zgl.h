@@ -194,6 +194,17 @@ typedef struct zgl_scene_desc {
     float cam_focal_dist;
     int32_t film_width, film_height;
     int32_t sampler;                /* 0 independent (rand), 1 sobol */
+    /* Albedo textures (material_loader.glsl:8-17, Texture.cpp:134-171): a
+     * triangle whose obj_mat_tex has tex = mat_tex >> 16 != -1 takes its
+     * base colour from texture `tex` at the interpolated texcoord instead of
+     * from its material.  obj_texcoords: float[obj_n_vertices*2] (NULL = all
+     * zero).  tex_size: int32[n_textures*2] (width, height).  tex_rgb: the
+     * images' 8-bit sRGB RGB texels concatenated, each row-major with its
+     * top row first (stb_image order, no flip). */
+    const float* obj_texcoords;
+    int32_t n_textures;
+    const int32_t* tex_size;
+    const uint8_t* tex_rgb;
 } zgl_scene_desc;
 
 enum { ZGL_SCENE_HOST_ONLY = 1 };
@@ -211,12 +222,14 @@ zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene
  *   "noise" float[filmW*filmH*2], "pixel_seeds" uint32[filmW*filmH*2],
  *   "camera" float[19] (front, right, up, inverse camera matrix column-major,
  *   tan(fov/2)), "scalars" float[4] (lightSum, envSum as used by the shaders,
- *   objPrimCount, nLightTriangles), "info" int64[10] (film width, film
+ *   objPrimCount, nLightTriangles), "info" int64[11] (film width, film
  *   height, vertices, object vertices, triangles, object triangles, light
- *   triangles, materials, environment width, environment height), the
+ *   triangles, materials, environment width, environment height, textures), the
  *   flattened "vertices" and "normals"
- *   float[nv*3], "indices" uint32[ntri*3], "mat_tex" int32[objPrimCount] and
- *   "materials" float[nmat*16]. */
+ *   float[nv*3], "indices" uint32[ntri*3], "mat_tex" int32[objPrimCount],
+ *   "materials" float[nmat*16], "tex_scale" float[n_textures*2] (image size /
+ *   largest image size, Texture.cpp:163-170) and "srgb_lut" float[256] (the
+ *   linear value of each 8-bit sRGB code). */
 zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out, size_t bytes);
 
 /* Scene::load (src/core/Scene.cpp:58-127) + createGLContext: read a scene XML

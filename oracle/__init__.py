@@ -120,7 +120,24 @@ class OrcScene(C.Structure):
         ("camAsp", C.c_float), ("filmW", C.c_int32), ("filmH", C.c_int32),
         ("maxDepth", C.c_int32), ("russianRoulette", C.c_int32), ("sampleLight", C.c_int32),
         ("lightEnvUniformSample", C.c_int32), ("lightPortion", C.c_float), ("rrStartDepth", C.c_int32),
+        ("texCoords", C.c_void_p), ("nTextures", C.c_int32), ("texMaxW", C.c_int32), ("texMaxH", C.c_int32),
+        ("texLayers", C.c_void_p), ("texScale", C.c_void_p),
     ]
+
+
+def texture_layers(textures):
+    """Texture2DArray (Texture.cpp:134-171): (layers uint8 (n, Hmax, Wmax, 3)
+    with each image in the top-left corner, uv scales float32 (n, 2))."""
+    if not textures:
+        return None, None
+    wmax = max(t.shape[1] for t in textures)
+    hmax = max(t.shape[0] for t in textures)
+    layers = np.zeros((len(textures), hmax, wmax, 3), np.uint8)
+    scale = np.zeros((len(textures), 2), np.float32)
+    for k, t in enumerate(textures):
+        layers[k, :t.shape[0], :t.shape[1]] = t
+        scale[k] = (np.float32(t.shape[1]) / np.float32(wmax), np.float32(t.shape[0]) / np.float32(hmax))
+    return layers, scale
 
 
 def _render_lib():
@@ -148,6 +165,8 @@ def _render_lib():
         L.orc_transc.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.orc_postprocess.restype = None
         L.orc_postprocess.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p]
+        L.orc_texture_sample.restype = None
+        L.orc_texture_sample.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]
         L.orc_diff_grad.restype = None
         L.orc_diff_grad.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                     C.c_int32, C.c_void_p, C.c_int32]
@@ -274,6 +293,16 @@ class OracleScene:
         s.lensRadius, s.focalDist = data.cam_lens_radius, data.cam_focal_dist
         s.filmW, s.filmH = W, H
         s.camAsp = float(np.float32(W) / np.float32(H))
+        textures = getattr(data, "textures", None)
+        if textures:
+            self.tex_layers, self.tex_scale = texture_layers(textures)
+            tc = getattr(data, "obj_texcoords", None)
+            nvo = np.asarray(data.obj_vertices).reshape(-1, 3).shape[0]
+            self.texcoords = (np.zeros((nvo, 2), np.float32) if tc is None
+                              else np.ascontiguousarray(np.asarray(tc, np.float32).reshape(-1, 2)))
+            s.texCoords, s.texLayers, s.texScale = _p(self.texcoords), _p(self.tex_layers), _p(self.tex_scale)
+            s.nTextures = len(textures)
+            s.texMaxH, s.texMaxW = self.tex_layers.shape[1], self.tex_layers.shape[2]
         p = params or {}
         s.maxDepth = p.get("max_depth", 4)
         s.russianRoulette = p.get("russian_roulette", 0)
@@ -282,6 +311,13 @@ class OracleScene:
         s.lightPortion = p.get("light_portion", 0.5)
         s.rrStartDepth = p.get("rr_start_depth", 1)
         self.s = s
+
+    def texture_sample(self, tex_id, uv):
+        """The albedo texture lookup at texcoords uv (n, 2) -> rgb (n, 3)."""
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        out = np.zeros((uv.shape[0], 3), np.float32)
+        _render_lib().orc_texture_sample(C.byref(self.s), int(tex_id), _p(uv), uv.shape[0], _p(out))
+        return out
 
     def render_pt(self, pixels, passes, spp0=0, fc0=1, nthreads=None):
         """Sum of `passes` progressive passes for the pixel indices (y * W + x)."""

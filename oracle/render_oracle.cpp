@@ -71,6 +71,13 @@ struct OrcScene {
     int32_t lightEnvUniformSample;
     float lightPortion;
     int32_t rrStartDepth;  // Russian roulette from this bounce on (1 = the reference)
+    // albedo textures (Texture.cpp:134-171): per object vertex texcoords;
+    // nTextures layers of texMaxW x texMaxH 8-bit sRGB RGB texels (each image
+    // in the top-left corner, zero elsewhere) and the uv scale of each
+    const float* texCoords;     // objVertices*2, NULL when nTextures == 0
+    int32_t nTextures, texMaxW, texMaxH;
+    const uint8_t* texLayers;   // nTextures*texMaxH*texMaxW*3
+    const float* texScale;      // nTextures*2
 };
 
 }  // extern "C"
@@ -583,6 +590,44 @@ inline uint32_t loadMaterialType(const OrcScene& sc, int matId) {
     std::memcpy(&t, &sc.materials[16 * matId + 13], 4);
     return (uint32_t)t;
 }
+// sRGB code -> linear (GL_SRGB decode), in double, rounded once to float
+const float* srgbTable() {
+    static float lut[256];
+    static bool init = false;
+    if (!init) {
+        for (int i = 0; i < 256; i++) {
+            double c = i / 255.0;
+            lut[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        init = true;
+    }
+    return lut;
+}
+
+// texture2DArray(uTextures, vec3(fract(uv) * uvScale, texId)).rgb
+// (material_loader.glsl:14-15): level 0 with GL_LINEAR magnification,
+// GL_REPEAT over the layer, sRGB decoded per texel, then the bilinear blend
+// (1-a)(1-b) T00 + a(1-b) T10 + (1-a) b T01 + a b T11 in float32.
+vec3 albedoTexture(const OrcScene& sc, int texId, vec2 uv) {
+    const float* lut = srgbTable();
+    const float s = (uv.x - std::floor(uv.x)) * sc.texScale[2 * texId];
+    const float t = (uv.y - std::floor(uv.y)) * sc.texScale[2 * texId + 1];
+    const int W = sc.texMaxW, H = sc.texMaxH;
+    const float u = s * (float)W - 0.5f, v = t * (float)H - 0.5f;
+    const float a = u - std::floor(u), b = v - std::floor(v);
+    auto wrap = [](int i, int n) { return ((i % n) + n) % n; };
+    const int i0 = wrap((int)std::floor(u), W), j0 = wrap((int)std::floor(v), H);
+    const int i1 = wrap(i0 + 1, W), j1 = wrap(j0 + 1, H);
+    auto T = [&](int i, int j, int c) {
+        return lut[sc.texLayers[(((size_t)texId * H + j) * W + i) * 3 + c]];
+    };
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    float c3[3];
+    for (int c = 0; c < 3; c++)
+        c3[c] = w00 * T(i0, j0, c) + w10 * T(i1, j0, c) + w01 * T(i0, j1, c) + w11 * T(i1, j1, c);
+    return vec3(c3[0], c3[1], c3[2]);
+}
+
 inline BSDFParam loadMaterial(const OrcScene& sc, uint32_t type, int matId) {  // :81-97
     const float* m = sc.materials + 16 * matId;
     BSDFParam p;
@@ -643,8 +688,9 @@ inline vec3 N(const OrcScene& sc, uint32_t i) { return vec3(sc.normals[3 * i], s
 
 struct SurfaceInfo {
     vec3 ns, ng;
+    vec2 uv;
 };
-inline SurfaceInfo triangleSurfaceInfo(const OrcScene& sc, int id, vec3 p) {  // :188-224 (uv unused)
+inline SurfaceInfo triangleSurfaceInfo(const OrcScene& sc, int id, vec3 p) {  // :188-224
     uint32_t ia = sc.indices[3 * id], ib = sc.indices[3 * id + 1], ic = sc.indices[3 * id + 2];
     vec3 a = V(sc, ia), b = V(sc, ib), c = V(sc, ic);
     vec3 na = N(sc, ia), nb = N(sc, ib), nc = N(sc, ic);
@@ -656,8 +702,19 @@ inline SurfaceInfo triangleSurfaceInfo(const OrcScene& sc, int id, vec3 p) {  //
     SurfaceInfo s;
     s.ns = normalize(na * la + nb * lb + nc * lc);
     s.ng = normalize(cross(pa, pb));
+    s.uv = vec2(0.0f, 0.0f);
+    if (sc.texCoords && id < sc.objPrimCount) {
+        const float* T = sc.texCoords;
+        s.uv = vec2(T[2 * ia] * la + T[2 * ib] * lb + T[2 * ic] * lc,
+                    T[2 * ia + 1] * la + T[2 * ib + 1] * lb + T[2 * ic + 1] * lc);
+    }
     if (dot(s.ns, s.ng) < 0.0f) s.ng = -s.ng;
     return s;
+}
+// the base colour of a textured triangle (matTex >> 16 != -1)
+inline void applyTexture(const OrcScene& sc, int matTexId, const SurfaceInfo& surf, BSDFParam& p) {
+    const int texId = matTexId >> 16;
+    if (texId != -1) p.baseColor = albedoTexture(sc, texId, surf.uv);
 }
 inline float triangleArea(const OrcScene& sc, int id) {
     return triangleArea(V(sc, sc.indices[3 * id]), V(sc, sc.indices[3 * id + 1]), V(sc, sc.indices[3 * id + 2]));
@@ -858,6 +915,7 @@ vec3 pathIntegTrace(const OrcScene& sc, Ray ray, int& s, Rng& g) {  // :35-143
             }
         }
         BSDFParam mp = loadMaterial(sc, matType, matId);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp);
         if (sc.sampleLight) {
             float ud = sample1D(sc, g, s);
             float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
@@ -1035,6 +1093,7 @@ inline void loadSurface(const OrcScene& sc, int id, vec3 pos, vec3 wo, SurfaceIn
         surf.ng = -surf.ng;
     }
     mp = loadMaterial(sc, matType, matId);
+    applyTexture(sc, sc.matTexIndex[id], surf, mp);
 }
 
 // lightIntegTrace (light_path_integ.glsl:45-146); rand() stream only.
@@ -1135,6 +1194,7 @@ vec3 traceCameraPath(const OrcScene& sc, Ray ray, Rng& g, int& s) {
             surf.ng = -surf.ng;
         }
         BSDFParam mp = loadMaterial(sc, matType, matId);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp);
         {
             float a0 = sample1D(sc, g, s), a1 = sample1D(sc, g, s);
             int light = lightSampleOne(sc, vec2(a0, a1));
@@ -1247,6 +1307,7 @@ void traceLightPath(const OrcScene& sc, Rng& g, float* film, float uScale) {
         s0t1 /= coefToPos;
         s1t1 /= coefToPos / (bounce == 1 ? remap(dist * dist) : 1.0f);
         BSDFParam mp = loadMaterial(sc, matType, matId);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp);
         {
             float c0 = rand01(g), c1 = rand01(g);
             CameraIiSample ci = thinLensCameraSampleIi(sc, pos, vec2(c0, c1));
@@ -1418,17 +1479,27 @@ D3 principledD(const float* m, const double* q, D3 wo, D3 wi, D3 n) {
 }
 
 // out[i][c] = (d f_c / d q_i) / f_c for the BSDF value of material matId.
-void bsdfLogGrad(const OrcScene& sc, int matId, vec3 wo, vec3 wi, vec3 n, double out[6][3]) {
+// A textured triangle (tex != nullptr: its texture colour) has no base
+// colour parameter: those entries stay zero and the others are taken at the
+// texture colour.
+void bsdfLogGrad(const OrcScene& sc, int matId, vec3 wo, vec3 wi, vec3 n, double out[6][3],
+                 const vec3* tex = nullptr) {
     const float* m = sc.materials + 16 * matId;
     for (int i = 0; i < 6; i++) out[i][0] = out[i][1] = out[i][2] = 0.0;
     const uint32_t type = loadMaterialType(sc, matId);
     if (type != PrincipledBRDF && type != Lambertian) return;  // no differentiable parameters
     if (type == Lambertian) {
-        for (int c = 0; c < 3; c++) out[c][c] = m[c] != 0.0f ? 1.0 / (double)m[c] : 0.0;
+        if (!tex)
+            for (int c = 0; c < 3; c++) out[c][c] = m[c] != 0.0f ? 1.0 / (double)m[c] : 0.0;
         return;
     }
     const D3 o = d3(wo), i3 = d3(wi), nn = d3(n);
     double q[6] = {m[0], m[1], m[2], m[3], m[5], m[6]};
+    if (tex) {
+        q[0] = tex->x;
+        q[1] = tex->y;
+        q[2] = tex->z;
+    }
     const D3 f = principledD(m, q, o, i3, nn);
     const double fv[3] = {f.x, f.y, f.z};
     for (int i = 0; i < 6; i++) {
@@ -1441,6 +1512,8 @@ void bsdfLogGrad(const OrcScene& sc, int matId, vec3 wo, vec3 wi, vec3 n, double
         const double dv[3] = {(fp.x - fmn.x) / (2 * h), (fp.y - fmn.y) / (2 * h), (fp.z - fmn.z) / (2 * h)};
         for (int c = 0; c < 3; c++) out[i][c] = fv[c] != 0.0 ? dv[c] / fv[c] : 0.0;
     }
+    if (tex)
+        for (int i = 0; i < 3; i++) out[i][0] = out[i][1] = out[i][2] = 0.0;
 }
 
 struct AdjCtx {
@@ -1496,6 +1569,9 @@ void pathAdjoint(const OrcScene& sc, Ray ray, int& s, Rng& g, AdjCtx& cx) {
             surf.ng = -surf.ng;
         }
         BSDFParam mp = loadMaterial(sc, matType, matId);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp);
+        vec3 texC = mp.baseColor;
+        const vec3* texColor = (sc.matTexIndex[id] >> 16) != -1 ? &texC : nullptr;
         if (sc.sampleLight) {
             float ud = sample1D(sc, g, s);
             float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
@@ -1509,7 +1585,7 @@ void pathAdjoint(const OrcScene& sc, Ray ray, int& s, Rng& g, AdjCtx& cx) {
                 float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
                 float weight = biHeuristic(ls.pdf, fpdf);
                 vec3 C = f * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
-                bsdfLogGrad(sc, matId, wo, ls.wi, surf.ns, lg);
+                bsdfLogGrad(sc, matId, wo, ls.wi, surf.ns, lg, texColor);
                 addContribution(cx, C, lg, matId, lid);
             }
         }
@@ -1519,7 +1595,7 @@ void pathAdjoint(const OrcScene& sc, Ray ray, int& s, Rng& g, AdjCtx& cx) {
         float bsdfPdf = bs.pdf;
         bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
         if (bsdfPdf < 1e-8f) break;
-        bsdfLogGrad(sc, matId, wo, wi, surf.ns, lg);
+        bsdfLogGrad(sc, matId, wo, wi, surf.ns, lg, texColor);
         for (int i = 0; i < 6; i++)
             for (int c = 0; c < 3; c++) cx.A[(size_t)(6 * matId + i) * 3 + c] += lg[i][c];
         throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
@@ -1948,6 +2024,16 @@ void orc_diff_grad(const OrcScene* sc, int32_t spp, const float* dimage, const i
 // The display pass of post_proc.glsl:11-59 (the tone mappers reinhard and CE
 // are defined there but never selected): frame RGBA32F of (W/s) x (H/s)
 // texels, out RGBA32F of W x H; texels past the film read as zero.
+// albedoTexture of texture texId at n texcoords (uv float[n*2]) -> out float[n*3]
+void orc_texture_sample(const OrcScene* sc, int32_t texId, const float* uv, int64_t n, float* out) {
+    for (int64_t i = 0; i < n; i++) {
+        vec3 c = albedoTexture(*sc, texId, vec2(uv[2 * i], uv[2 * i + 1]));
+        out[3 * i] = c.x;
+        out[3 * i + 1] = c.y;
+        out[3 * i + 2] = c.z;
+    }
+}
+
 void orc_postprocess(const float* frame, int32_t W, int32_t H, int32_t s, float scale, int32_t mapper, float* out) {
     const int inW = W / s, inH = H / s;
     auto calc = [](float x) {

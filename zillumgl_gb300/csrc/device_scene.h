@@ -36,6 +36,13 @@ struct DeviceScene {
     float camMatInv[9];
     float tanFOV, lensRadius, focalDist, camAsp;
     int32_t filmW, filmH;
+    // albedo textures: per object triangle the three corner texcoords; RGBA8
+    // layers of texW x texH; per texture the uv scale; sRGB -> linear table
+    const float2* uv;
+    const uint32_t* texels;
+    const float2* texScale;
+    const float* srgb;
+    int32_t texW, texH;
 };
 
 }  // namespace zgl

@@ -68,7 +68,7 @@ __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sa
                 surf.ng = -surf.ng;
             }
         }
-        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
         if (pp.sampleLight) {
             float ud = sample1D(g);
             float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);

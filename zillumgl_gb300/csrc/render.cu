@@ -198,7 +198,7 @@ __device__ __forceinline__ void shadeSurface(const DeviceScene& sc, int id, v3 p
         surf.ns = -surf.ns;
         surf.ng = -surf.ng;
     }
-    mp = loadMaterial<FULL>(sc, matType, matId);
+    mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
 }
 
 // lightIntegTrace (light_path_integ.glsl:45-146); the light tracer forces the
@@ -305,7 +305,7 @@ __device__ v3 tripleCameraTrace(const DeviceScene& sc, const PathParams& pp, Ray
             surf.ns = -surf.ns;
             surf.ng = -surf.ng;
         }
-        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
         {
             float a0 = sample1D(g), a1 = sample1D(g);
             int light = lightSampleOne(sc, mk2(a0, a1));
@@ -422,7 +422,7 @@ __device__ void tripleLightTrace(const DeviceScene& sc, const PathParams& pp, Sa
         float coefToPos = remap(prevPdfDir * absDot(surf.ns, wo));
         s0t1 /= coefToPos;
         s1t1 /= coefToPos / (bounce == 1 ? remap(dist * dist) : 1.0f);
-        BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
+        BSDFParam mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
         {
             float c0 = rand01(g), c1 = rand01(g);
             CameraIiSample ci = thinLensCameraSampleIi(sc, pos, mk2(c0, c1));

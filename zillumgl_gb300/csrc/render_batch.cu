@@ -194,7 +194,7 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, Pa
         surf.ns = -surf.ns;
         surf.ng = -surf.ng;
     }
-    BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
+    BSDFParam mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
     if (pp.sampleLight) {
         float ud = sample1D(g);
         float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g),

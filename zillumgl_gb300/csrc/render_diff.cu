@@ -230,6 +230,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
     int bounce = 1;
     while (__any_sync(kFullMask, alive)) {
         int mkey = -1, nkey = -1, hkey = -1;
+        bool textured = false;
         float mg[kDiffMatParams], npw[3], hpw[3];
 #pragma unroll
         for (int i = 0; i < kDiffMatParams; i++) mg[i] = 0.0f;
@@ -242,11 +243,13 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 surf.ns = -surf.ns;
                 surf.ng = -surf.ng;
             }
-            const BSDFParam mp = loadMaterial<FULL>(sc, matType, matId);
+            const BSDFParam mp = loadMaterial<FULL>(sc, matType, tri.matTex, id, surf);
             // metal-workflow and dielectric materials have no differentiable
             // parameters; their vertices only carry the paths
             const bool diffMat = !FULL || matType == kLambertian || matType == kPrincipled;
             mkey = diffMat ? kDiffMatParams * matId : -1;
+            // a textured triangle's base colour is the texture's, not a parameter
+            textured = FULL && (tri.matTex >> 16) != -1;
             if (pp.sampleLight) {
                 const float ud = sample1D(g);
                 const float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
@@ -310,6 +313,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
             }
             if (++bounce > pp.maxDepth) alive = false;
         }
+        if (textured) mg[0] = mg[1] = mg[2] = 0.0f;
         warp_flush<kDiffMatParams>(sg, mkey, mg);
         warp_flush<3>(sg, nkey, npw);
         warp_flush<3>(sg, hkey, hpw);

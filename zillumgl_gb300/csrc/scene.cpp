@@ -276,6 +276,60 @@ void light_tables(zgl_scene& s) {
         fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: lights have zero total power or zero area");
 }
 
+// sRGB code -> linear value (the sRGB transfer function of GL_SRGB textures,
+// evaluated in double and rounded once to float)
+void srgb_lut(std::vector<float>& lut) {
+    lut.resize(256);
+    for (int i = 0; i < 256; i++) {
+        double c = i / 255.0;
+        lut[(size_t)i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
+}
+
+// Texture2DArray (Texture.cpp:134-171): layers of the largest width and
+// height, each image in the top-left corner of its layer (the rest zero),
+// uv scale = image size / layer size; and the object texcoords.
+void texture_tables(zgl_scene& s, const zgl_scene_desc& d) {
+    const size_t nvo = d.obj_n_vertices;
+    s.texcoords.assign(2 * nvo, 0.0f);
+    if (d.obj_texcoords) {
+        s.texcoords.assign(d.obj_texcoords, d.obj_texcoords + 2 * nvo);
+        for (float x : s.texcoords)
+            if (!std::isfinite(x)) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: texcoord not finite");
+    }
+    if (d.n_textures < 0 || d.n_textures > 0x7fff)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: %d textures (0..32767)", d.n_textures);
+    s.nTextures = d.n_textures;
+    s.texMaxW = s.texMaxH = 0;
+    s.texels.clear();
+    s.texScale.clear();
+    srgb_lut(s.srgbLut);
+    if (s.nTextures == 0) return;
+    if (!d.tex_size || !d.tex_rgb) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: textures need tex_size and tex_rgb");
+    for (int t = 0; t < s.nTextures; t++) {
+        int32_t w = d.tex_size[2 * t], h = d.tex_size[2 * t + 1];
+        if (w <= 0 || h <= 0 || w > 16384 || h > 16384)
+            fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: texture %d size %dx%d out of range", t, w, h);
+        s.texMaxW = std::max(s.texMaxW, w);
+        s.texMaxH = std::max(s.texMaxH, h);
+    }
+    const size_t layer = (size_t)s.texMaxW * s.texMaxH;
+    if (layer * (size_t)s.nTextures > ((size_t)1 << 31))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: texture array above 2^31 texels");
+    s.texels.assign(layer * (size_t)s.nTextures, 0u);
+    s.texScale.resize(2 * (size_t)s.nTextures);
+    const uint8_t* src = d.tex_rgb;
+    for (int t = 0; t < s.nTextures; t++) {
+        int32_t w = d.tex_size[2 * t], h = d.tex_size[2 * t + 1];
+        uint32_t* dst = &s.texels[layer * (size_t)t];
+        for (int32_t y = 0; y < h; y++)
+            for (int32_t x = 0; x < w; x++, src += 3)
+                dst[(size_t)y * s.texMaxW + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 8) | ((uint32_t)src[2] << 16);
+        s.texScale[2 * (size_t)t] = (float)w / (float)s.texMaxW;
+        s.texScale[2 * (size_t)t + 1] = (float)h / (float)s.texMaxH;
+    }
+}
+
 void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
     if (d.obj_n_triangles > 0 && (!d.obj_vertices || !d.obj_normals || !d.obj_indices || !d.obj_mat_tex))
         fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: object arrays missing");
@@ -330,11 +384,16 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
             if (!std::isfinite(s.materials[16 * m + k]))
                 fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: material %zu parameter %d is not finite", m, k);
     }
+    texture_tables(s, d);
     s.matTex.assign(d.obj_mat_tex, d.obj_mat_tex + d.obj_n_triangles);
     for (size_t t = 0; t < d.obj_n_triangles; t++) {
         int32_t mt = s.matTex[t];
         int32_t mat = mt & 0xffff, tex = mt >> 16;
-        if (tex != -1) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu uses a texture (not supported yet)", t);
+        if (tex != -1) {
+            if (tex < 0 || tex >= s.nTextures)
+                fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu uses texture %d of %d", t, tex, s.nTextures);
+            s.fullMaterials = true;
+        }
         if ((size_t)mat >= d.n_materials) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu material out of range", t);
     }
 
@@ -444,6 +503,19 @@ void upload_scene(zgl_scene& s) {
     std::vector<uint2> seeds((size_t)s.filmW * s.filmH);
     for (size_t i = 0; i < seeds.size(); i++) seeds[i] = make_uint2(s.seeds[2 * i], s.seeds[2 * i + 1]);
     s.d_seeds = upload(seeds);
+    if (s.nTextures > 0) {
+        std::vector<float2> uv((size_t)s.objPrimCount * 3);
+        for (size_t i = 0; i < uv.size(); i++) {
+            uint32_t vi = s.indices[i];
+            uv[i] = make_float2(s.texcoords[2 * (size_t)vi], s.texcoords[2 * (size_t)vi + 1]);
+        }
+        s.d_uv = upload(uv);
+        s.d_texels = upload(s.texels);
+        std::vector<float2> sc((size_t)s.nTextures);
+        for (size_t t = 0; t < sc.size(); t++) sc[t] = make_float2(s.texScale[2 * t], s.texScale[2 * t + 1]);
+        s.d_texScale = upload(sc);
+        s.d_srgb = upload(s.srgbLut);
+    }
 }
 
 }  // namespace
@@ -524,6 +596,12 @@ zgl::DeviceScene zgl_scene::view() const {
     v.camAsp = camAsp;
     v.filmW = filmW;
     v.filmH = filmH;
+    v.uv = d_uv;
+    v.texels = d_texels;
+    v.texScale = d_texScale;
+    v.srgb = d_srgb;
+    v.texW = texMaxW;
+    v.texH = texMaxH;
     return v;
 }
 
@@ -531,8 +609,13 @@ void zgl_scene::free_device() {
     zgl::accel_free(accel);
     accel = nullptr;
     for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lightPower, (void*)d_lightAlias, (void*)d_lightProb,
-                    (void*)d_env, (void*)d_envAlias, (void*)d_envProb, (void*)d_sobol, (void*)d_seeds})
+                    (void*)d_env, (void*)d_envAlias, (void*)d_envProb, (void*)d_sobol, (void*)d_seeds,
+                    (void*)d_uv, (void*)d_texels, (void*)d_texScale, (void*)d_srgb})
         if (p) cudaFree(p);
+    d_uv = nullptr;
+    d_texels = nullptr;
+    d_texScale = nullptr;
+    d_srgb = nullptr;
     d_shade = d_materials = d_lightPower = d_env = nullptr;
     d_lightAlias = d_envAlias = nullptr;
     d_lightProb = d_envProb = nullptr;
@@ -588,14 +671,17 @@ zgl_status zgl_scene_export(const zgl_scene* s, const char* table, void* out, si
         c[18] = s->tanFOV;
         give(c, sizeof(c));
     } else if (t == "info") {
-        int64_t c[10] = {s->filmW, s->filmH, (int64_t)s->vertices.size() / 3, s->nObjVertices, s->ntri,
-                         s->objPrimCount, s->nLight, (int64_t)s->materials.size() / 16, s->envW, s->envH};
+        int64_t c[11] = {s->filmW, s->filmH, (int64_t)s->vertices.size() / 3, s->nObjVertices, s->ntri,
+                         s->objPrimCount, s->nLight, (int64_t)s->materials.size() / 16, s->envW, s->envH,
+                         s->nTextures};
         give(c, sizeof(c));
     } else if (t == "vertices") give(s->vertices.data(), 4 * s->vertices.size());
     else if (t == "normals") give(s->normals.data(), 4 * s->normals.size());
     else if (t == "indices") give(s->indices.data(), 4 * s->indices.size());
     else if (t == "mat_tex") give(s->matTex.data(), 4 * s->matTex.size());
     else if (t == "materials") give(s->materials.data(), 4 * s->materials.size());
+    else if (t == "tex_scale") give(s->texScale.data(), 4 * s->texScale.size());
+    else if (t == "srgb_lut") give(s->srgbLut.data(), 4 * s->srgbLut.size());
     else if (t == "scalars") {
         float c[4] = {s->lightSum, s->envSum, (float)s->objPrimCount, (float)s->nLight};
         give(c, sizeof(c));

@@ -23,7 +23,18 @@ struct zgl_scene {
     int64_t nObjVertices = 0;
     int32_t nLight = 0;
     std::vector<float> materials;  // 16 per material
-    bool fullMaterials = false;    // some material is metal workflow, dielectric or thin dielectric
+    // some material is metal workflow, dielectric or thin dielectric, or some
+    // triangle is textured
+    bool fullMaterials = false;
+
+    // albedo textures (Texture.cpp:134-171): layers of texMaxW x texMaxH
+    // RGBA8 texels (the image in the top-left corner, zero elsewhere), the
+    // per-texture uv scale and the per-corner texcoords of object triangles
+    std::vector<float> texcoords;    // 2 per object vertex
+    int32_t nTextures = 0, texMaxW = 0, texMaxH = 0;
+    std::vector<uint32_t> texels;    // nTextures * texMaxH * texMaxW
+    std::vector<float> texScale;     // 2 per texture
+    std::vector<float> srgbLut;      // 256
 
     // lights (Scene.cpp:200-243): instance ranges and powers, then per triangle
     std::vector<uint32_t> lightFirst;   // n_instances + 1
@@ -66,6 +77,10 @@ struct zgl_scene {
     float* d_envProb = nullptr;
     uint32_t* d_sobol = nullptr;
     uint2* d_seeds = nullptr;
+    float2* d_uv = nullptr;          // 3 per object triangle
+    uint32_t* d_texels = nullptr;
+    float2* d_texScale = nullptr;
+    float* d_srgb = nullptr;
 
     zgl::DeviceScene view() const;
     void free_device();

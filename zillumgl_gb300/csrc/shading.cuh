@@ -517,7 +517,7 @@ __device__ __forceinline__ uint32_t loadMaterialType(const DeviceScene& sc, int 
 // lean one when it can; the dispatch for the other three types costs the
 // lean scenes 6-16% otherwise).
 template <bool FULL>
-__device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_t type, int matId) {
+__device__ __forceinline__ BSDFParam loadMaterialParams(const DeviceScene& sc, uint32_t type, int matId) {
     const float4 m0 = __ldg(&sc.materials[4 * matId + 0]);
     BSDFParam p;
     p.baseColor = mk3(m0.x, m0.y, m0.z);
@@ -611,6 +611,7 @@ __device__ __forceinline__ TriShade loadTri(const DeviceScene& sc, int id) {
 }
 struct Surface {
     v3 ns, ng;
+    float la, lb;  // barycentric weights of corners a and b (lc = 1 - la - lb)
 };
 __device__ __forceinline__ Surface surfaceInfo(const TriShade& t, v3 p) {  // intersection.glsl:188-224
     v3 pa = t.a - p, pb = t.b - p, pc = t.c - p;
@@ -619,10 +620,64 @@ __device__ __forceinline__ Surface surfaceInfo(const TriShade& t, v3 p) {  // in
     float lb = length(cross(pc, pa)) * areaInv;
     float lc = 1.0f - la - lb;
     Surface s;
+    s.la = la;
+    s.lb = lb;
     s.ns = normalize(t.na * la + t.nb * lb + t.nc * lc);
     s.ng = normalize(cross(pa, pb));
     if (dot(s.ns, s.ng) < 0.0f) s.ng = -s.ng;
     return s;
+}
+// texture2DArray(uTextures, vec3(fract(uv) * uvScale, texId)).rgb
+// (material_loader.glsl:14-15) on the 8-bit sRGB texture array of
+// Texture.cpp:146-161.  A compute shader samples level 0, i.e. with the
+// magnification filter (GL_LINEAR), wrapping GL_REPEAT over the whole layer;
+// texels are decoded sRGB -> linear before filtering.  The bilinear weights
+// are float32 (hardware filtering rounds them to fixed point).
+__device__ __forceinline__ v3 albedoTexture(const DeviceScene& sc, int texId, v2 uv) {
+    const float2 scale = __ldg(&sc.texScale[texId]);
+    const float s = (uv.x - floorf(uv.x)) * scale.x;
+    const float t = (uv.y - floorf(uv.y)) * scale.y;
+    const int W = sc.texW, H = sc.texH;
+    const float u = s * (float)W - 0.5f, v = t * (float)H - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    int i0 = (int)fu, j0 = (int)fv;
+    if (i0 < 0) i0 += W;
+    if (j0 < 0) j0 += H;
+    const int i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+    const uint32_t* layer = sc.texels + (size_t)texId * W * H;
+    const uint32_t t00 = __ldg(&layer[(size_t)j0 * W + i0]), t10 = __ldg(&layer[(size_t)j0 * W + i1]);
+    const uint32_t t01 = __ldg(&layer[(size_t)j1 * W + i0]), t11 = __ldg(&layer[(size_t)j1 * W + i1]);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    float c[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int sh = 8 * k;
+        c[k] = w00 * __ldg(&sc.srgb[(t00 >> sh) & 255u]) + w10 * __ldg(&sc.srgb[(t10 >> sh) & 255u]) +
+               w01 * __ldg(&sc.srgb[(t01 >> sh) & 255u]) + w11 * __ldg(&sc.srgb[(t11 >> sh) & 255u]);
+    }
+    return mk3(c[0], c[1], c[2]);
+}
+// ret.uv = ta * la + tb * lb + tc * lc (intersection.glsl:218)
+__device__ __forceinline__ v2 surfaceUV(const DeviceScene& sc, int triId, const Surface& surf) {
+    const float2 ta = __ldg(&sc.uv[3 * (size_t)triId]), tb = __ldg(&sc.uv[3 * (size_t)triId + 1]);
+    const float2 tc = __ldg(&sc.uv[3 * (size_t)triId + 2]);
+    const float lc = 1.0f - surf.la - surf.lb;
+    return mk2(ta.x * surf.la + tb.x * surf.lb + tc.x * lc, ta.y * surf.la + tb.y * surf.lb + tc.y * lc);
+}
+// loadMaterial (material_loader.glsl:81-95): the record's parameters, with
+// the base colour from the albedo texture when the triangle has one
+// (matTex >> 16 != -1; only scenes that run the full instantiation have
+// textured triangles).
+template <bool FULL>
+__device__ __forceinline__ BSDFParam loadMaterial(const DeviceScene& sc, uint32_t type, int32_t matTex, int triId,
+                                                  const Surface& surf) {
+    BSDFParam p = loadMaterialParams<FULL>(sc, type, matTex & 0x0000ffff);
+    if (FULL) {
+        const int texId = matTex >> 16;
+        if (texId != -1) p.baseColor = albedoTexture(sc, texId, surfaceUV(sc, triId, surf));
+    }
+    return p;
 }
 __device__ __forceinline__ v3 geomNormal(const DeviceScene& sc, int triId, v3 p) {
     return surfaceInfo(loadTri(sc, triId), p).ng;

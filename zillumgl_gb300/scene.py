@@ -64,6 +64,7 @@ class SceneDesc(C.Structure):
         ("cam_pos", C.c_float * 3), ("cam_angle", C.c_float * 3), ("cam_fov", C.c_float),
         ("cam_lens_radius", C.c_float), ("cam_focal_dist", C.c_float),
         ("film_width", C.c_int32), ("film_height", C.c_int32), ("sampler", C.c_int32),
+        ("obj_texcoords", C.c_void_p), ("n_textures", C.c_int32), ("tex_size", C.c_void_p), ("tex_rgb", C.c_void_p),
     ]
 
 
@@ -104,6 +105,11 @@ class SceneData:
     sampler: int = 1
     env_rgb: np.ndarray | None = None  # (H, W, 3) float32
     env_rotation: float = 0.0
+    # albedo textures: per object vertex texcoords (n, 2) and 8-bit sRGB RGB
+    # images (h, w, 3) uint8, top row first; a triangle uses texture
+    # obj_mat_tex >> 16 (-1 = none)
+    obj_texcoords: np.ndarray | None = None
+    textures: list | None = None
     _keep: list = field(default_factory=list, repr=False)
 
     def normalized(self) -> "SceneData":
@@ -119,6 +125,11 @@ class SceneData:
         self.light_power = _f32(self.light_power)
         if self.env_rgb is not None:
             self.env_rgb = np.ascontiguousarray(np.asarray(self.env_rgb, np.float32))
+        if self.obj_texcoords is not None:
+            self.obj_texcoords = _f32(self.obj_texcoords, 2)
+        if self.textures:
+            self.textures = [np.ascontiguousarray(np.asarray(t, np.uint8).reshape(t.shape[0], t.shape[1], 3))
+                             for t in self.textures]
         return self
 
     def desc(self) -> SceneDesc:
@@ -144,6 +155,12 @@ class SceneData:
         d.cam_fov, d.cam_lens_radius, d.cam_focal_dist = self.cam_fov, self.cam_lens_radius, self.cam_focal_dist
         d.film_width, d.film_height = self.film
         d.sampler = self.sampler
+        d.obj_texcoords = p(self.obj_texcoords)
+        if self.textures:
+            size = np.array([(t.shape[1], t.shape[0]) for t in self.textures], np.int32).reshape(-1)
+            rgb = np.concatenate([t.reshape(-1) for t in self.textures])
+            self._keep[:] = [size, rgb]
+            d.n_textures, d.tex_size, d.tex_rgb = len(self.textures), size.ctypes.data, rgb.ctypes.data
         return d
 
     # flattened arrays (objects then lights), for checkers
@@ -164,7 +181,8 @@ class Scene:
         "mat_tex": np.int32, "materials": np.float32,
         "light_power": np.float32, "light_alias": np.int32, "light_prob": np.float32, "env_alias": np.int32,
         "env_prob": np.float32, "env_texels": np.float32, "sobol": np.uint32, "noise": np.float32,
-        "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32,
+        "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32, "tex_scale": np.float32,
+        "srgb_lut": np.float32,
     }
 
     def __init__(self, data: SceneData, host_only: bool = False):
@@ -187,22 +205,23 @@ class Scene:
         return self
 
     def _info(self):
-        info = np.empty(10, np.int64)
+        info = np.empty(11, np.int64)
         call("zgl_scene_export", self._h, b"info", info.ctypes.data, info.nbytes)
         self.info = {k: int(v) for k, v in zip(
             ["film_w", "film_h", "vertices", "obj_vertices", "triangles", "obj_triangles", "light_triangles",
-             "materials", "env_w", "env_h"], info)}
+             "materials", "env_w", "env_h", "textures"], info)}
         self.film = (self.info["film_w"], self.info["film_h"])
 
     def table_size(self, name: str) -> int:
         i = self.info
         nl, (W, H), ew, eh = i["light_triangles"], self.film, i["env_w"], i["env_h"]
         return {
-            "info": 10, "vertices": 3 * i["vertices"], "normals": 3 * i["vertices"], "indices": 3 * i["triangles"],
+            "info": 11, "vertices": 3 * i["vertices"], "normals": 3 * i["vertices"], "indices": 3 * i["triangles"],
             "mat_tex": i["obj_triangles"], "materials": 16 * i["materials"],
             "light_power": nl * 3, "light_alias": nl, "light_prob": nl,
             "env_alias": (ew + 1) * eh, "env_prob": (ew + 1) * eh, "env_texels": ew * eh * 3,
             "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2, "camera": 19, "scalars": 4,
+            "tex_scale": 2 * i["textures"], "srgb_lut": 256,
         }[name]
 
     def export(self, name: str) -> np.ndarray:

@@ -379,6 +379,50 @@ def material_zoo_scene(seed: int = 41, width: int = 64, height: int = 64, sample
     return d.normalized()
 
 
+def texture_images(seed: int = 51):
+    """Three seeded 8-bit sRGB RGB images of different sizes (a 40x24
+    two-colour checkerboard, a 17x31 noise image and a 64x64 gradient with a
+    grid), top row first."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:24, 0:40]
+    c0, c1 = rng.integers(0, 256, 3), rng.integers(0, 256, 3)
+    checker = np.where(((x // 5 + y // 4) % 2)[..., None] == 0, c0, c1).astype(np.uint8)
+    noise = rng.integers(0, 256, (17, 31, 3)).astype(np.uint8)
+    y, x = np.mgrid[0:64, 0:64]
+    grad = np.stack([x * 4, y * 4, 255 - (x + y) * 2], -1)
+    grad[(x % 16 == 0) | (y % 16 == 0)] = 255
+    return [checker, noise, np.clip(grad, 0, 255).astype(np.uint8)]
+
+
+def textured_scene(seed: int = 51, width: int = 64, height: int = 64, sampler: int = 1, base: str = "cornell"):
+    """A scene with albedo textures: ``base`` is the Cornell-style box
+    ("cornell"), the material zoo ("zoo") or the 8-material box of
+    :func:`diff_scene` ("diff").  The floor, back and left walls, the tall box
+    and the principled sphere are textured (three images of different sizes),
+    the other objects keep their material colour.  Texcoords are linear in
+    the position and span about [-1.5, 2.5], so they wrap and go negative."""
+    from .scene import mat_tex
+
+    make = {"cornell": cornell_scene, "zoo": material_zoo_scene, "diff": diff_scene}[base]
+    d = make(seed=seed, width=width, height=height, sampler=sampler)
+    if base == "diff":  # diff_scene shares one material between the boxes: map through the object order
+        d0 = cornell_scene(seed=seed, width=width, height=height, sampler=sampler)
+        objects = d0.obj_mat_tex & 0xFFFF
+    else:
+        objects = d.obj_mat_tex & 0xFFFF
+    rng = np.random.default_rng(seed + 7)
+    a, b = rng.uniform(-1.0, 1.0, 3), rng.uniform(-1.0, 1.0, 3)
+    p = d.obj_vertices.astype(np.float64)
+    d.obj_texcoords = np.stack([p @ a + 0.5, p @ b - 0.25], 1).astype(np.float32)
+    # cornell_scene material order: floor, ceiling, back, left, right, tall box, short box, sphere, sphere
+    tex_of_object = {0: 0, 2: 1, 3: 2, 5: 1, 7: 2}
+    mats = d.obj_mat_tex & 0xFFFF
+    d.obj_mat_tex = np.array([mat_tex(int(m), tex_of_object.get(int(o), -1)) for m, o in zip(mats, objects)],
+                             np.int32)
+    d.textures = texture_images(seed)
+    return d.normalized()
+
+
 def diff_scene(seed: int = 11, width: int = 512, height: int = 512, sampler: int = 1):
     """The Cornell-style box of :func:`cornell_scene` with 8 principled
     materials (5 walls, the two boxes sharing one, the two spheres), each with
