@@ -228,16 +228,22 @@ zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene
  *   flattened "vertices" and "normals"
  *   float[nv*3], "indices" uint32[ntri*3], "mat_tex" int32[objPrimCount],
  *   "materials" float[nmat*16], "tex_scale" float[n_textures*2] (image size /
- *   largest image size, Texture.cpp:163-170) and "srgb_lut" float[256] (the
- *   linear value of each 8-bit sRGB code). */
+ *   largest image size, Texture.cpp:163-170), "texcoords"
+ *   float[object vertices*2] and "srgb_lut" float[256] (the linear value of
+ *   each 8-bit sRGB code). */
 zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out, size_t bytes);
 
 /* Scene::load (src/core/Scene.cpp:58-127) + createGLContext: read a scene XML
  * file (integrator size, sampler, camera, model instances with transforms,
  * materials or light radiance, environment map) and build the scene.  Models
- * are Wavefront OBJ files and the environment map a PFM image (the reference
- * uses assimp and stb_image, which this build does not include).  `flags` as
- * for zgl_scene_create.  Malformed files give ZGL_ERR_PARSE. */
+ * are Wavefront OBJ files (texcoords flipped as aiProcess_FlipUVs does, one
+ * material slot per `usemtl` with the .mtl's Kd and map_Kd; an instance's
+ * <material> replaces every slot's parameters and keeps the textures), albedo
+ * textures are binary/ASCII PPM or uncompressed BMP images (a texture that
+ * cannot be read leaves its faces untextured, as Resource::addImage does) and
+ * the environment map is a PFM image (the reference uses assimp and
+ * stb_image, which this build does not include).  `flags` as for
+ * zgl_scene_create.  Malformed files give ZGL_ERR_PARSE. */
 zgl_status zgl_scene_load_xml(const char* path, int32_t flags, zgl_scene** out);
 
 zgl_status zgl_scene_destroy(zgl_scene* scene);

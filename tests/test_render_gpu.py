@@ -132,6 +132,44 @@ def test_xml_loaded_scene_renders_like_the_oracle(zgl_lib, cuda, tmp_path):
     sc.close()
 
 
+def test_xml_loaded_textured_scene_renders_like_the_oracle(zgl_lib, cuda, tmp_path):
+    """OBJ models with .mtl materials and PPM/BMP albedo textures, loaded from
+    XML, render per pixel like the oracle given the images themselves."""
+    from tests.test_xml_scene import _write_textured
+    from zillumgl_gb300.scene import SceneData
+
+    images = _write_textured(tmp_path)
+    sc = Scene.load(tmp_path / "scene.xml")
+    i = sc.info
+    v = sc.export("vertices").reshape(-1, 3)
+    n = sc.export("normals").reshape(-1, 3)
+    idx = sc.export("indices")
+    nvo, nto = i["obj_vertices"], i["obj_triangles"]
+    data = SceneData(
+        obj_vertices=v[:nvo], obj_normals=n[:nvo], obj_indices=idx[:3 * nto], obj_mat_tex=sc.export("mat_tex"),
+        materials=sc.export("materials").reshape(-1, 16), light_vertices=v[nvo:], light_normals=n[nvo:],
+        light_indices=idx[3 * nto:] - np.uint32(nvo), light_first=np.array([0, 2], np.uint32),
+        light_power=np.array([[30.0, 30.0, 30.0]]), film=sc.film, cam_pos=(1.0, -3.5, 3.0),
+        cam_angle=(0.0, -45.0, 0.0),
+        cam_fov=60.0, sampler=1, obj_texcoords=sc.export("texcoords").reshape(-1, 2),
+        textures=images).normalized()
+    params = dict(max_depth=4)
+    integ = PathIntegrator(sc, **params)
+    for _ in range(2):
+        integ.render_one_pass()
+    frame, _ = integ.get_frame()
+    W, H = sc.film
+    ref = oracle.OracleScene(data, sc.export("sobol"), params).render_pt(np.arange(W * H), 2)
+    got = frame[..., :3].reshape(-1, 3)
+    assert ref.mean() > 0.01
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    data.obj_mat_tex = data.obj_mat_tex | np.int32(-65536)  # the same scene without textures differs
+    plain = oracle.OracleScene(data, sc.export("sobol"), params).render_pt(np.arange(W * H), 2)
+    assert np.abs(plain - ref).max() > 0.05
+    integ.close()
+    sc.close()
+
+
 def test_render_passes_equals_consecutive_passes(zgl_lib, cuda):
     """render_passes(n) in one launch == n render_one_pass calls, bit for bit,
     including a start after earlier passes and a finite sample budget."""

@@ -156,3 +156,118 @@ def test_xml_without_env_is_black(zgl_lib, tmp_path):
     sc = Scene.load(tmp_path / "scene.xml", host_only=True)
     assert sc.info["env_w"] == 0 and sc.export("scalars")[1] == 0.0
     sc.close()
+
+
+# ---------------------------------------------------------------- textures
+TEX_OBJ = """mtllib tex.mtl
+v -1 -1 0
+v 1 -1 0
+v 1 1 0
+v -1 1 0
+v 3 -1 0
+v 3 1 0
+vt 0 0
+vt 2 0
+vt 2 2
+vt 0 2
+vt 0.25 0.75
+vn 0 0 1
+usemtl checker
+f 1/1/1 2/2/1 3/3/1 4/4/1
+usemtl noise
+f 2/1/1 5/2/1 6/3/1
+f 2/5/1 6/3/1 3/4/1
+usemtl plain
+f 4/1/1 3/2/1 6/5/1
+"""
+TEX_MTL = """newmtl checker
+Kd 0.9 0.1 0.2
+map_Kd -s 1 1 1 checker.ppm
+newmtl noise
+Kd 0.3 0.4 0.5
+map_Kd noise.bmp
+newmtl plain
+Kd 0.25 0.5 0.75
+"""
+TEX_SCENE = """<?xml version="1.0"?>
+<scene>
+  <integrator type="path"><size width="32" height="24"/></integrator>
+  <sampler type="sobol"/>
+  <camera type="thinLens"><position value="1 -3.5 3"/><angle value="0 -45 0"/><fov value="60"/>
+    <lensRadius value="0"/><focalDistance value="1"/></camera>
+  <modelInstances>
+    <modelInstance path="tex.obj" type="object">
+      <transform translate="0 0 0" scale="1 1 1" rotate="0 -90 0"/>
+      <material type="default"/>
+    </modelInstance>
+    <modelInstance path="tex.obj" type="object">
+      <transform translate="0 0 0.5" scale="1 1 1" rotate="0 -90 0"/>
+      MATERIAL
+    </modelInstance>
+    <modelInstance path="quad.obj" type="light">
+      <transform translate="0 0 3" scale="1 1 1" rotate="0 90 0"/>
+      <radiance value="30 30 30"/>
+    </modelInstance>
+  </modelInstances>
+</scene>
+"""
+
+
+def _bmp24(img):
+    """Uncompressed 24-bit BMP, bottom row first, rows padded to 4 bytes."""
+    import struct
+
+    H, W = img.shape[:2]
+    stride = (W * 3 + 3) & ~3
+    rows = b"".join(img[y, :, ::-1].tobytes() + b"\0" * (stride - 3 * W) for y in range(H - 1, -1, -1))
+    head = struct.pack("<2sIHHI", b"BM", 54 + len(rows), 0, 0, 54)
+    info = struct.pack("<IiiHHIIiiII", 40, W, H, 1, 24, 0, len(rows), 2835, 2835, 0, 0)
+    return head + info + rows
+
+
+def _write_textured(tmp_path, material='<material type="principled"><roughness value="0.5"/></material>'):
+    rng = np.random.default_rng(9)
+    checker = np.where(((np.add.outer(np.arange(6), np.arange(10)) % 2)[..., None]) == 0,
+                       np.array([230, 20, 40], np.uint8), np.array([10, 200, 90], np.uint8)).astype(np.uint8)
+    noise = rng.integers(0, 256, (5, 7, 3)).astype(np.uint8)
+    (tmp_path / "checker.ppm").write_bytes(b"P6\n# a comment\n10 6\n255\n" + checker.tobytes())
+    (tmp_path / "noise.bmp").write_bytes(_bmp24(noise))
+    (tmp_path / "tex.obj").write_text(TEX_OBJ)
+    (tmp_path / "tex.mtl").write_text(TEX_MTL)
+    (tmp_path / "quad.obj").write_text(QUAD)
+    (tmp_path / "scene.xml").write_text(TEX_SCENE.replace("MATERIAL", material))
+    return [checker, noise]
+
+
+def test_obj_textures_materials_and_texcoords(zgl_lib, tmp_path):
+    _write_textured(tmp_path)
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    i = sc.info
+    assert i["textures"] == 2 and i["obj_triangles"] == 2 * 5 and i["materials"] == 2 * 3
+    mats = sc.export("materials").reshape(-1, 16)
+    # "default": each usemtl slot takes its Kd on Material's defaults (Lambertian)
+    assert np.allclose(mats[:3, :3], [[0.9, 0.1, 0.2], [0.3, 0.4, 0.5], [0.25, 0.5, 0.75]])
+    assert np.all(mats[:3, 13:14].view(np.int32) == 0)
+    # an explicit material replaces every slot's parameters (Scene.cpp:47-53)
+    assert np.all(mats[3:, 13:14].view(np.int32) == 1) and np.allclose(mats[3:, 3], 0.5)
+    mt = sc.export("mat_tex")
+    # textures follow the slots and are shared between the two instances
+    assert (mt & 0xFFFF).tolist() == [0, 0, 1, 1, 2, 3, 3, 4, 4, 5]
+    assert (mt >> 16).tolist() == [0, 0, 1, 1, -1, 0, 0, 1, 1, -1]
+    # texcoords: v flipped (aiProcess_FlipUVs), corners joined on (v, vt, vn)
+    uv = sc.export("texcoords").reshape(-1, 2)
+    assert i["obj_vertices"] == 2 * 12  # 12 distinct (v, vt, vn) corners per instance
+    assert {tuple(x) for x in uv[:12].tolist()} == {(0.0, 1.0), (2.0, 1.0), (2.0, -1.0), (0.0, -1.0), (0.25, 0.25)}
+    scale = sc.export("tex_scale").reshape(-1, 2)
+    assert np.array_equal(scale, np.array([[1.0, 1.0], [np.float32(7) / np.float32(10), np.float32(5) / np.float32(6)]],
+                                          np.float32))
+    sc.close()
+
+
+def test_missing_or_unreadable_texture_leaves_faces_untextured(zgl_lib, tmp_path):
+    _write_textured(tmp_path)
+    (tmp_path / "noise.bmp").write_bytes(b"BM not an image")
+    (tmp_path / "checker.ppm").unlink()
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    assert sc.info["textures"] == 0 and np.all((sc.export("mat_tex") >> 16) == -1)
+    sc.close()

@@ -681,6 +681,7 @@ zgl_status zgl_scene_export(const zgl_scene* s, const char* table, void* out, si
     else if (t == "mat_tex") give(s->matTex.data(), 4 * s->matTex.size());
     else if (t == "materials") give(s->materials.data(), 4 * s->materials.size());
     else if (t == "tex_scale") give(s->texScale.data(), 4 * s->texScale.size());
+    else if (t == "texcoords") give(s->texcoords.data(), 4 * s->texcoords.size());
     else if (t == "srgb_lut") give(s->srgbLut.data(), 4 * s->srgbLut.size());
     else if (t == "scalars") {
         float c[4] = {s->lightSum, s->envSum, (float)s->objPrimCount, (float)s->nLight};

@@ -11,10 +11,11 @@
 //     MaterialLoader.cpp:5-68 for all their meshes ("default" keeps
 //     Material's defaults).
 // The reference imports meshes with assimp and images with stb_image, which
-// are not part of this build: meshes are read from Wavefront OBJ files (v, vn,
-// f with fan triangulation, identical (position, normal) corners joined,
-// smooth area-weighted normals when the file has none) and the environment
-// from a PFM float image.
+// are not part of this build: meshes are read from Wavefront OBJ files (v, vt,
+// vn, f with fan triangulation, flipped texcoords, identical corners joined,
+// smooth area-weighted normals when the file has none, mtllib / usemtl
+// material slots with Kd and map_Kd), albedo textures from PPM or BMP files
+// and the environment from a PFM float image.
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -239,20 +240,82 @@ void parse_floats(const std::string& s, float* out, int n, const float* dflt) {
 }
 
 // ------------------------------------------------------------- OBJ meshes
-struct Mesh {
-    std::vector<float> v, n;  // 3 per vertex
-    std::vector<uint32_t> idx;
+// One material slot of a model: an .mtl material (Kd, map_Kd) or the OBJ
+// importer's default material (diffuse 0.6, no texture) for faces without a
+// known `usemtl`.  assimp makes one aiMaterial per slot and one mesh per slot
+// (Resource.cpp:81-89, :148-165).
+struct ObjSlot {
+    std::string name;
+    float kd[3] = {0.6f, 0.6f, 0.6f};
+    std::string mapKd;  // path relative to the model file, "" = none
 };
 
+struct Mesh {
+    std::vector<float> v, n, uv;  // 3, 3 and 2 per joined corner
+    std::vector<uint32_t> idx;
+    std::vector<int32_t> slot;    // per triangle
+    std::vector<ObjSlot> slots;   // in order of first use
+};
+
+std::string dir_of(const std::string& path) {
+    size_t slash = path.find_last_of('/');
+    return slash == std::string::npos ? std::string() : path.substr(0, slash + 1);
+}
+
+// newmtl / Kd / map_Kd of a Wavefront material library (other keys ignored)
+void load_mtl(const std::string& path, std::map<std::string, ObjSlot>& lib) {
+    std::ifstream f(path);
+    if (!f) return;  // a missing library leaves the default material, as the importer does
+    std::string line;
+    ObjSlot* cur = nullptr;
+    while (std::getline(f, line)) {
+        std::istringstream is(line);
+        std::string tag;
+        if (!(is >> tag) || tag[0] == '#') continue;
+        if (tag == "newmtl") {
+            std::string name;
+            std::getline(is >> std::ws, name);
+            while (!name.empty() && std::isspace((unsigned char)name.back())) name.pop_back();
+            cur = &lib[name];
+            cur->name = name;
+        } else if (cur && tag == "Kd") {
+            float r, g, b;
+            if (is >> r >> g >> b) cur->kd[0] = r, cur->kd[1] = g, cur->kd[2] = b;
+        } else if (cur && tag == "map_Kd") {
+            std::string tok, last;  // options (-s, -o, ...) come first; the file name is last
+            while (is >> tok) last = tok;
+            cur->mapKd = last;
+        }
+    }
+}
+
+// Wavefront OBJ with the post-processing the reference asks of assimp
+// (Resource.cpp:44-54): polygons fan-triangulated, texcoords flipped
+// (v -> 1 - v, aiProcess_FlipUVs), identical (position, texcoord, normal)
+// corners joined, smooth area-weighted normals when the file has none; faces
+// grouped into material slots by `usemtl` / `mtllib`.
 Mesh load_obj(const std::string& path) {
     std::ifstream f(path);
     if (!f) fail(ZGL_ERR_PARSE, "cannot open model '%s'", path.c_str());
-    std::vector<float> P, N;
-    std::map<std::pair<long, long>, uint32_t> corner;
+    std::vector<float> P, N, T;
+    std::map<std::tuple<long, long, long>, uint32_t> corner;
+    std::map<std::string, ObjSlot> lib;
+    std::map<std::string, int32_t> slotOf;
     Mesh m;
-    std::vector<std::pair<long, long>> keys;
+    std::vector<std::tuple<long, long, long>> keys;
     std::string line;
     size_t lineno = 0;
+    int32_t cur = -1;
+    auto slot_for = [&](const std::string& name) {
+        auto it = slotOf.find(name);
+        if (it != slotOf.end()) return it->second;
+        ObjSlot sl;
+        auto lt = lib.find(name);
+        if (lt != lib.end()) sl = lt->second;
+        sl.name = name;
+        m.slots.push_back(sl);
+        return slotOf[name] = (int32_t)m.slots.size() - 1;
+    };
     while (std::getline(f, line)) {
         lineno++;
         std::istringstream is(line);
@@ -266,23 +329,43 @@ Mesh load_obj(const std::string& path) {
             float x, y, z;
             if (!(is >> x >> y >> z)) fail(ZGL_ERR_PARSE, "%s:%zu: bad normal", path.c_str(), lineno);
             N.insert(N.end(), {x, y, z});
+        } else if (tag == "vt") {
+            float u, v = 0.0f;
+            if (!(is >> u)) fail(ZGL_ERR_PARSE, "%s:%zu: bad texcoord", path.c_str(), lineno);
+            is >> v;
+            T.insert(T.end(), {u, 1.0f - v});
+        } else if (tag == "mtllib") {
+            std::string name;
+            while (is >> name) load_mtl(dir_of(path) + name, lib);
+        } else if (tag == "usemtl") {
+            std::string name;
+            std::getline(is >> std::ws, name);
+            while (!name.empty() && std::isspace((unsigned char)name.back())) name.pop_back();
+            cur = slot_for(name);
         } else if (tag == "f") {
             std::vector<uint32_t> poly;
             std::string tok;
             while (is >> tok) {
-                long vi = 0, ni = 0;
+                long vi = 0, ti = 0, ni = 0;
                 size_t s1 = tok.find('/');
-                vi = std::stol(tok.substr(0, s1));
-                if (s1 != std::string::npos) {
-                    size_t s2 = tok.find('/', s1 + 1);
-                    if (s2 != std::string::npos && s2 + 1 < tok.size()) ni = std::stol(tok.substr(s2 + 1));
+                try {
+                    vi = std::stol(tok.substr(0, s1));
+                    if (s1 != std::string::npos) {
+                        size_t s2 = tok.find('/', s1 + 1);
+                        std::string t = tok.substr(s1 + 1, s2 == std::string::npos ? std::string::npos : s2 - s1 - 1);
+                        if (!t.empty()) ti = std::stol(t);
+                        if (s2 != std::string::npos && s2 + 1 < tok.size()) ni = std::stol(tok.substr(s2 + 1));
+                    }
+                } catch (const std::exception&) {
+                    fail(ZGL_ERR_PARSE, "%s:%zu: bad face corner '%s'", path.c_str(), lineno, tok.c_str());
                 }
-                long nv = (long)P.size() / 3, nn = (long)N.size() / 3;
+                long nv = (long)P.size() / 3, nt = (long)T.size() / 2, nn = (long)N.size() / 3;
                 if (vi < 0) vi += nv + 1;
+                if (ti < 0) ti += nt + 1;
                 if (ni < 0) ni += nn + 1;
-                if (vi < 1 || vi > nv || ni < 0 || ni > nn)
+                if (vi < 1 || vi > nv || ti < 0 || ti > nt || ni < 0 || ni > nn)
                     fail(ZGL_ERR_PARSE, "%s:%zu: face index out of range", path.c_str(), lineno);
-                auto key = std::make_pair(vi, ni);
+                auto key = std::make_tuple(vi, ti, ni);
                 auto it = corner.find(key);
                 uint32_t id;
                 if (it == corner.end()) {
@@ -295,18 +378,25 @@ Mesh load_obj(const std::string& path) {
                 poly.push_back(id);
             }
             if (poly.size() < 3) fail(ZGL_ERR_PARSE, "%s:%zu: face with fewer than 3 corners", path.c_str(), lineno);
-            for (size_t k = 1; k + 1 < poly.size(); k++) m.idx.insert(m.idx.end(), {poly[0], poly[k], poly[k + 1]});
+            if (cur < 0) cur = slot_for("");
+            for (size_t k = 1; k + 1 < poly.size(); k++) {
+                m.idx.insert(m.idx.end(), {poly[0], poly[k], poly[k + 1]});
+                m.slot.push_back(cur);
+            }
         }
     }
     bool haveN = true;
     for (auto& k : keys) {
-        m.v.insert(m.v.end(), {P[3 * (k.first - 1)], P[3 * (k.first - 1) + 1], P[3 * (k.first - 1) + 2]});
-        if (k.second == 0) haveN = false;
+        long vi = std::get<0>(k), ti = std::get<1>(k);
+        m.v.insert(m.v.end(), {P[3 * (vi - 1)], P[3 * (vi - 1) + 1], P[3 * (vi - 1) + 2]});
+        if (ti > 0) m.uv.insert(m.uv.end(), {T[2 * (ti - 1)], T[2 * (ti - 1) + 1]});
+        else m.uv.insert(m.uv.end(), {0.0f, 0.0f});
+        if (std::get<2>(k) == 0) haveN = false;
     }
     m.n.assign(m.v.size(), 0.0f);
     if (haveN) {
         for (size_t i = 0; i < keys.size(); i++)
-            for (int c = 0; c < 3; c++) m.n[3 * i + c] = N[3 * (keys[i].second - 1) + c];
+            for (int c = 0; c < 3; c++) m.n[3 * i + c] = N[3 * (std::get<2>(keys[i]) - 1) + c];
     } else {
         // smooth normals: area-weighted face normals summed per position
         std::map<long, std::vector<float>> acc;
@@ -317,19 +407,103 @@ Mesh load_obj(const std::string& path) {
             float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
             float fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
             for (int j = 0; j < 3; j++) {
-                auto& s = acc[keys[m.idx[3 * t + j]].first];
+                auto& s = acc[std::get<0>(keys[m.idx[3 * t + j]])];
                 if (s.empty()) s.assign(3, 0.0f);
                 for (int c2 = 0; c2 < 3; c2++) s[c2] += fn[c2];
             }
         }
         for (size_t i = 0; i < keys.size(); i++) {
-            auto& s = acc[keys[i].first];
+            auto& s = acc[std::get<0>(keys[i])];
             float l = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
             for (int c = 0; c < 3; c++) m.n[3 * i + c] = l > 0.0f ? s[c] / l : (c == 2 ? 1.0f : 0.0f);
         }
     }
     if (m.idx.empty()) fail(ZGL_ERR_PARSE, "model '%s' has no faces", path.c_str());
     return m;
+}
+
+// ------------------------------------------------------------- 8-bit images
+// Albedo textures as 8-bit RGB, top row first (what stb_image returns for
+// Image::createFromFile(path, Int8, 3), Image.cpp:10-32).  This build reads
+// binary/ASCII PPM (P6/P3, maxval <= 255) and uncompressed 24/32-bit BMP;
+// stb's PNG/JPEG/TGA decoders are not part of it.  Returns false when the
+// file cannot be read, which leaves the mesh untextured as in
+// Resource::addImage (Resource.cpp:24-35).
+bool read_pnm_token(std::istream& f, long& out) {
+    char c;
+    while (f.get(c)) {
+        if (c == '#') {
+            std::string rest;
+            std::getline(f, rest);
+        } else if (!std::isspace((unsigned char)c)) {
+            f.unget();
+            return static_cast<bool>(f >> out);
+        }
+    }
+    return false;
+}
+
+bool load_image_rgb8(const std::string& path, int& W, int& H, std::vector<uint8_t>& rgb) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    char m0 = 0, m1 = 0;
+    f.get(m0);
+    f.get(m1);
+    if (m0 == 'P' && (m1 == '6' || m1 == '3')) {
+        long w, h, maxv;
+        if (!read_pnm_token(f, w) || !read_pnm_token(f, h) || !read_pnm_token(f, maxv)) return false;
+        if (w <= 0 || h <= 0 || w > 16384 || h > 16384 || maxv <= 0 || maxv > 255) return false;
+        W = (int)w;
+        H = (int)h;
+        rgb.assign((size_t)W * H * 3, 0);
+        if (m1 == '6') {
+            f.get();  // the single whitespace after maxval
+            f.read(reinterpret_cast<char*>(rgb.data()), (std::streamsize)rgb.size());
+            if (!f) return false;
+        } else {
+            for (auto& b : rgb) {
+                long v;
+                if (!read_pnm_token(f, v) || v < 0 || v > maxv) return false;
+                b = (uint8_t)v;
+            }
+        }
+        if (maxv != 255)
+            for (auto& b : rgb) b = (uint8_t)((b * 255 + maxv / 2) / maxv);
+        return true;
+    }
+    if (m0 == 'B' && m1 == 'M') {
+        uint8_t hdr[52];
+        f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
+        if (!f) return false;
+        auto u32 = [&](int o) { return (uint32_t)hdr[o] | ((uint32_t)hdr[o + 1] << 8) | ((uint32_t)hdr[o + 2] << 16) | ((uint32_t)hdr[o + 3] << 24); };
+        auto u16 = [&](int o) { return (uint32_t)hdr[o] | ((uint32_t)hdr[o + 1] << 8); };
+        uint32_t dataOff = u32(8);  // hdr[o] is file byte o + 2: bfOffBits, then BITMAPINFOHEADER
+        int32_t w = (int32_t)u32(16), h = (int32_t)u32(20);
+        uint32_t bpp = u16(26), comp = u32(28);
+        if ((bpp != 24 && bpp != 32) || comp != 0 || w <= 0 || h == 0 || w > 16384 || h > 16384 || h < -16384)
+            return false;
+        bool topDown = h < 0;
+        W = w;
+        H = topDown ? -h : h;
+        size_t stride = (((size_t)W * bpp / 8) + 3) & ~(size_t)3;
+        std::vector<uint8_t> row(stride);
+        rgb.assign((size_t)W * H * 3, 0);
+        f.seekg(dataOff);
+        for (int y = 0; y < H; y++) {
+            f.read(reinterpret_cast<char*>(row.data()), (std::streamsize)stride);
+            if (!f) return false;
+            int dy = topDown ? y : H - 1 - y;
+            for (int x = 0; x < W; x++) {
+                const uint8_t* px = &row[(size_t)x * (bpp / 8)];
+                uint8_t* o = &rgb[3 * ((size_t)dy * W + x)];
+                o[0] = px[2];
+                o[1] = px[1];
+                o[2] = px[0];
+            }
+        }
+        return true;
+    }
+    return false;
 }
 
 // PFM float image (bottom row first in the file); returned top row first.
@@ -450,12 +624,30 @@ zgl_scene* load_scene_xml(const std::string& path, int32_t flags) {
         d.cam_lens_radius = (float)std::atof(get("lensRadius").c_str());
         d.cam_focal_dist = (float)std::atof(get("focalDistance").c_str());
     }
-    std::vector<float> ov, on, lv, ln, lp, mats;
+    std::vector<float> ov, on, ouv, lv, ln, lp, mats;
     std::vector<uint32_t> oi, li, lf{0};
     std::vector<int32_t> omt;
+    // textures of the whole scene, one per distinct file (Resource::addImage)
+    std::map<std::string, int32_t> texOf;
+    std::vector<int32_t> texSize;
+    std::vector<uint8_t> texRGB;
+    auto add_image = [&](const std::string& file) -> int32_t {
+        auto it = texOf.find(file);
+        if (it != texOf.end()) return it->second;
+        int W = 0, H = 0;
+        std::vector<uint8_t> rgb;
+        int32_t id = -1;
+        if (load_image_rgb8(file, W, H, rgb)) {
+            id = (int32_t)(texSize.size() / 2);
+            texSize.insert(texSize.end(), {W, H});
+            texRGB.insert(texRGB.end(), rgb.begin(), rgb.end());
+        }
+        return texOf[file] = id;
+    };
     if (const XmlNode* insts = scene->child("modelInstances")) {
         for (auto& inst : insts->children) {
-            Mesh mesh = load_obj(resolve_path(path, inst->attr("path")));
+            const std::string objPath = resolve_path(path, inst->attr("path"));
+            Mesh mesh = load_obj(objPath);
             float pos[3], scale[3], rot[3];
             const XmlNode* tr = inst->child("transform");
             parse_floats(tr ? tr->attr("translate") : "", pos, 3, zero3);
@@ -500,13 +692,29 @@ zgl_scene* load_scene_xml(const std::string& path, int32_t flags) {
                 parse_floats(r ? r->attr("value") : "", rad, 3, zero3);
                 lp.insert(lp.end(), rad, rad + 3);
             } else {
+                // one material per slot: the XML <material> for every slot
+                // (Scene.cpp:47-53), else the slot's Kd on Material's
+                // defaults; the slot's map_Kd texture either way
                 float m16[16];
                 bool dflt;
                 material_from_xml(inst->child("material"), m16, dflt);
-                mats.insert(mats.end(), m16, m16 + 16);
-                int32_t mi = (int32_t)(mats.size() / 16 - 1);
+                const int32_t matBase = (int32_t)(mats.size() / 16);
+                std::vector<int32_t> slotTex;
+                for (const ObjSlot& sl : mesh.slots) {
+                    float r[16];
+                    std::memcpy(r, m16, sizeof(r));
+                    if (dflt) std::memcpy(r, sl.kd, 3 * sizeof(float));
+                    mats.insert(mats.end(), r, r + 16);
+                    std::string tex = sl.mapKd;
+                    if (!tex.empty() && tex[0] != '/') tex = dir_of(objPath) + tex;
+                    slotTex.push_back(tex.empty() ? -1 : add_image(tex));
+                }
                 for (uint32_t k : mesh.idx) oi.push_back(base + k);
-                for (size_t t = 0; t < mesh.idx.size() / 3; t++) omt.push_back((int32_t)(0xffff0000u | (uint32_t)mi));
+                ouv.insert(ouv.end(), mesh.uv.begin(), mesh.uv.end());
+                for (size_t t = 0; t < mesh.idx.size() / 3; t++) {
+                    const int32_t sl = mesh.slot[t];
+                    omt.push_back((int32_t)(((uint32_t)slotTex[(size_t)sl] << 16) | (uint32_t)(matBase + sl)));
+                }
             }
         }
     }
@@ -537,6 +745,10 @@ zgl_scene* load_scene_xml(const std::string& path, int32_t flags) {
     d.light_power = lp.data();
     d.n_light_instances = lp.size() / 3;
     d.env_rgb = env.empty() ? nullptr : env.data();
+    d.obj_texcoords = ouv.empty() ? nullptr : ouv.data();
+    d.n_textures = (int32_t)(texSize.size() / 2);
+    d.tex_size = texSize.data();
+    d.tex_rgb = texRGB.data();
     zgl_scene* out = nullptr;
     zgl_status st = zgl_scene_create(&d, flags, &out);
     if (st != ZGL_OK) throw Error{st};

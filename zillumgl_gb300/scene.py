@@ -182,7 +182,7 @@ class Scene:
         "light_power": np.float32, "light_alias": np.int32, "light_prob": np.float32, "env_alias": np.int32,
         "env_prob": np.float32, "env_texels": np.float32, "sobol": np.uint32, "noise": np.float32,
         "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32, "tex_scale": np.float32,
-        "srgb_lut": np.float32,
+        "srgb_lut": np.float32, "texcoords": np.float32,
     }
 
     def __init__(self, data: SceneData, host_only: bool = False):
@@ -221,7 +221,7 @@ class Scene:
             "light_power": nl * 3, "light_alias": nl, "light_prob": nl,
             "env_alias": (ew + 1) * eh, "env_prob": (ew + 1) * eh, "env_texels": ew * eh * 3,
             "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2, "camera": 19, "scalars": 4,
-            "tex_scale": 2 * i["textures"], "srgb_lut": 256,
+            "tex_scale": 2 * i["textures"], "srgb_lut": 256, "texcoords": 2 * i["obj_vertices"],
         }[name]
 
     def export(self, name: str) -> np.ndarray:
