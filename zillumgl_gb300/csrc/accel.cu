@@ -81,18 +81,42 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 // ---------------------------------------------------------------------------
 // Persistent traversal: each warp keeps its lanes busy by refilling a lane
-// with the next ray once its traversal ends.  Idle lanes are counted with
-// __ballot_sync/__popc; once at least kRefillIdle lanes (or all) are idle,
-// one lane grabs that many ray indices with a single atomicAdd on the work
-// counter and each idle lane takes its rank.  The common general ray mode
-// runs a specialised box test; the rare axis-dominant and near-zero modes use
-// the generic one.  Every ray is still traversed by one lane in exactly the
+// with the next ray once its traversal ends (ray trip counts differ by two
+// orders of magnitude, so one-thread-per-ray warps run at a third of their
+// lanes).  Lanes run up to kSteps table steps on their own between warp-level
+// checks; then idle lanes are counted with __ballot_sync/__popc and, once at
+// least kRefillIdle lanes (or all) are idle, one lane takes that many ray
+// indices with a single atomicAdd on the work counter and each idle lane
+// takes its rank.  Every ray is still traversed by one lane in exactly the
 // reference order, so results are identical to the one-thread-per-ray
 // kernels.
 // ---------------------------------------------------------------------------
 constexpr int kPersistBlock = 128;
 constexpr int kRefillIdle = 8;
+constexpr int kSteps = 8;
+constexpr int kChunk = 256;  // consecutive rays a warp takes from the work counter at a time
 constexpr unsigned kFull = 0xffffffffu;
+
+// One table step of ray r at entry k (bvhHit / bvhTest loop body).
+template <bool ANY, int MODE>
+__device__ __forceinline__ void trace_step(const DeviceAccel& a, const float4* __restrict__ base,
+                                           const TraceRay& r, int& k, float& dist, int& closest) {
+    const float4 lo = __ldg(base + 2 * k);
+    const float4 hi = __ldg(base + 2 * k + 1);
+    float tmin;
+    const bool h = (MODE < 0 ? box_hit(lo, hi, r, tmin) : box_hit_m<MODE>(lo, hi, r, tmin)) && !(tmin > dist);
+    const int prim = __float_as_int(lo.w);
+    int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+    if (h && prim >= 0) {
+        float t;
+        if (tri_hit(a.tris, prim, r, t) && t < dist) {
+            dist = t;
+            closest = prim;
+            if (ANY) next = a.M;
+        }
+    }
+    k = next;
+}
 
 template <bool ANY>
 __global__ void __launch_bounds__(kPersistBlock)
@@ -105,6 +129,7 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
     const int M = a.M;
     bool active = false;
     bool exhausted = false;  // warp-uniform
+    unsigned long long next = 0, end = 0;  // the warp's current chunk of ray indices (warp-uniform)
     int64_t ray = 0;
     TraceRay r;
     const float4* __restrict__ base = a.nodes;
@@ -113,15 +138,20 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
     for (;;) {
         const unsigned idle = __ballot_sync(kFull, !active);
         const int nidle = __popc(idle);
+        if (nidle == 32 && exhausted) break;
         if (!exhausted && (nidle >= kRefillIdle || nidle == 32)) {
-            const int leader = __ffs(idle) - 1;
-            unsigned long long b = 0;
-            if (lane == leader) b = atomicAdd(counter, (unsigned long long)nidle);
-            b = __shfl_sync(kFull, b, leader);
-            if (b + nidle >= (unsigned long long)n) exhausted = true;
+            if (next >= end) {  // take the next chunk
+                unsigned long long c = 0;
+                if (lane == 0) c = atomicAdd(counter, (unsigned long long)kChunk);
+                next = __shfl_sync(kFull, c, 0);
+                end = next + kChunk < (unsigned long long)n ? next + kChunk : (unsigned long long)n;
+                if (next >= end) exhausted = true;
+            }
+            const unsigned long long b = next;
+            next = b + nidle < end ? b + nidle : end;
             if (!active) {
                 const unsigned long long idx = b + __popc(idle & lt);
-                if (idx < (unsigned long long)n) {
+                if (idx < end) {
                     ray = (int64_t)idx;
                     r = make_trace_ray(load3(org, ray), load3(dir, ray));
                     base = a.nodes + (size_t)r.face * (size_t)M * 2;
@@ -131,28 +161,16 @@ trace_persistent_kernel(DeviceAccel a, const float* __restrict__ org, const floa
                     active = true;
                 }
             }
-        }
-        if (__ballot_sync(kFull, active) == 0u) {
-            if (exhausted) break;
-            continue;
+            if (__ballot_sync(kFull, active) == 0u) continue;
         }
         if (active) {
-            const float4 lo = __ldg(base + 2 * (size_t)k);
-            const float4 hi = __ldg(base + 2 * (size_t)k + 1);
-            float tmin;
-            const bool bh = r.mode == 3 ? box_hit_m<3>(lo, hi, r, tmin) : box_hit(lo, hi, r, tmin);
-            const bool h = bh && !(tmin > dist);
-            const int prim = __float_as_int(lo.w);
-            int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
-            if (h && prim >= 0) {
-                float t;
-                if (tri_hit(a.tris, prim, r, t) && t < dist) {
-                    dist = t;
-                    closest = prim;
-                    if (ANY) next = M;
-                }
+            if (r.mode == 3) {
+#pragma unroll 1
+                for (int s = 0; s < kSteps && k < M; s++) trace_step<ANY, 3>(a, base, r, k, dist, closest);
+            } else {
+#pragma unroll 1
+                for (int s = 0; s < kSteps && k < M; s++) trace_step<ANY, -1>(a, base, r, k, dist, closest);
             }
-            k = next;
             if (k >= M) {
                 if (ANY) {
                     occ[ray] = (uint8_t)(closest >= 0);
