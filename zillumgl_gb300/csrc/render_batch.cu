@@ -229,7 +229,7 @@ __device__ __forceinline__ int find_request(const BatchLaunch& L, int64_t item) 
 }
 
 template <int BLOCK, bool FULL>
-__global__ void __launch_bounds__(BLOCK) batch_kernel(const __grid_constant__ BatchLaunch L) {
+__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK) batch_kernel(const __grid_constant__ BatchLaunch L) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     // warp-uniform: claimed but not yet handed-out work items [qnext, qend)
