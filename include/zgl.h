@@ -222,15 +222,18 @@ zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene
  *   "noise" float[filmW*filmH*2], "pixel_seeds" uint32[filmW*filmH*2],
  *   "camera" float[19] (front, right, up, inverse camera matrix column-major,
  *   tan(fov/2)), "scalars" float[4] (lightSum, envSum as used by the shaders,
- *   objPrimCount, nLightTriangles), "info" int64[11] (film width, film
+ *   objPrimCount, nLightTriangles), "info" int64[13] (film width, film
  *   height, vertices, object vertices, triangles, object triangles, light
- *   triangles, materials, environment width, environment height, textures), the
+ *   triangles, materials, environment width, environment height, textures,
+ *   texture layer width, texture layer height), the
  *   flattened "vertices" and "normals"
  *   float[nv*3], "indices" uint32[ntri*3], "mat_tex" int32[objPrimCount],
  *   "materials" float[nmat*16], "tex_scale" float[n_textures*2] (image size /
  *   largest image size, Texture.cpp:163-170), "texcoords"
- *   float[object vertices*2] and "srgb_lut" float[256] (the linear value of
- *   each 8-bit sRGB code). */
+ *   float[object vertices*2], "tex_texels" uint32[textures*layer height*layer
+ *   width] (RGB8 in the low three bytes, images in the top-left corner of
+ *   their layer) and "srgb_lut" float[256] (the linear value of each 8-bit
+ *   sRGB code). */
 zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out, size_t bytes);
 
 /* Scene::load (src/core/Scene.cpp:58-127) + createGLContext: read a scene XML

@@ -271,3 +271,48 @@ def test_missing_or_unreadable_texture_leaves_faces_untextured(zgl_lib, tmp_path
     sc = Scene.load(tmp_path / "scene.xml", host_only=True)
     assert sc.info["textures"] == 0 and np.all((sc.export("mat_tex") >> 16) == -1)
     sc.close()
+
+
+def _bmp32_top_down(img):
+    """Uncompressed 32-bit BMP with a negative height (rows top first)."""
+    import struct
+
+    H, W = img.shape[:2]
+    bgra = np.concatenate([img[..., ::-1], np.full((H, W, 1), 255, np.uint8)], -1)
+    rows = bgra.tobytes()
+    head = struct.pack("<2sIHHI", b"BM", 54 + len(rows), 0, 0, 54)
+    info = struct.pack("<IiiHHIIiiII", 40, W, -H, 1, 32, 0, len(rows), 2835, 2835, 0, 0)
+    return head + info + rows
+
+
+def test_image_variants_and_default_material(zgl_lib, tmp_path):
+    """ASCII PPM (maxval 100, rescaled), top-down 32-bit BMP, and an OBJ
+    without a material library (assimp's default material: diffuse 0.6)."""
+    _write_textured(tmp_path)
+    rng = np.random.default_rng(3)
+    small = rng.integers(0, 101, (3, 4, 3))
+    txt = "P3\n4 3\n100\n" + " ".join(str(int(x)) for x in small.reshape(-1)) + "\n"
+    (tmp_path / "checker.ppm").write_text(txt)
+    big = rng.integers(0, 256, (9, 12, 3)).astype(np.uint8)
+    (tmp_path / "noise.bmp").write_bytes(_bmp32_top_down(big))
+    (tmp_path / "plain.obj").write_text(QUAD)
+    scene = TEX_SCENE.replace("MATERIAL", '<material type="default"/>').replace(
+        '<modelInstance path="quad.obj" type="light">',
+        '<modelInstance path="plain.obj" type="object"><transform translate="0 0 -1"/>'
+        '<material type="default"/></modelInstance>\n    <modelInstance path="quad.obj" type="light">')
+    (tmp_path / "scene.xml").write_text(scene)
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    assert sc.info["textures"] == 2
+    # sizes 4x3 and 12x9: scales relative to the 12x9 layer
+    scale = sc.export("tex_scale").reshape(-1, 2)
+    assert np.array_equal(scale, np.array([[np.float32(4) / np.float32(12), np.float32(3) / np.float32(9)],
+                                           [1.0, 1.0]], np.float32))
+    tex = sc.export("tex_texels").reshape(2, 9, 12)
+    rgb = np.stack([tex & 255, (tex >> 8) & 255, (tex >> 16) & 255], -1).astype(np.int64)
+    assert np.array_equal(rgb[0, :3, :4], (small * 255 + 50) // 100)  # maxval 100 rescaled to 255
+    assert np.all(rgb[0, 3:] == 0) and np.all(rgb[0, :, 4:] == 0)  # rest of the layer zero
+    assert np.array_equal(rgb[1], big)  # top-down BMP rows kept in order
+    mats = sc.export("materials").reshape(-1, 16)
+    assert np.allclose(mats[-1, :3], 0.6)  # the OBJ without .mtl
+    assert (sc.export("mat_tex")[-2:] >> 16).tolist() == [-1, -1]
+    sc.close()

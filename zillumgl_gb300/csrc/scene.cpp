@@ -671,9 +671,9 @@ zgl_status zgl_scene_export(const zgl_scene* s, const char* table, void* out, si
         c[18] = s->tanFOV;
         give(c, sizeof(c));
     } else if (t == "info") {
-        int64_t c[11] = {s->filmW, s->filmH, (int64_t)s->vertices.size() / 3, s->nObjVertices, s->ntri,
+        int64_t c[13] = {s->filmW, s->filmH, (int64_t)s->vertices.size() / 3, s->nObjVertices, s->ntri,
                          s->objPrimCount, s->nLight, (int64_t)s->materials.size() / 16, s->envW, s->envH,
-                         s->nTextures};
+                         s->nTextures, s->texMaxW, s->texMaxH};
         give(c, sizeof(c));
     } else if (t == "vertices") give(s->vertices.data(), 4 * s->vertices.size());
     else if (t == "normals") give(s->normals.data(), 4 * s->normals.size());
@@ -682,6 +682,7 @@ zgl_status zgl_scene_export(const zgl_scene* s, const char* table, void* out, si
     else if (t == "materials") give(s->materials.data(), 4 * s->materials.size());
     else if (t == "tex_scale") give(s->texScale.data(), 4 * s->texScale.size());
     else if (t == "texcoords") give(s->texcoords.data(), 4 * s->texcoords.size());
+    else if (t == "tex_texels") give(s->texels.data(), 4 * s->texels.size());
     else if (t == "srgb_lut") give(s->srgbLut.data(), 4 * s->srgbLut.size());
     else if (t == "scalars") {
         float c[4] = {s->lightSum, s->envSum, (float)s->objPrimCount, (float)s->nLight};

@@ -182,7 +182,7 @@ class Scene:
         "light_power": np.float32, "light_alias": np.int32, "light_prob": np.float32, "env_alias": np.int32,
         "env_prob": np.float32, "env_texels": np.float32, "sobol": np.uint32, "noise": np.float32,
         "pixel_seeds": np.uint32, "camera": np.float32, "scalars": np.float32, "tex_scale": np.float32,
-        "srgb_lut": np.float32, "texcoords": np.float32,
+        "srgb_lut": np.float32, "texcoords": np.float32, "tex_texels": np.uint32,
     }
 
     def __init__(self, data: SceneData, host_only: bool = False):
@@ -205,23 +205,24 @@ class Scene:
         return self
 
     def _info(self):
-        info = np.empty(11, np.int64)
+        info = np.empty(13, np.int64)
         call("zgl_scene_export", self._h, b"info", info.ctypes.data, info.nbytes)
         self.info = {k: int(v) for k, v in zip(
             ["film_w", "film_h", "vertices", "obj_vertices", "triangles", "obj_triangles", "light_triangles",
-             "materials", "env_w", "env_h", "textures"], info)}
+             "materials", "env_w", "env_h", "textures", "tex_w", "tex_h"], info)}
         self.film = (self.info["film_w"], self.info["film_h"])
 
     def table_size(self, name: str) -> int:
         i = self.info
         nl, (W, H), ew, eh = i["light_triangles"], self.film, i["env_w"], i["env_h"]
         return {
-            "info": 11, "vertices": 3 * i["vertices"], "normals": 3 * i["vertices"], "indices": 3 * i["triangles"],
+            "info": 13, "vertices": 3 * i["vertices"], "normals": 3 * i["vertices"], "indices": 3 * i["triangles"],
             "mat_tex": i["obj_triangles"], "materials": 16 * i["materials"],
             "light_power": nl * 3, "light_alias": nl, "light_prob": nl,
             "env_alias": (ew + 1) * eh, "env_prob": (ew + 1) * eh, "env_texels": ew * eh * 3,
             "sobol": 256 * 32, "noise": W * H * 2, "pixel_seeds": W * H * 2, "camera": 19, "scalars": 4,
             "tex_scale": 2 * i["textures"], "srgb_lut": 256, "texcoords": 2 * i["obj_vertices"],
+            "tex_texels": i["textures"] * i["tex_w"] * i["tex_h"],
         }[name]
 
     def export(self, name: str) -> np.ndarray:
