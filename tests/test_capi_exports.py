@@ -61,3 +61,25 @@ def test_invalid_arguments_return_status_not_abort(zgl_lib):
     edge = v.copy()
     edge[2] = (1e8, -1e8, 0.5)
     assert BVH(edge, np.array([0, 1, 2], np.uint32)).build_host().bounds.shape == (1, 6)
+
+
+def test_device_build_argument_checks_need_no_gpu(zgl_lib):
+    """zgl_accel_build_device validates its arguments before any device work."""
+    import ctypes as C
+
+    from zillumgl_gb300 import BVH, ZglError
+    from zillumgl_gb300._lib import call
+
+    v = np.zeros((3, 3), np.float32)
+    i = np.array([0, 1, 2], np.uint32)
+    for bad in (5000, -1):
+        with pytest.raises(ZglError) as e:
+            BVH(v, i).build_device(small_threshold=bad)
+        assert e.value.status == 1 and "small_threshold" in str(e.value)
+    with pytest.raises(ZglError) as e:
+        call("zgl_accel_build_device", v.ctypes.data, 3, i.ctypes.data, 1, 0, 0, None)
+    assert e.value.status == 1
+    with pytest.raises(ZglError) as e:
+        out = C.c_void_p()
+        call("zgl_accel_build_device", None, 3, None, 1, 0, 0, C.byref(out))
+    assert e.value.status == 1
