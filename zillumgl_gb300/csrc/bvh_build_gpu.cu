@@ -29,7 +29,6 @@
 // buffers; a node's range lives in the buffer of its depth parity.
 #include <algorithm>
 #include <cstring>
-#include <vector>
 
 #include "accel.h"
 #include "zgl_internal.h"
