@@ -302,8 +302,6 @@ zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integ
  * accumulated into the frame; asynchronous on `stream`. */
 zgl_status zgl_integrator_render_pass(zgl_integrator* integ, void* stream);
 
-/* Integrator::reset (NaivePath.cpp:107-115): the next pass restarts the
- * progressive sum at sample 0. */
 /* `passes` consecutive calls of zgl_integrator_render_pass in one go: the
  * frame, sample count and counters end exactly as after those calls.  The
  * path tracer renders all of them in one launch (per-pass radiance in a
@@ -313,6 +311,8 @@ zgl_status zgl_integrator_render_pass(zgl_integrator* integ, void* stream);
  * No counterpart in the reference (one dispatch per pass). */
 zgl_status zgl_integrator_render_passes(zgl_integrator* integ, int32_t passes, void* stream);
 
+/* Integrator::reset (NaivePath.cpp:107-115): the next pass restarts the
+ * progressive sum at sample 0. */
 zgl_status zgl_integrator_reset(zgl_integrator* integ);
 
 /* Integrator::getFrame: the frame holds the running SUM of samples, RGBA
@@ -328,6 +328,29 @@ zgl_status zgl_integrator_frame(zgl_integrator* integ, float* out, int32_t* spp,
 zgl_status zgl_integrator_result_scale(const zgl_integrator* integ, float* out);
 
 zgl_status zgl_integrator_destroy(zgl_integrator* integ);
+
+/* Checkpoint / resume (no counterpart in the reference, whose
+ * Scene::saveToFile is empty, Scene.cpp:129-131).  An integrator's whole
+ * progressive state is its running sum plus the counters below; the samplers
+ * are counter-based, so an integrator restored from a checkpoint continues
+ * exactly like one that never stopped (the path tracer bit for bit).  The
+ * sum holds zgl_integrator_state_size floats: the path tracer's RGBA frame
+ * (filmW*filmH*4) or the light / triple integrators' RGB film
+ * (filmW*filmH*3).  `sum` may be host or device memory; both calls return
+ * after the copy.  A checkpoint restores into any integrator of the same
+ * kind on a scene with the same film size. */
+typedef struct zgl_integrator_state {
+    int32_t kind;             /* ZGL_INTEGRATOR_* of the saving integrator */
+    int32_t cur_sample;       /* passes rendered since the last reset */
+    int32_t free_counter;     /* the rand() seed counter */
+    int32_t finished;         /* the finite-sample limit was reached */
+    float sample_per_pixel;   /* light / triple bookkeeping of resultScale */
+} zgl_integrator_state;
+zgl_status zgl_integrator_state_size(const zgl_integrator* integ, size_t* floats);
+zgl_status zgl_integrator_save(const zgl_integrator* integ, zgl_integrator_state* state, float* sum,
+                               void* stream);
+zgl_status zgl_integrator_restore(zgl_integrator* integ, const zgl_integrator_state* state, const float* sum,
+                                  void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batched rendering: many requests in persistent launches                   */

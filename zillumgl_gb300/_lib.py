@@ -73,6 +73,9 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_integrator_frame": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_integrator_result_scale": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "zgl_integrator_destroy": (C.c_int32, [C.c_void_p]),
+    "zgl_integrator_state_size": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "zgl_integrator_save": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_integrator_restore": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_batch_config_default": (C.c_int32, [C.c_void_p]),
     "zgl_batch_create": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "zgl_batch_render": (C.c_int32, [C.c_void_p, C.c_void_p]),

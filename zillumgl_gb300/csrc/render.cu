@@ -6,6 +6,7 @@
 // neighbours.  The 256 Sobol values of the pass's sample row are computed
 // once per block into shared memory.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -858,6 +859,56 @@ zgl_status zgl_integrator_result_scale(const zgl_integrator* it, float* out) {
     ZGL_API_BEGIN
     if (!it || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_result_scale: NULL");
     *out = it->kind == ZGL_INTEGRATOR_PATH ? 1.0f / (float)(it->curSample + 1) : 1.0f / it->samplePerPixel;
+    ZGL_API_END
+}
+
+zgl_status zgl_integrator_state_size(const zgl_integrator* it, size_t* floats) {
+    ZGL_API_BEGIN
+    if (!it || !floats) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_state_size: NULL");
+    const size_t npix = (size_t)it->scene->filmW * it->scene->filmH;
+    *floats = (it->kind == ZGL_INTEGRATOR_PATH ? 4 : 3) * npix;
+    ZGL_API_END
+}
+
+zgl_status zgl_integrator_save(const zgl_integrator* it, zgl_integrator_state* state, float* sum, void* stream) {
+    ZGL_API_BEGIN
+    if (!it || !state || !sum) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_save: NULL");
+    const size_t npix = (size_t)it->scene->filmW * it->scene->filmH;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (it->kind == ZGL_INTEGRATOR_PATH)
+        ZGL_CUDA(cudaMemcpyAsync(sum, it->d_frame, sizeof(float4) * npix, cudaMemcpyDefault, st));
+    else
+        ZGL_CUDA(cudaMemcpyAsync(sum, it->d_film, sizeof(float) * 3 * npix, cudaMemcpyDefault, st));
+    ZGL_CUDA(cudaStreamSynchronize(st));
+    state->kind = it->kind;
+    state->cur_sample = it->curSample;
+    state->free_counter = it->freeCounter;
+    state->finished = it->finished ? 1 : 0;
+    state->sample_per_pixel = it->samplePerPixel;
+    ZGL_API_END
+}
+
+zgl_status zgl_integrator_restore(zgl_integrator* it, const zgl_integrator_state* state, const float* sum,
+                                  void* stream) {
+    ZGL_API_BEGIN
+    if (!it || !state || !sum) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_restore: NULL");
+    if (state->kind != it->kind)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_restore: checkpoint of integrator kind %d, this one is %d",
+             state->kind, it->kind);
+    if (state->cur_sample < 0 || state->free_counter < 0 || !(state->sample_per_pixel >= 0.0f) ||
+        !std::isfinite(state->sample_per_pixel))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_restore: invalid counters");
+    const size_t npix = (size_t)it->scene->filmW * it->scene->filmH;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (it->kind == ZGL_INTEGRATOR_PATH)
+        ZGL_CUDA(cudaMemcpyAsync(it->d_frame, sum, sizeof(float4) * npix, cudaMemcpyDefault, st));
+    else
+        ZGL_CUDA(cudaMemcpyAsync(it->d_film, sum, sizeof(float) * 3 * npix, cudaMemcpyDefault, st));
+    ZGL_CUDA(cudaStreamSynchronize(st));
+    it->curSample = state->cur_sample;
+    it->freeCounter = state->free_counter;
+    it->finished = state->finished != 0;
+    it->samplePerPixel = state->sample_per_pixel;
     ZGL_API_END
 }
 

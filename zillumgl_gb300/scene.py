@@ -255,6 +255,13 @@ def default_params(**kw) -> IntegratorParams:
     return p
 
 
+class IntegratorState(C.Structure):
+    """zgl_integrator_state: the counters of a checkpoint."""
+
+    _fields_ = [("kind", C.c_int32), ("cur_sample", C.c_int32), ("free_counter", C.c_int32),
+                ("finished", C.c_int32), ("sample_per_pixel", C.c_float)]
+
+
 class PathIntegrator:
     """NaivePathIntegrator (src/core/Integrator.h:68-91) on the GPU."""
 
@@ -296,6 +303,28 @@ class PathIntegrator:
         v = C.c_float()
         call("zgl_integrator_result_scale", self._h, C.byref(v))
         return v.value
+
+    def save(self, stream=None):
+        """Checkpoint: (counters dict, running sum as a float32 array)."""
+        from .accel import _stream_handle
+
+        n = C.c_size_t()
+        call("zgl_integrator_state_size", self._h, C.byref(n))
+        total = np.empty(n.value, np.float32)
+        st = IntegratorState()
+        call("zgl_integrator_save", self._h, C.byref(st), total.ctypes.data, _stream_handle(stream))
+        return {k: getattr(st, k) for k, _ in st._fields_}, total
+
+    def restore(self, state: dict, total, stream=None) -> None:
+        """Continue from a checkpoint taken by :meth:`save`."""
+        from .accel import _ptr, _stream_handle
+
+        n = C.c_size_t()
+        call("zgl_integrator_state_size", self._h, C.byref(n))
+        if total.size != n.value:
+            raise ValueError(f"checkpoint holds {total.size} floats, this integrator needs {n.value}")
+        st = IntegratorState(**state)
+        call("zgl_integrator_restore", self._h, C.byref(st), _ptr(total), _stream_handle(stream))
 
     def close(self):
         if self._h:
