@@ -507,6 +507,7 @@ static void validate_mesh(const char* fn, const float* vertices, size_t n_vertic
 zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices, const uint32_t* indices,
                               size_t n_triangles, float* bounds, int32_t* hit_table) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_bvh_build_host");
     validate_mesh("zgl_bvh_build_host", vertices, n_vertices, indices, n_triangles);
     if (n_triangles > 0 && (!bounds || !hit_table))
         fail(ZGL_ERR_INVALID_ARG, "zgl_bvh_build_host: NULL output array");
@@ -522,6 +523,7 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices, const ui
 zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint32_t* indices,
                            size_t n_triangles, zgl_accel** out) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_accel_build");
     if (!out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build: out is NULL");
     *out = nullptr;
     validate_mesh("zgl_accel_build", vertices, n_vertices, indices, n_triangles);
@@ -532,6 +534,7 @@ zgl_status zgl_accel_build(const float* vertices, size_t n_vertices, const uint3
 zgl_status zgl_accel_build_device(const float* vertices, size_t n_vertices, const uint32_t* indices,
                                   size_t n_triangles, int32_t small_threshold, void* stream, zgl_accel** out) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_accel_build_device");
     if (!out) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_build_device: out is NULL");
     *out = nullptr;
     if (n_triangles > 0 && (!vertices || !indices))
@@ -588,6 +591,7 @@ zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule) {
 zgl_status zgl_trace_closest(const zgl_accel* accel, const float* origins, const float* dirs, size_t n,
                              int32_t* hit_id, float* hit_t, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_trace_closest");
     if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest: NULL accel");
     if (n == 0) return ZGL_OK;
     if (!origins || !dirs || !hit_id || !hit_t) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_closest: NULL array");
@@ -606,6 +610,7 @@ zgl_status zgl_trace_closest(const zgl_accel* accel, const float* origins, const
 zgl_status zgl_trace_any(const zgl_accel* accel, const float* origins, const float* dirs, const float* tmax,
                          size_t n, uint8_t* occluded, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_trace_any");
     if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_any: NULL accel");
     if (n == 0) return ZGL_OK;
     if (!origins || !dirs || !tmax || !occluded) fail(ZGL_ERR_INVALID_ARG, "zgl_trace_any: NULL array");

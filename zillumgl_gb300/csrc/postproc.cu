@@ -52,6 +52,7 @@ extern "C" {
 zgl_status zgl_postprocess(const float* frame, int32_t width, int32_t height, int32_t preview_scale,
                            float result_scale, int32_t tone_mapper, float* out, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_postprocess");
     if (!frame || !out) zgl::fail(ZGL_ERR_INVALID_ARG, "zgl_postprocess: NULL array");
     if (width <= 0 || height <= 0 || width > 65536 || height > 65536)
         zgl::fail(ZGL_ERR_INVALID_ARG, "zgl_postprocess: size %dx%d out of range", width, height);

@@ -741,6 +741,7 @@ zgl_status zgl_integrator_create(zgl_scene* scene, int32_t kind, const zgl_integ
 
 zgl_status zgl_integrator_render_pass(zgl_integrator* it, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_integrator_render_pass");
     if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_pass: NULL");
     it->freeCounter++;  // counts every call (NaivePath.cpp:79, LightPath.cpp:85, TriplePath.cpp:268)
     const zgl_scene* sc = it->scene;
@@ -773,6 +774,7 @@ zgl_status zgl_integrator_render_pass(zgl_integrator* it, void* stream) {
 
 zgl_status zgl_integrator_render_passes(zgl_integrator* it, int32_t passes, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_integrator_render_passes");
     if (!it) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_passes: NULL");
     if (passes < 0 || passes > 4096) fail(ZGL_ERR_INVALID_ARG, "zgl_integrator_render_passes: %d passes", passes);
     if (it->kind != ZGL_INTEGRATOR_PATH) {

@@ -637,6 +637,7 @@ zgl_status zgl_batch_get_config(const zgl_batch* b, zgl_batch_config* out) {
 
 zgl_status zgl_batch_render(zgl_batch* b, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_batch_render");
     if (!b) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_render: NULL");
     cudaStream_t user = (cudaStream_t)stream;
     if (!b->exec || !same_cfg(b->graph_cfg, b->cfg)) {
@@ -671,6 +672,7 @@ zgl_status zgl_batch_render(zgl_batch* b, void* stream) {
 
 zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chosen) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_batch_autotune");
     if (!b) fail(ZGL_ERR_INVALID_ARG, "zgl_batch_autotune: NULL");
     cudaStream_t st = b->stream;
     ZGL_CUDA(cudaEventRecord(b->ev_in, (cudaStream_t)stream));

@@ -431,6 +431,7 @@ zgl_status zgl_diff_set_params(zgl_diff* d, const float* params) {
 
 zgl_status zgl_diff_forward(zgl_diff* d, float* image, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_diff_forward");
     if (!d || !image) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_forward: NULL");
     if (!device_ptr(image)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_forward: image must be device memory");
     const zgl_scene* s = d->scene;
@@ -450,6 +451,7 @@ zgl_status zgl_diff_forward(zgl_diff* d, float* image, void* stream) {
 
 zgl_status zgl_diff_backward(zgl_diff* d, const float* d_image, float* d_params, void* stream) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_diff_backward");
     if (!d || !d_image || !d_params) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_backward: NULL");
     if (!device_ptr(d_image) || !device_ptr(d_params))
         fail(ZGL_ERR_INVALID_ARG, "zgl_diff_backward: arrays must be device memory");

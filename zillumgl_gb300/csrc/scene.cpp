@@ -629,6 +629,7 @@ extern "C" {
 
 zgl_status zgl_scene_create(const zgl_scene_desc* desc, int32_t flags, zgl_scene** out) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_scene_create");
     if (!desc || !out) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: NULL argument");
     *out = nullptr;
     auto* s = new zgl_scene();

@@ -759,6 +759,7 @@ zgl_scene* load_scene_xml(const std::string& path, int32_t flags) {
 
 extern "C" zgl_status zgl_scene_load_xml(const char* path, int32_t flags, zgl_scene** out) {
     ZGL_API_BEGIN
+    ZGL_RANGE("zgl_scene_load_xml");
     if (!path || !out) zgl::fail(ZGL_ERR_INVALID_ARG, "zgl_scene_load_xml: NULL argument");
     *out = nullptr;
     *out = zgl::load_scene_xml(path, flags);

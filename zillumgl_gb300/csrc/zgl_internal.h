@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdarg>
 #include <cstdio>
@@ -31,9 +32,19 @@ inline void cuda_check(cudaError_t e, const char* what) {
     }
 }
 
+// A named range over an entry point, shown on nsys / ncu timelines (NVTX;
+// costs nothing unless a tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 }  // namespace zgl
 
 #define ZGL_CUDA(call) ::zgl::cuda_check((call), #call)
+#define ZGL_RANGE(name) ::zgl::NvtxRange zgl_nvtx_range_(name)
 
 // Wraps the body of an extern "C" entry point.
 #define ZGL_API_BEGIN \
