@@ -104,6 +104,24 @@ def test_autotune_then_render(batch_setup):
     b.close()
 
 
+def test_autotune_cache_reuses_the_choice(batch_setup, tmp_path):
+    import json
+
+    reqs, refs = batch_setup
+    path = tmp_path / "tune.json"
+    b = BatchRenderer(reqs)
+    first = b.autotune(cache=path)
+    b.close()
+    table = json.loads(path.read_text())
+    assert list(table.values()) == [first]
+    b2 = BatchRenderer(reqs)
+    assert b2.autotune(cache=path) == first  # from the file, untimed
+    assert b2.config() == first
+    b2.render()
+    _check(reqs, refs)
+    b2.close()
+
+
 @pytest.mark.parametrize("schedule", [FLAT, PERSISTENT])
 def test_batch_in_sample_chunks(zgl_lib, cuda, schedule):
     """A 1 MiB scratch budget forces one sample index per launch for a 256^2

@@ -364,6 +364,60 @@ class BatchConfig(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+def _gpu_name() -> str:
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_name(torch.cuda.current_device())
+    except Exception:
+        pass
+    return "cuda"
+
+
+def autotune_cache_key(gpu: str, summary) -> str:
+    """Cache key of a batch: GPU name and the workload class, i.e. request
+    count, total samples and largest scene (triangles), each rounded to a
+    power of two.  ``summary`` lists (triangles, pixels, spp) per request."""
+    import math
+
+    def p2(x):
+        return 0 if x <= 1 else int(round(math.log2(x)))
+
+    n = len(summary)
+    samples = sum(px * spp for _, px, spp in summary)
+    tris = max((t for t, _, _ in summary), default=0)
+    return f"{gpu}|requests 2^{p2(n)}|samples 2^{p2(samples)}|triangles 2^{p2(tris)}"
+
+
+def cached_autotune(path, key: str, tune, apply) -> dict:
+    """The configuration stored under ``key`` in the JSON file ``path``
+    (applied with ``apply``), or ``tune()``'s result, which is then stored.
+    The file is rewritten atomically; an unreadable file counts as empty."""
+    import json
+    import os
+
+    table = {}
+    try:
+        with open(path) as f:
+            table = json.load(f)
+        if not isinstance(table, dict):
+            table = {}
+    except (OSError, ValueError):
+        table = {}
+    if key in table:
+        cfg = {k: int(v) for k, v in table[key].items()}
+        apply(cfg)
+        return cfg
+    cfg = tune()
+    table[key] = cfg
+    tmp = f"{path}.tmp{os.getpid()}"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+    return cfg
+
+
 class BatchRenderer:
     """Many path-tracing requests in persistent launches (zgl_batch_*).
 
@@ -376,6 +430,8 @@ class BatchRenderer:
 
         arr = (RenderRequest * len(requests))()
         self._keep = []
+        self._summary = [(int(scene.info["triangles"]), int(scene.film[0]) * int(scene.film[1]), int(spp))
+                         for scene, spp, _, _ in requests]
         for i, (scene, spp, params, frame) in enumerate(requests):
             arr[i].scene = scene.handle.value
             arr[i].spp = spp
@@ -395,12 +451,24 @@ class BatchRenderer:
 
         call("zgl_batch_render", self._h, _stream_handle(stream))
 
-    def autotune(self, stream=None) -> dict:
+    def autotune(self, stream=None, cache=None) -> dict:
+        """Pick the fastest configuration (zgl_batch_autotune) and keep it.
+
+        With ``cache`` (a JSON file path) the choice is stored under a key of
+        the GPU's name and the workload class (request count, total samples
+        and largest scene, each rounded to a power of two); a later call with
+        the same key reuses it without timing anything."""
         from .accel import _stream_handle
 
-        cfg = BatchConfig()
-        call("zgl_batch_autotune", self._h, _stream_handle(stream), C.byref(cfg))
-        return cfg.as_dict()
+        def tune():
+            cfg = BatchConfig()
+            call("zgl_batch_autotune", self._h, _stream_handle(stream), C.byref(cfg))
+            return cfg.as_dict()
+
+        if cache is None:
+            return tune()
+        key = autotune_cache_key(_gpu_name(), self._summary)
+        return cached_autotune(cache, key, tune, lambda c: self.set_config(**c))
 
     def config(self) -> dict:
         cfg = BatchConfig()
