@@ -18,7 +18,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .build_oracle import LIB, REF_LIB, build_oracle, build_reference
+from .build_oracle import LIB, REF_LIB, REFERENCE_SRC, build_oracle, build_reference
 
 _lib = None
 _ref = None
@@ -48,7 +48,7 @@ def ref_lib() -> C.CDLL | None:
     """The reference's own standalone headers, or None when unavailable."""
     global _ref
     if _ref is None:
-        path = build_reference() if Path("/root/reference/src").is_dir() else (REF_LIB if REF_LIB.exists() else None)
+        path = build_reference() if REFERENCE_SRC.is_dir() else (REF_LIB if REF_LIB.exists() else None)
         if path is None or not Path(path).exists():
             return None
         L = C.CDLL(str(path))
