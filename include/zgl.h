@@ -245,7 +245,7 @@ zgl_status zgl_scene_export(const zgl_scene* scene, const char* table, void* out
  * textures are binary/ASCII PPM or uncompressed BMP images (a texture that
  * cannot be read leaves its faces untextured, as Resource::addImage does) and
  * the environment map is a PFM image (the reference uses assimp and
- * stb_image, which this build does not include).  `flags` as for
+ * stb_image, which this library does not include).  `flags` as for
  * zgl_scene_create.  Malformed files give ZGL_ERR_PARSE. */
 zgl_status zgl_scene_load_xml(const char* path, int32_t flags, zgl_scene** out);
 

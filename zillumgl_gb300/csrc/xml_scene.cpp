@@ -11,7 +11,7 @@
 //     MaterialLoader.cpp:5-68 for all their meshes ("default" keeps
 //     Material's defaults).
 // The reference imports meshes with assimp and images with stb_image, which
-// are not part of this build: meshes are read from Wavefront OBJ files (v, vt,
+// are not part of this library: meshes are read from Wavefront OBJ files (v, vt,
 // vn, f with fan triangulation, flipped texcoords, identical corners joined,
 // smooth area-weighted normals when the file has none, mtllib / usemtl
 // material slots with Kd and map_Kd), albedo textures from PPM or BMP files
