@@ -424,7 +424,7 @@ Mesh load_obj(const std::string& path) {
 
 // ------------------------------------------------------------- 8-bit images
 // Albedo textures as 8-bit RGB, top row first (what stb_image returns for
-// Image::createFromFile(path, Int8, 3), Image.cpp:10-32).  This build reads
+// Image::createFromFile(path, Int8, 3), Image.cpp:10-32).  This library reads
 // binary/ASCII PPM (P6/P3, maxval <= 255) and uncompressed 24/32-bit BMP;
 // stb's PNG/JPEG/TGA decoders are not part of it.  Returns false when the
 // file cannot be read, which leaves the mesh untextured as in
