@@ -316,3 +316,38 @@ def test_image_variants_and_default_material(zgl_lib, tmp_path):
     assert np.allclose(mats[-1, :3], 0.6)  # the OBJ without .mtl
     assert (sc.export("mat_tex")[-2:] >> 16).tolist() == [-1, -1]
     sc.close()
+
+
+def test_obj_edge_cases(zgl_lib, tmp_path):
+    """Unknown usemtl names and a missing .mtl fall back to the default
+    material (diffuse 0.6); `vt u` alone means v = 0 (flipped to 1);
+    negative face indices count back from the last vertex / texcoord;
+    a bad corner token is a parse error."""
+    obj = """mtllib missing.mtl
+v 0 0 0
+v 1 0 0
+v 0 1 0
+v 1 1 0
+vt 0.25
+vt 0.5 0.5
+vn 0 0 1
+usemtl nowhere
+f -4/-2/-1 -3/-1/-1 -2/-1/-1
+usemtl nowhere
+f 2/1/1 4/2/1 3/2/1
+"""
+    (tmp_path / "edge.obj").write_text(obj)
+    (tmp_path / "quad.obj").write_text(QUAD)
+    scene = TEX_SCENE.replace("tex.obj", "edge.obj").replace("MATERIAL", '<material type="default"/>')
+    (tmp_path / "scene.xml").write_text(scene)
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    mats = sc.export("materials").reshape(-1, 16)
+    assert mats.shape[0] == 2 and np.allclose(mats[:, :3], 0.6)  # one slot per instance
+    assert (sc.export("mat_tex") >> 16).tolist() == [-1] * 4
+    uv = sc.export("texcoords").reshape(-1, 2)
+    assert {tuple(x) for x in uv.tolist()} == {(0.25, 1.0), (0.5, 0.5)}
+    sc.close()
+    (tmp_path / "edge.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1/x 2 3\n")
+    with pytest.raises(ZglError) as e:
+        Scene.load(tmp_path / "scene.xml", host_only=True)
+    assert e.value.status == 5
