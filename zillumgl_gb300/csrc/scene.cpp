@@ -4,9 +4,11 @@
 #include "scene.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <utility>
 
 #include "zgl_internal.h"
@@ -181,18 +183,63 @@ void camera_update(zgl_scene& s, const float* angle, float fov) {  // Camera.cpp
     s.tanFOV = std::tan(fov * 0.5f * rad);
 }
 
+// Runs f(b, e) over [0, n) in contiguous chunks of at least `grain` items on
+// the host threads (inline when n is small).  f must not throw.
+template <class F>
+void parallel_for(int64_t n, F&& f, int64_t grain = 4096) {
+    const int nt = (int)std::min<int64_t>(host_threads(), std::max<int64_t>(1, n / grain));
+    if (nt <= 1) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        const int64_t b = t * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back([&f, b, e] { f(b, e); });
+    }
+    for (auto& x : th) x.join();
+}
+
+// Smallest i in [0, n) with bad(i), or -1; checked on the host threads.
+template <class P>
+int64_t first_bad(int64_t n, P&& bad) {
+    std::atomic<int64_t> first{INT64_MAX};
+    parallel_for(n, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; i++)
+            if (bad(i)) {
+                int64_t cur = first.load();
+                while (i < cur && !first.compare_exchange_weak(cur, i)) {
+                }
+                return;
+            }
+    }, 1 << 16);
+    const int64_t f = first.load();
+    return f == INT64_MAX ? -1 : f;
+}
+
 // libstdc++'s std::default_random_engine (minstd_rand0, seed 1) through
 // uniform_real_distribution<float>(0, 1): Sampler::genNoiseTexture
 // (Sampler.cpp:66-80) as built by GCC.
+// The draws are split over host threads; each chunk starts from the
+// engine's state at its first index (16807^i mod (2^31 - 1)), so the values
+// equal the sequential stream.
 void noise_texture(int W, int H, std::vector<float>& out) {
     out.resize((size_t)W * H * 2);
-    uint64_t x = 1;
-    for (size_t i = 0; i < out.size(); i++) {
-        x = (x * 16807u) % 2147483647u;
-        float v = (float)(x - 1) / 2147483646.0f;
-        if (v >= 1.0f) v = std::nextafter(1.0f, 0.0f);
-        out[i] = v * (1.0f - 0.0f) + 0.0f;
-    }
+    const uint64_t p = 2147483647u;
+    parallel_for((int64_t)out.size(), [&](int64_t b, int64_t e) {
+        uint64_t x = 1, base = 16807u;
+        for (uint64_t k = (uint64_t)b; k; k >>= 1) {  // x = 16807^b mod p
+            if (k & 1u) x = (x * base) % p;
+            base = (base * base) % p;
+        }
+        for (int64_t i = b; i < e; i++) {
+            x = (x * 16807u) % p;
+            float v = (float)(x - 1) / 2147483646.0f;
+            if (v >= 1.0f) v = std::nextafter(1.0f, 0.0f);
+            out[(size_t)i] = v * (1.0f - 0.0f) + 0.0f;
+        }
+    });
 }
 
 // texture(uNoiseTex, st): bilinear, repeat wrap, texel centres at (i + 0.5) / size.
@@ -218,16 +265,18 @@ v2 noise_lookup(const std::vector<float>& t, int W, int H, v2 st) {
 // noiseCoord = tex(noise, tex(noise, coord / size)); (uint(W n.x), uint(H n.y)).
 void pixel_seeds(const std::vector<float>& noise, int W, int H, std::vector<uint32_t>& out) {
     out.resize((size_t)W * H * 2);
-    v2 size = mk2((float)W, (float)H);
-    for (int y = 0; y < H; y++)
-        for (int x = 0; x < W; x++) {
-            v2 scr = mk2((float)x, (float)y) / size;
-            v2 nc = noise_lookup(noise, W, H, scr);
-            nc = noise_lookup(noise, W, H, nc);
-            v2 tc = size * nc;
-            out[2 * ((size_t)y * W + x)] = zf2u(tc.x);
-            out[2 * ((size_t)y * W + x) + 1] = zf2u(tc.y);
-        }
+    const v2 size = mk2((float)W, (float)H);
+    parallel_for(H, [&](int64_t y0, int64_t y1) {
+        for (int y = (int)y0; y < (int)y1; y++)
+            for (int x = 0; x < W; x++) {
+                v2 scr = mk2((float)x, (float)y) / size;
+                v2 nc = noise_lookup(noise, W, H, scr);
+                nc = noise_lookup(noise, W, H, nc);
+                v2 tc = size * nc;
+                out[2 * ((size_t)y * W + x)] = zf2u(tc.x);
+                out[2 * ((size_t)y * W + x) + 1] = zf2u(tc.y);
+            }
+    }, 8);
 }
 
 template <class T>
@@ -354,11 +403,13 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
         s.vertices.insert(s.vertices.end(), d.light_vertices, d.light_vertices + 3 * nvl);
         s.normals.insert(s.normals.end(), d.light_normals, d.light_normals + 3 * nvl);
     }
-    for (float v : s.vertices)
-        if (!(v == v)) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: NaN vertex coordinate");
+    if (first_bad((int64_t)s.vertices.size(), [&](int64_t i) { return !(s.vertices[(size_t)i] == s.vertices[(size_t)i]); }) >= 0)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: NaN vertex coordinate");
     s.indices.assign(d.obj_indices, d.obj_indices + 3 * d.obj_n_triangles);
-    for (size_t i = 0; i < 3 * d.obj_n_triangles; i++)
-        if (d.obj_indices[i] >= nvo) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: object index %zu out of range", i);
+    {
+        const int64_t i = first_bad(3 * (int64_t)d.obj_n_triangles, [&](int64_t k) { return d.obj_indices[k] >= nvo; });
+        if (i >= 0) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: object index %lld out of range", (long long)i);
+    }
     for (size_t i = 0; i < 3 * d.light_n_triangles; i++) {
         if (d.light_indices[i] >= nvl) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: light index %zu out of range", i);
         s.indices.push_back((uint32_t)(d.light_indices[i] + nvo));
@@ -386,15 +437,22 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
     }
     texture_tables(s, d);
     s.matTex.assign(d.obj_mat_tex, d.obj_mat_tex + d.obj_n_triangles);
-    for (size_t t = 0; t < d.obj_n_triangles; t++) {
-        int32_t mt = s.matTex[t];
-        int32_t mat = mt & 0xffff, tex = mt >> 16;
-        if (tex != -1) {
-            if (tex < 0 || tex >= s.nTextures)
-                fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu uses texture %d of %d", t, tex, s.nTextures);
-            s.fullMaterials = true;
+    {
+        const int64_t t = first_bad((int64_t)d.obj_n_triangles, [&](int64_t k) {
+            const int32_t mt = s.matTex[(size_t)k], mat = mt & 0xffff, tex = mt >> 16;
+            return (tex != -1 && (tex < 0 || tex >= s.nTextures)) || (size_t)mat >= d.n_materials;
+        });
+        if (t >= 0) {
+            const int32_t tex = s.matTex[(size_t)t] >> 16;
+            if (tex != -1 && (tex < 0 || tex >= s.nTextures))
+                fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %lld uses texture %d of %d", (long long)t, tex,
+                     s.nTextures);
+            fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %lld material out of range", (long long)t);
         }
-        if ((size_t)mat >= d.n_materials) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: triangle %zu material out of range", t);
+        // a textured triangle selects the full material instantiation
+        if (s.nTextures > 0 &&
+            first_bad((int64_t)d.obj_n_triangles, [&](int64_t k) { return (s.matTex[(size_t)k] >> 16) != -1; }) >= 0)
+            s.fullMaterials = true;
     }
 
     // light instances, then power split by area and the light alias table
@@ -422,22 +480,30 @@ void build_scene(zgl_scene& s, const zgl_scene_desc& d) {
         s.envH = H;
         size_t n = (size_t)W * H * 3;
         s.envTexels.resize(n);
-        for (size_t i = 0; i < n; i++) {
-            float v = d.env_rgb[i];
-            if (!std::isfinite(v) || v < 0.0f) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: bad environment texel");
-            s.envTexels[i] = half_round(v);
-        }
+        std::atomic<bool> bad{false};
+        parallel_for((int64_t)n, [&](int64_t b, int64_t e) {
+            for (int64_t i = b; i < e; i++) {
+                float v = d.env_rgb[i];
+                if (!std::isfinite(v) || v < 0.0f) bad = true;
+                s.envTexels[(size_t)i] = half_round(v);
+            }
+        });
+        if (bad) fail(ZGL_ERR_INVALID_ARG, "zgl_scene_create: bad environment texel");
         s.envAlias.assign((size_t)(W + 1) * H, 0);
         s.envProb.assign((size_t)(W + 1) * H, 0.0f);
         auto off = [W](int i, int j) { return (size_t)i * (W + 1) + j; };
-        for (int i = 0; i < H; i++)
-            for (int j = 0; j < W; j++) {
-                const float* p = d.env_rgb + 3 * ((size_t)i * W + j);
-                float lum = 0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2];
-                s.envProb[off(i, j)] = lum * std::sin((float)(i + 0.5f) / (float)H * 3.141592653589793f);
+        // per row: luminance times the row's solid-angle weight, then the
+        // row's alias table (rows are independent)
+        parallel_for(H, [&](int64_t r0, int64_t r1) {
+            for (int i = (int)r0; i < (int)r1; i++) {
+                for (int j = 0; j < W; j++) {
+                    const float* p = d.env_rgb + 3 * ((size_t)i * W + j);
+                    float lum = 0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2];
+                    s.envProb[off(i, j)] = lum * std::sin((float)(i + 0.5f) / (float)H * 3.141592653589793f);
+                }
+                s.envProb[off(i, W)] = env_alias(&s.envAlias[off(i, 0)], &s.envProb[off(i, 0)], W, 1);
             }
-        for (int i = 0; i < H; i++)
-            s.envProb[off(i, W)] = env_alias(&s.envAlias[off(i, 0)], &s.envProb[off(i, 0)], W, 1);
+        }, 8);
         float sum = env_alias(&s.envAlias[(size_t)W], &s.envProb[(size_t)W], H, W + 1);
         s.envSum = (float)zf2i(sum);  // EnvironmentMap::sumPdf returns int
     }
@@ -467,19 +533,21 @@ void upload_scene(zgl_scene& s) {
     s.accel = accel_create_device(s.vertices.data(), (int64_t)s.vertices.size() / 3, s.indices.data(), s.ntri, 0,
                                   0);
     std::vector<float4> shade((size_t)s.ntri * 5);
-    for (int64_t t = 0; t < s.ntri; t++) {
-        auto P = [&](int j) { return &s.vertices[3 * (size_t)s.indices[3 * t + j]]; };
-        auto N = [&](int j) { return &s.normals[3 * (size_t)s.indices[3 * t + j]]; };
-        const float *a = P(0), *b = P(1), *c = P(2), *na = N(0), *nb = N(1), *nc = N(2);
-        int32_t mt = t < s.objPrimCount ? s.matTex[(size_t)t] : -1;
-        float mtf;
-        std::memcpy(&mtf, &mt, 4);
-        shade[5 * t + 0] = make_float4(a[0], a[1], a[2], b[0]);
-        shade[5 * t + 1] = make_float4(b[1], b[2], c[0], c[1]);
-        shade[5 * t + 2] = make_float4(c[2], na[0], na[1], na[2]);
-        shade[5 * t + 3] = make_float4(nb[0], nb[1], nb[2], nc[0]);
-        shade[5 * t + 4] = make_float4(nc[1], nc[2], mtf, 0.0f);
-    }
+    parallel_for(s.ntri, [&](int64_t t0, int64_t t1) {
+        for (int64_t t = t0; t < t1; t++) {
+            auto P = [&](int j) { return &s.vertices[3 * (size_t)s.indices[3 * t + j]]; };
+            auto N = [&](int j) { return &s.normals[3 * (size_t)s.indices[3 * t + j]]; };
+            const float *a = P(0), *b = P(1), *c = P(2), *na = N(0), *nb = N(1), *nc = N(2);
+            int32_t mt = t < s.objPrimCount ? s.matTex[(size_t)t] : -1;
+            float mtf;
+            std::memcpy(&mtf, &mt, 4);
+            shade[5 * t + 0] = make_float4(a[0], a[1], a[2], b[0]);
+            shade[5 * t + 1] = make_float4(b[1], b[2], c[0], c[1]);
+            shade[5 * t + 2] = make_float4(c[2], na[0], na[1], na[2]);
+            shade[5 * t + 3] = make_float4(nb[0], nb[1], nb[2], nc[0]);
+            shade[5 * t + 4] = make_float4(nc[1], nc[2], mtf, 0.0f);
+        }
+    });
     s.d_shade = upload(shade);
     std::vector<float4> mats(s.materials.size() / 4);
     for (size_t i = 0; i < mats.size(); i++)
