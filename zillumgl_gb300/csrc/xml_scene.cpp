@@ -16,11 +16,14 @@
 // smooth area-weighted normals when the file has none, mtllib / usemtl
 // material slots with Kd and map_Kd), albedo textures from PPM or BMP files
 // and the environment from a PFM float image.
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -294,17 +297,82 @@ void load_mtl(const std::string& path, std::map<std::string, ObjSlot>& lib) {
 // (v -> 1 - v, aiProcess_FlipUVs), identical (position, texcoord, normal)
 // corners joined, smooth area-weighted normals when the file has none; faces
 // grouped into material slots by `usemtl` / `mtllib`.
+namespace {
+
+// Cursor over one line of an OBJ file.
+struct LineScan {
+    const char* p;
+    const char* end;
+    void skip_ws() {
+        while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) p++;
+    }
+    bool at_end() {
+        skip_ws();
+        return p >= end;
+    }
+    // next whitespace-delimited token
+    std::string token() {
+        skip_ws();
+        const char* b = p;
+        while (p < end && *p != ' ' && *p != '\t' && *p != '\r') p++;
+        return std::string(b, p);
+    }
+    // the rest of the line, trimmed
+    std::string rest() {
+        skip_ws();
+        const char* e = end;
+        while (e > p && (e[-1] == ' ' || e[-1] == '\t' || e[-1] == '\r')) e--;
+        return std::string(p, e);
+    }
+    // a float as istream >> float reads it (strtof)
+    bool number(float& out) {
+        skip_ws();
+        if (p >= end) return false;
+        char buf[64];
+        const char* b = p;
+        while (p < end && *p != ' ' && *p != '\t' && *p != '\r') p++;
+        size_t len = std::min<size_t>((size_t)(p - b), sizeof(buf) - 1);
+        std::memcpy(buf, b, len);
+        buf[len] = '\0';
+        char* stop = nullptr;
+        out = std::strtof(buf, &stop);
+        return stop != buf && *stop == '\0';
+    }
+};
+
+// one index of a face corner ("" = absent); false on a malformed number
+bool corner_index(const char* b, const char* e, long& out) {
+    out = 0;
+    if (b == e) return true;
+    bool neg = false;
+    if (*b == '-' || *b == '+') {
+        neg = *b == '-';
+        b++;
+    }
+    if (b == e) return false;
+    long v = 0;
+    for (; b < e; b++) {
+        if (*b < '0' || *b > '9' || v > 100000000000l) return false;
+        v = 10 * v + (*b - '0');
+    }
+    out = neg ? -v : v;
+    return true;
+}
+
+}  // namespace
+
 Mesh load_obj(const std::string& path) {
-    std::ifstream f(path);
+    std::ifstream f(path, std::ios::binary);
     if (!f) fail(ZGL_ERR_PARSE, "cannot open model '%s'", path.c_str());
+    const std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
     std::vector<float> P, N, T;
-    std::map<std::tuple<long, long, long>, uint32_t> corner;
     std::map<std::string, ObjSlot> lib;
     std::map<std::string, int32_t> slotOf;
     Mesh m;
+    // joined corners: per position a chain of its (texcoord, normal) variants
+    std::vector<int32_t> head;  // per position: first corner id or -1
+    std::vector<int32_t> next;  // per corner: next corner of the same position
     std::vector<std::tuple<long, long, long>> keys;
-    std::string line;
-    size_t lineno = 0;
     int32_t cur = -1;
     auto slot_for = [&](const std::string& name) {
         auto it = slotOf.find(name);
@@ -316,66 +384,70 @@ Mesh load_obj(const std::string& path) {
         m.slots.push_back(sl);
         return slotOf[name] = (int32_t)m.slots.size() - 1;
     };
-    while (std::getline(f, line)) {
+    std::vector<uint32_t> poly;
+    size_t lineno = 0;
+    const char* q = text.data();
+    const char* const qend = q + text.size();
+    while (q < qend) {
+        const char* eol = static_cast<const char*>(std::memchr(q, '\n', (size_t)(qend - q)));
+        if (!eol) eol = qend;
+        LineScan ls{q, eol};
+        q = eol + 1;
         lineno++;
-        std::istringstream is(line);
-        std::string tag;
-        if (!(is >> tag) || tag[0] == '#') continue;
+        if (ls.at_end() || *ls.p == '#') continue;
+        const std::string tag = ls.token();
         if (tag == "v") {
             float x, y, z;
-            if (!(is >> x >> y >> z)) fail(ZGL_ERR_PARSE, "%s:%zu: bad vertex", path.c_str(), lineno);
+            if (!ls.number(x) || !ls.number(y) || !ls.number(z))
+                fail(ZGL_ERR_PARSE, "%s:%zu: bad vertex", path.c_str(), lineno);
             P.insert(P.end(), {x, y, z});
         } else if (tag == "vn") {
             float x, y, z;
-            if (!(is >> x >> y >> z)) fail(ZGL_ERR_PARSE, "%s:%zu: bad normal", path.c_str(), lineno);
+            if (!ls.number(x) || !ls.number(y) || !ls.number(z))
+                fail(ZGL_ERR_PARSE, "%s:%zu: bad normal", path.c_str(), lineno);
             N.insert(N.end(), {x, y, z});
         } else if (tag == "vt") {
             float u, v = 0.0f;
-            if (!(is >> u)) fail(ZGL_ERR_PARSE, "%s:%zu: bad texcoord", path.c_str(), lineno);
-            is >> v;
+            if (!ls.number(u)) fail(ZGL_ERR_PARSE, "%s:%zu: bad texcoord", path.c_str(), lineno);
+            ls.number(v);
             T.insert(T.end(), {u, 1.0f - v});
         } else if (tag == "mtllib") {
-            std::string name;
-            while (is >> name) load_mtl(dir_of(path) + name, lib);
+            while (!ls.at_end()) load_mtl(dir_of(path) + ls.token(), lib);
         } else if (tag == "usemtl") {
-            std::string name;
-            std::getline(is >> std::ws, name);
-            while (!name.empty() && std::isspace((unsigned char)name.back())) name.pop_back();
-            cur = slot_for(name);
+            cur = slot_for(ls.rest());
         } else if (tag == "f") {
-            std::vector<uint32_t> poly;
-            std::string tok;
-            while (is >> tok) {
+            poly.clear();
+            while (!ls.at_end()) {
+                ls.skip_ws();
+                const char* b = ls.p;
+                while (ls.p < ls.end && *ls.p != ' ' && *ls.p != '\t' && *ls.p != '\r') ls.p++;
+                const char* e = ls.p;
+                const char* s1 = std::find(b, e, '/');
+                const char* s2 = s1 == e ? e : std::find(s1 + 1, e, '/');
                 long vi = 0, ti = 0, ni = 0;
-                size_t s1 = tok.find('/');
-                try {
-                    vi = std::stol(tok.substr(0, s1));
-                    if (s1 != std::string::npos) {
-                        size_t s2 = tok.find('/', s1 + 1);
-                        std::string t = tok.substr(s1 + 1, s2 == std::string::npos ? std::string::npos : s2 - s1 - 1);
-                        if (!t.empty()) ti = std::stol(t);
-                        if (s2 != std::string::npos && s2 + 1 < tok.size()) ni = std::stol(tok.substr(s2 + 1));
-                    }
-                } catch (const std::exception&) {
-                    fail(ZGL_ERR_PARSE, "%s:%zu: bad face corner '%s'", path.c_str(), lineno, tok.c_str());
-                }
-                long nv = (long)P.size() / 3, nt = (long)T.size() / 2, nn = (long)N.size() / 3;
+                bool ok = s1 != b && corner_index(b, s1, vi);
+                if (ok && s1 != e) ok = corner_index(s1 + 1, s2, ti);
+                if (ok && s2 != e) ok = corner_index(s2 + 1, e, ni);
+                if (!ok)
+                    fail(ZGL_ERR_PARSE, "%s:%zu: bad face corner '%s'", path.c_str(), lineno,
+                         std::string(b, e).c_str());
+                const long nv = (long)P.size() / 3, nt = (long)T.size() / 2, nn = (long)N.size() / 3;
                 if (vi < 0) vi += nv + 1;
                 if (ti < 0) ti += nt + 1;
                 if (ni < 0) ni += nn + 1;
                 if (vi < 1 || vi > nv || ti < 0 || ti > nt || ni < 0 || ni > nn)
                     fail(ZGL_ERR_PARSE, "%s:%zu: face index out of range", path.c_str(), lineno);
-                auto key = std::make_tuple(vi, ti, ni);
-                auto it = corner.find(key);
-                uint32_t id;
-                if (it == corner.end()) {
-                    id = (uint32_t)keys.size();
-                    corner[key] = id;
-                    keys.push_back(key);
-                } else {
-                    id = it->second;
+                if (head.size() < (size_t)nv) head.resize((size_t)nv, -1);
+                int32_t id = head[(size_t)vi - 1];
+                while (id >= 0 && (std::get<1>(keys[(size_t)id]) != ti || std::get<2>(keys[(size_t)id]) != ni))
+                    id = next[(size_t)id];
+                if (id < 0) {
+                    id = (int32_t)keys.size();
+                    keys.emplace_back(vi, ti, ni);
+                    next.push_back(head[(size_t)vi - 1]);
+                    head[(size_t)vi - 1] = id;
                 }
-                poly.push_back(id);
+                poly.push_back((uint32_t)id);
             }
             if (poly.size() < 3) fail(ZGL_ERR_PARSE, "%s:%zu: face with fewer than 3 corners", path.c_str(), lineno);
             if (cur < 0) cur = slot_for("");
@@ -386,6 +458,8 @@ Mesh load_obj(const std::string& path) {
         }
     }
     bool haveN = true;
+    m.v.reserve(3 * keys.size());
+    m.uv.reserve(2 * keys.size());
     for (auto& k : keys) {
         long vi = std::get<0>(k), ti = std::get<1>(k);
         m.v.insert(m.v.end(), {P[3 * (vi - 1)], P[3 * (vi - 1) + 1], P[3 * (vi - 1) + 2]});
@@ -399,7 +473,7 @@ Mesh load_obj(const std::string& path) {
             for (int c = 0; c < 3; c++) m.n[3 * i + c] = N[3 * (std::get<2>(keys[i]) - 1) + c];
     } else {
         // smooth normals: area-weighted face normals summed per position
-        std::map<long, std::vector<float>> acc;
+        std::vector<float> acc(P.size(), 0.0f);
         for (size_t t = 0; t < m.idx.size() / 3; t++) {
             const float* a = &m.v[3 * m.idx[3 * t]];
             const float* b = &m.v[3 * m.idx[3 * t + 1]];
@@ -407,15 +481,14 @@ Mesh load_obj(const std::string& path) {
             float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
             float fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
             for (int j = 0; j < 3; j++) {
-                auto& s = acc[std::get<0>(keys[m.idx[3 * t + j]])];
-                if (s.empty()) s.assign(3, 0.0f);
-                for (int c2 = 0; c2 < 3; c2++) s[c2] += fn[c2];
+                float* sum = &acc[3 * (size_t)(std::get<0>(keys[m.idx[3 * t + j]]) - 1)];
+                for (int c2 = 0; c2 < 3; c2++) sum[c2] += fn[c2];
             }
         }
         for (size_t i = 0; i < keys.size(); i++) {
-            auto& s = acc[std::get<0>(keys[i])];
-            float l = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-            for (int c = 0; c < 3; c++) m.n[3 * i + c] = l > 0.0f ? s[c] / l : (c == 2 ? 1.0f : 0.0f);
+            const float* sum = &acc[3 * (size_t)(std::get<0>(keys[i]) - 1)];
+            float l = std::sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]);
+            for (int c = 0; c < 3; c++) m.n[3 * i + c] = l > 0.0f ? sum[c] / l : (c == 2 ? 1.0f : 0.0f);
         }
     }
     if (m.idx.empty()) fail(ZGL_ERR_PARSE, "model '%s' has no faces", path.c_str());
