@@ -63,6 +63,13 @@ def _cases():
     v = np.array([[-0.0, 0, 0], [0.0, 1, 0], [1, -0.0, 0], [0, 0, -0.0], [0, 0, 0.0], [1, 1, 1]], np.float32)
     yield "signed_zero", v, np.array([0, 1, 2, 3, 4, 5, 1, 2, 3, 0, 4, 5], np.uint32)
     yield ("signed_zero_grid", *_signed_zero_grid())
+    # large enough for the multi-threaded top nodes (>= 2^18 triangles), with
+    # 5% of the coordinates set to -0.0 / +0.0
+    v, idx = triangle_soup(300_000, 13)
+    z = np.random.default_rng(14).random(v.shape) < 0.05
+    v = v.copy()
+    v[z] = np.where(np.random.default_rng(15).random(int(z.sum())) < 0.5, np.float32(-0.0), np.float32(0.0))
+    yield "soup_300k_zeros", v, idx
 
 
 @pytest.mark.parametrize("name,v,idx", list(_cases()), ids=lambda x: x if isinstance(x, str) else "")
