@@ -27,7 +27,9 @@ def _export(acc):
 
 
 def _all_cases():
-    yield from _cases()
+    # the host builder's 300k signed-zero soup stays a host case (the device
+    # builder has its own signed-zero grid, 100k and 1M soups)
+    yield from (c for c in _cases() if c[0] != "soup_300k_zeros")
     v = np.tile(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), (700, 1))
     yield "identical_2100", v, np.arange(v.shape[0], dtype=np.uint32)
     yield ("soup_100k", *triangle_soup(100_000, 13))
