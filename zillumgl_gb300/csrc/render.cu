@@ -6,6 +6,7 @@
 // neighbours.  The 256 Sobol values of the pass's sample row are computed
 // once per block into shared memory.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -73,13 +74,17 @@ path_kernel(DeviceScene sc, PathParams pp, int32_t spp, int32_t freeCounter, uin
 
 constexpr int kOccupied = 16;  // blocks of 128 threads per SM: 2048 threads
 
+// SM count of the current device (cached per device)
 int sm_count() {
-    static int n = 0;
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool cached = dev >= 0 && dev < 64;
+    int n = cached ? cache[dev].load(std::memory_order_relaxed) : 0;
     if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (n <= 0) n = 1;
+        if (cached) cache[dev].store(n, std::memory_order_relaxed);
     }
     return n;
 }
