@@ -83,3 +83,27 @@ def test_device_build_argument_checks_need_no_gpu(zgl_lib):
         out = C.c_void_p()
         call("zgl_accel_build_device", None, 3, None, 1, 0, 0, C.byref(out))
     assert e.value.status == 1
+
+
+def test_header_is_plain_c99(tmp_path):
+    """include/zgl.h compiles as C99 (-pedantic, warnings as errors) in a C
+    translation unit that takes the address of every entry point it declares
+    (the boundary a C or FFI caller binds)."""
+    import re
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = Path(__file__).resolve().parents[1]
+    header = (root / "include" / "zgl.h").read_text()
+    names = sorted(set(re.findall(r"\b(zgl_[a-z0-9_]+)\s*\(", header)))
+    src = tmp_path / "use.c"
+    refs = "\n".join(f"    (void)&{n};" for n in names)
+    src.write_text(f'#include "zgl.h"\nint main(void) {{\n    zgl_scene_desc d = {{0}};\n    (void)d;\n{refs}\n'
+                   "    return 0;\n}\n")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{root / 'include'}", "-c",
+                        str(src), "-o", str(tmp_path / "use.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert len(names) > 40
