@@ -511,11 +511,9 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices, const ui
     validate_mesh("zgl_bvh_build_host", vertices, n_vertices, indices, n_triangles);
     if (n_triangles > 0 && (!bounds || !hit_table))
         fail(ZGL_ERR_INVALID_ARG, "zgl_bvh_build_host: NULL output array");
-    HostBVH h;
-    build_bvh(vertices, indices, (int64_t)n_triangles, h, host_threads());
-    if (h.M > 0) {
-        std::memcpy(bounds, h.bounds.data(), sizeof(float) * h.M * 6);
-        std::memcpy(hit_table, h.hitTable.data(), sizeof(int32_t) * h.M * 18);
+    if (n_triangles > 0) {  // straight into the caller's arrays
+        std::vector<int32_t> sizes(2 * n_triangles - 1);
+        build_bvh_into(vertices, indices, (int64_t)n_triangles, bounds, sizes.data(), hit_table, host_threads());
     }
     ZGL_API_END
 }

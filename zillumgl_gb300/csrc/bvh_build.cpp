@@ -226,8 +226,7 @@ void parallel_range(int64_t n, int nthreads, F&& f) {
 }
 
 // buildHitTable (BVH.cpp:298-345) for one face.
-void hit_table_face(const HostBVH& t, int face, int32_t* table) {
-    int64_t M = t.M;
+void hit_table_face(const float* bounds, const int32_t* sizeIndices, int64_t M, int face, int32_t* table) {
     int axis = face >> 1;
     bool greater = (face & 1) == 0;
     std::vector<int64_t> stack;
@@ -237,7 +236,7 @@ void hit_table_face(const HostBVH& t, int face, int32_t* table) {
     while (!stack.empty()) {
         int64_t k = stack.back();
         stack.pop_back();
-        int32_t s = t.sizeIndices[k];
+        int32_t s = sizeIndices[k];
         bool leaf = (s & kLeafMask) != 0;
         int64_t nsize = leaf ? 1 : s;
         table[index * 3 + 0] = (int32_t)k;
@@ -245,11 +244,11 @@ void hit_table_face(const HostBVH& t, int face, int32_t* table) {
         table[index * 3 + 2] = (int32_t)(index + nsize);
         index++;
         if (leaf) continue;
-        int64_t lsize = t.sizeIndices[k + 1];
+        int64_t lsize = sizeIndices[k + 1];
         if (lsize & kLeafMask) lsize = 1;
         int64_t lch = k + 1, rch = k + 1 + lsize;
-        const float* bl = &t.bounds[6 * lch];
-        const float* br = &t.bounds[6 * rch];
+        const float* bl = &bounds[6 * lch];
+        const float* br = &bounds[6 * rch];
         float cl = (bl[axis] + bl[3 + axis]) * 0.5f;
         float cr = (br[axis] + br[3 + axis]) * 0.5f;
         bool first = greater ? (cl > cr) : (cl < cr);
@@ -265,10 +264,16 @@ void hit_table_face(const HostBVH& t, int face, int32_t* table) {
 void build_bvh(const float* v, const uint32_t* idx, int64_t ntri, HostBVH& out, int nthreads) {
     out.ntri = ntri;
     out.M = ntri > 0 ? 2 * ntri - 1 : 0;
-    out.bounds.assign((size_t)out.M * 6, 0.0f);
-    out.sizeIndices.assign((size_t)out.M, 0);
-    out.hitTable.assign((size_t)out.M * 18, 0);
-    if (ntri == 0) return;
+    out.bounds.resize((size_t)out.M * 6);
+    out.sizeIndices.resize((size_t)out.M);
+    out.hitTable.resize((size_t)out.M * 18);
+    build_bvh_into(v, idx, ntri, out.bounds.data(), out.sizeIndices.data(), out.hitTable.data(), nthreads);
+}
+
+void build_bvh_into(const float* v, const uint32_t* idx, int64_t ntri, float* bounds, int32_t* sizeIndices,
+                    int32_t* hitTable, int nthreads) {
+    if (ntri <= 0) return;
+    const int64_t M = 2 * ntri - 1;
     if (nthreads < 1) nthreads = 1;
 
     std::vector<PrimRef> prims((size_t)ntri);
@@ -291,8 +296,8 @@ void build_bvh(const float* v, const uint32_t* idx, int64_t ntri, HostBVH& out, 
 
     Builder b;
     b.prims = prims.data();
-    b.bounds = out.bounds.data();
-    b.sizes = out.sizeIndices.data();
+    b.bounds = bounds;
+    b.sizes = sizeIndices;
     b.serial_cutoff = std::max<int64_t>(1024, ntri / (16 * (int64_t)nthreads));
     b.push(Task{0, root, root.max_extent(), 0, ntri - 1});
     std::vector<std::thread> th;
@@ -301,7 +306,7 @@ void build_bvh(const float* v, const uint32_t* idx, int64_t ntri, HostBVH& out, 
 
     std::vector<std::thread> faces;
     for (int f = 0; f < 6; f++)
-        faces.emplace_back([&out, f] { hit_table_face(out, f, out.hitTable.data() + (size_t)out.M * 3 * f); });
+        faces.emplace_back([=] { hit_table_face(bounds, sizeIndices, M, f, hitTable + (size_t)M * 3 * f); });
     for (auto& x : faces) x.join();
 }
 

@@ -30,4 +30,9 @@ struct HostBVH {
 void build_bvh(const float* vertices, const uint32_t* indices, int64_t ntri, HostBVH& out,
                int nthreads);
 
+// The same build into caller arrays (M = 2*ntri - 1): bounds float[M*6],
+// sizeIndices int32[M], hitTable int32[6*M*3]; every entry is written.
+void build_bvh_into(const float* vertices, const uint32_t* indices, int64_t ntri, float* bounds,
+                    int32_t* sizeIndices, int32_t* hitTable, int nthreads);
+
 }  // namespace zgl
