@@ -351,3 +351,18 @@ f 2/1/1 4/2/1 3/2/1
     with pytest.raises(ZglError) as e:
         Scene.load(tmp_path / "scene.xml", host_only=True)
     assert e.value.status == 5
+
+
+def test_crlf_line_endings(zgl_lib, tmp_path):
+    """OBJ and MTL files with Windows line endings load like LF ones."""
+    _write_textured(tmp_path)
+    ref = Scene.load(tmp_path / "scene.xml", host_only=True)
+    want = {k: ref.export(k) for k in ("vertices", "texcoords", "mat_tex", "materials", "tex_scale")}
+    ref.close()
+    for name in ("tex.obj", "tex.mtl"):
+        text = (tmp_path / name).read_text()
+        (tmp_path / name).write_bytes(text.replace("\n", "\r\n").encode())
+    sc = Scene.load(tmp_path / "scene.xml", host_only=True)
+    for k, v in want.items():
+        assert np.array_equal(sc.export(k), v), k
+    sc.close()
