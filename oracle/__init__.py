@@ -18,10 +18,11 @@ from pathlib import Path
 
 import numpy as np
 
-from .build_oracle import LIB, REF_LIB, REFERENCE_SRC, build_oracle, build_reference
+from .build_oracle import GLSL_LIB, LIB, REF_LIB, REFERENCE_SRC, build_glsl_reference, build_oracle, build_reference
 
 _lib = None
 _ref = None
+_glsl = None
 
 
 def _p(a):
@@ -56,8 +57,78 @@ def ref_lib() -> C.CDLL | None:
         L.ref_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.ref_sobol_matrices.restype = C.c_int32
         L.ref_sobol_matrices.argtypes = [C.c_void_p, C.c_int32]
+        L.ref_bvh_build.restype = C.c_int64
+        L.ref_bvh_build.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         _ref = L
     return _ref
+
+
+def glsl_lib() -> C.CDLL | None:
+    """The reference's path-tracer shader compiled as C++ (oracle/glsl_to_cpp.py),
+    or None without the reference tree."""
+    global _glsl
+    if _glsl is None:
+        path = build_glsl_reference() if REFERENCE_SRC.is_dir() else (GLSL_LIB if GLSL_LIB.exists() else None)
+        if path is None or not Path(path).exists():
+            return None
+        L = C.CDLL(str(path))
+        L.glslref_render_pt.restype = None
+        L.glslref_render_pt.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_int32]
+        L.glslref_render_lt.restype = None
+        L.glslref_render_lt.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
+        L.glslref_render_triple.restype = None
+        L.glslref_render_triple.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                            C.c_void_p, C.c_int32]
+        L.glslref_trace.restype = None
+        L.glslref_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_void_p, C.c_int32]
+        _glsl = L
+    return _glsl
+
+
+def glsl_trace(packed_bounds, packed_hit, vertices, indices, origins, dirs, tmax=None, nthreads=None):
+    """bvhHit / bvhTest of the reference shader source (compiled as C++) on a
+    PackedBVH: (hit id or occluded flag, distance), or None without the
+    reference tree."""
+    L = glsl_lib()
+    if L is None:
+        return None
+    b = np.ascontiguousarray(packed_bounds, np.float32)
+    h = np.ascontiguousarray(packed_hit, np.int32)
+    v = np.ascontiguousarray(vertices, np.float32)
+    idx = np.ascontiguousarray(indices, np.uint32)
+    s = OrcScene()
+    s.vertices, s.normals, s.indices = _p(v), _p(v), _p(idx)
+    s.nTriangles = s.objPrimCount = idx.size // 3
+    s.bounds, s.hitTable, s.bvhSize = _p(b), _p(h), b.shape[0]
+    o = np.ascontiguousarray(origins, np.float32)
+    d = np.ascontiguousarray(dirs, np.float32)
+    tm = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+    hit = np.zeros(o.shape[0], np.int32)
+    dist = np.zeros(o.shape[0], np.float32)
+    L.glslref_trace(C.addressof(s), _p(o), _p(d), _p(tm), o.shape[0], _p(hit), _p(dist), nthreads or threads())
+    return hit, dist
+
+
+def ref_bvh_build(vertices: np.ndarray, indices: np.ndarray):
+    """PackedBVH of the reference's own BVH::build() (src/accelerator/BVH.cpp,
+    compiled from the reference tree): (bounds (M,6) f32, hitTable (6,M,3)
+    i32), or None without the reference tree.  The mesh must not be empty."""
+    ref = ref_lib()
+    if ref is None:
+        return None
+    v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1)
+    ntri = idx.size // 3
+    if ntri == 0:
+        raise ValueError("the reference builder does not handle an empty mesh")
+    M = 2 * ntri - 1
+    bounds = np.zeros((M, 6), np.float32)
+    hit = np.zeros((6, M, 3), np.int32)
+    r = ref.ref_bvh_build(_p(v), v.shape[0], _p(idx), ntri, _p(bounds), _p(hit))
+    assert r == M
+    return bounds, hit
 
 
 def threads() -> int:
@@ -326,6 +397,51 @@ class OracleScene:
         _render_lib().orc_render_pt(C.byref(self.s), spp0, passes, fc0, _p(pix), pix.size, _p(out),
                                     nthreads or threads())
         return out
+
+    def glsl_render_pt(self, pixels, passes, spp0=0, fc0=1, nthreads=None):
+        """render_pt by the reference's own shader source compiled as C++
+        (None without the reference tree).  Russian roulette follows the
+        shader, which starts it at the first bounce."""
+        L = glsl_lib()
+        if L is None:
+            return None
+        pix = np.ascontiguousarray(pixels, np.int32)
+        out = np.zeros((pix.size, 3), np.float32)
+        L.glslref_render_pt(C.addressof(self.s), spp0, passes, fc0, _p(pix), pix.size, _p(out), nthreads or threads())
+        return out
+
+    def glsl_render_lt(self, passes, blocks=32, spp0=0, fc0=1):
+        """render_lt by the reference's light_path_integ.glsl compiled as C++."""
+        L = glsl_lib()
+        if L is None:
+            return None
+        film = np.zeros((self.s.filmH, self.s.filmW, 3), np.float32)
+        L.glslref_render_lt(C.addressof(self.s), spp0, passes, fc0, blocks, _p(film))
+        return film
+
+    def glsl_render_triple(self, passes, blocks=64, loops=1, spp0=0, fc0=1, nthreads=None):
+        """render_triple by the reference's triple_path_pass_{pt,lpt}.glsl
+        compiled as C++."""
+        L = glsl_lib()
+        if L is None:
+            return None
+        film = np.zeros((self.s.filmH, self.s.filmW, 3), np.float32)
+        L.glslref_render_triple(C.addressof(self.s), spp0, passes, fc0, blocks, loops, _p(film), nthreads or threads())
+        return film
+
+    def glsl_trace(self, origins, dirs, tmax=None, nthreads=None):
+        """bvhHit (or bvhTest with tmax) of the reference shader on this
+        scene's PackedBVH: (hit id or occluded flag, distance)."""
+        L = glsl_lib()
+        if L is None:
+            return None
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        tm = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+        hit = np.zeros(o.shape[0], np.int32)
+        dist = np.zeros(o.shape[0], np.float32)
+        L.glslref_trace(C.addressof(self.s), _p(o), _p(d), _p(tm), o.shape[0], _p(hit), _p(dist), nthreads or threads())
+        return hit, dist
 
     def render_lt(self, passes, blocks=32, spp0=0, fc0=1):
         """Film sum (H, W, 3) of `passes` light-tracer passes."""
