@@ -40,6 +40,18 @@ METRIC = "Mrays/s traversal"
 UNIT = "Mrays/s"
 
 
+# kernel of each trace schedule (ZGL_TRACE_* of include/zgl.h); auto resolves
+# as the library does
+KERNELS = {"thread_per_ray": {"closest": "trace_closest_kernel", "any": "trace_any_kernel"},
+           "persistent": {"closest": "trace_persistent_kernel<false>", "any": "trace_persistent_kernel<true>"},
+           "deferred": {"closest": "trace_deferred_kernel<false>", "any": "trace_deferred_kernel<true>"}}
+AUTO_SCHEDULE = "thread_per_ray"
+
+
+def resolved_schedule(schedule: str) -> str:
+    return AUTO_SCHEDULE if schedule == "auto" else schedule
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -49,9 +61,10 @@ def parse_args():
     ap.add_argument("--sizes", default="1M,4M,16M")
     ap.add_argument("--side", type=int, default=4096, help="primary rays = side^2")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline work")
+    ap.add_argument("--ref-rays", type=int, default=1 << 20, help="rays per launch traced by --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent", "deferred"])
     ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
     ap.add_argument("--render", default="cornell,city,batch,diff", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
@@ -313,14 +326,21 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     traffic = profiled_traffic()
     l2, l2_sweep = l2_peak(stream)
-    roofline = {"bound": "hbm", "kernel": "trace_closest_kernel" if dom is closest else "trace_any_kernel",
+    kname = KERNELS[resolved_schedule(args.schedule)]["closest" if dom is closest else "any"]
+    roofline = {"bound": "latency",
+                "bound_note": "node and triangle bytes against the L2 / HBM roofline; the measured limiter is "
+                              "dependent-load latency and SIMD divergence (warp lanes active per instruction, "
+                              "long-scoreboard stalls), not DRAM bandwidth: DRAM traffic is a few percent of the "
+                              "algorithmic bytes, which L1 and L2 serve",
+                "kernel": kname, "l2_frac": round(achieved / l2, 4), "l2_peak": round(l2, 1),
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": f"{peak_kind} hbm_gbs (copy bandwidth)",
-                "l2_peak": round(l2, 1), "l2_frac": round(achieved / l2, 4),
                 "l2_peak_source": "zgl_measure_l2_read: L2-resident buffer read by all SMs with 16-byte ld.global.cg, "
                                   f"best of {l2_sweep} GB/s",
                 "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                 "traffic_note": traffic.get("note") if traffic else "no ncu capture committed yet",
+                "lanes_active_per_inst": traffic.get("lanes_active_per_inst") if traffic else None,
+                "lanes_note": traffic.get("lanes_note") if traffic else None,
                 "algorithmic_bytes_per_launch": int(dom_bytes),
                 "avg_launch_ms": round(dom_ms, 4)}
 
@@ -373,7 +393,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(scenes, specs, args.cpu_seconds)
+        cpu = cpu_baseline(scenes, specs, args.ref_rays)
     for N, v, idx, acc in scenes:
         acc.close()
     render = run_render(args, stream, dev) if args.render else None
@@ -554,8 +574,11 @@ def run_render(args, stream, dev):
         res["path"]["e2e_samples_per_s"] = round(W * H / e2e_s, 1)
         res["path"]["e2e_d2h_bytes_per_pass"] = W * H * 16
         integ.close()
-        if name == "cornell" and not args.no_cpu_baseline:
-            res["path"]["cpu_baseline"] = render_cpu_baseline(data, scene, runs[0][2])
+        if not args.no_cpu_baseline:
+            res["path"]["cpu_baseline"] = render_cpu_baseline(data, scene, runs[0][2], args.cpu_seconds / 3)
+            if name == "city":
+                for kind, _, params in runs[1:]:
+                    res[kind]["cpu_baseline"] = render_cpu_baseline_splat(data, kind, params, args.cpu_seconds / 3)
         scene.close()
         out[name] = res
     return out
@@ -634,9 +657,10 @@ def run_batch(args, stream, dev):
     for it in integs:
         it.close()
     batch.close()
+    cpu = None if args.no_cpu_baseline else batch_cpu_baseline(reqs, scenes, args.cpu_seconds / 3)
     for sc in scenes:
         sc.close()
-    return {"requests": len(reqs), "samples": total,
+    return {"requests": len(reqs), "samples": total, "cpu_baseline": cpu,
             "plain": {"ms": round(plain_ms, 2), "samples_per_s": round(total / (plain_ms * 1e-3), 1),
                       "launches": launches_plain},
             "plain_one_launch_per_request": {"ms": round(multi_ms, 2),
@@ -724,6 +748,10 @@ def run_diff(args, stream, dev):
            "samples_per_s_fwd_bwd": round(W * H * spp / (fb_ms * 1e-3), 1),
            "loss_first": loss_first, "loss_last": loss_last, "iterations": len(losses)}
     res["grad_check"] = diff_grad_check()
+    if not args.no_cpu_baseline:
+        hs = Scene(data, host_only=True)
+        res["cpu_baseline"] = diff_cpu_baseline(data, hs, spp, params, args.cpu_seconds / 3)
+        hs.close()
     return res
 
 
@@ -755,24 +783,122 @@ def diff_grad_check():
             float(np.abs(g - ref).max() / scale), "oracle_s": round(dt, 2)}
 
 
-def render_cpu_baseline(data, scene, params):
-    """The oracle path tracer on every host thread, one pass over a pixel sample."""
+def render_cpu_baseline(data, scene, params, target_s: float = 4.0):
+    """The oracle path tracer on every host thread, one pass over an evenly
+    strided pixel sample sized to about `target_s` seconds."""
     import oracle
 
     nthreads = os.cpu_count() or 1
     orc = oracle.OracleScene(data, scene.export("sobol"), params)
     W, H = data.film
-    pix = np.arange(W * H, dtype=np.int32)
-    orc.render_pt(pix[:256], 1)
+    npix = W * H
+    probe = np.arange(0, npix, max(1, npix // 2048), dtype=np.int32)
+    t0 = time.perf_counter()
+    orc.render_pt(probe, 1)
+    dt = time.perf_counter() - t0
+    stride = max(1, int(np.ceil(npix / max(probe.size * target_s / max(dt, 1e-3), 1.0))))
+    pix = np.arange(0, npix, stride, dtype=np.int32)
     t0 = time.perf_counter()
     orc.render_pt(pix, 1)
     dt = time.perf_counter() - t0
-    return {"samples_per_s": round(W * H / dt, 1), "cores": nthreads, "kind": "port",
-            "sample": f"one {W}x{H} pass of the oracle path tracer ({dt:.2f}s)"}
+    return {"samples_per_s": round(pix.size / dt, 1), "cores": nthreads, "kind": "port",
+            "sample": f"one pass of the oracle path tracer over every {stride}th pixel of the {W}x{H} film "
+                      f"({pix.size} samples, {dt:.2f}s)"}
 
 
-def cpu_baseline(scenes, specs, target_s: float):
-    """The oracle traversal on every host thread over a bounded ray sample."""
+def render_cpu_baseline_splat(data, kind, params, target_s: float = 4.0):
+    """The oracle light tracer or triple integrator on every host thread (per-
+    thread films).  The light tracer runs one pass of as many 1536-path blocks
+    as fit in about `target_s` seconds on the configuration's film; the triple
+    integrator runs one pass on a quarter-size film of the same scene (its
+    camera pass covers every pixel)."""
+    import oracle
+    from zillumgl_gb300.scene import Scene
+
+    nthreads = os.cpu_count() or 1
+    W, H = data.film
+    if kind == "triple":
+        from zillumgl_gb300.synthetic import city_scene
+
+        data = city_scene(seed=2, width=W // 4, height=H // 4)
+    sc = Scene(data, host_only=True)
+    orc = oracle.OracleScene(data, sc.export("sobol"), params)
+    sc.close()
+    w, h = data.film
+    if kind == "light":
+        t0 = time.perf_counter()
+        orc.render_threaded(kind, 1, 8, nthreads=nthreads)
+        dt8 = time.perf_counter() - t0
+        blocks = int(max(8, min(512, 8 * target_s / max(dt8, 1e-3))))
+        t0 = time.perf_counter()
+        orc.render_threaded(kind, 1, blocks, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        return {"light_paths_per_s": round(1536 * blocks / dt, 1), "cores": nthreads, "kind": "port",
+                "sample": f"one pass of {blocks} x 1536 light paths on the {w}x{h} film ({dt:.2f}s)"}
+    t0 = time.perf_counter()
+    orc.render_threaded(kind, 1, 64, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return {"samples_per_s": round(w * h / dt, 1), "cores": nthreads, "kind": "port",
+            "sample": f"one triple pass (camera path per pixel + 64 x 1536 light paths) on a {w}x{h} film of the "
+                      f"same scene ({dt:.2f}s)"}
+
+
+def batch_cpu_baseline(reqs, scenes, target_s: float = 4.0):
+    """The oracle path tracer on every host thread over an evenly strided
+    pixel sample of every request (one pass each): aggregate samples/s."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    orcs = [oracle.OracleScene(d, sc.export("sobol"), params) for (d, _, params), sc in zip(reqs, scenes)]
+
+    def run(per_req):
+        n = 0
+        t0 = time.perf_counter()
+        for (d, _, _), orc in zip(reqs, orcs):
+            W, H = d.film
+            pix = np.linspace(0, W * H - 1, per_req).astype(np.int32)
+            orc.render_pt(pix, 1)
+            n += pix.size
+        return n, time.perf_counter() - t0
+
+    n, dt = run(16)
+    per = int(max(16, 16 * target_s / max(dt, 1e-3)))
+    n, dt = run(per)
+    return {"samples_per_s": round(n / dt, 1), "cores": nthreads, "kind": "port",
+            "sample": f"one pass of the oracle path tracer over {per} evenly spaced pixels of each of the "
+                      f"{len(reqs)} requests ({n} samples, {dt:.2f}s)"}
+
+
+def diff_cpu_baseline(data, scene, spp, params, target_s: float = 4.0):
+    """The FP64 oracle adjoint (forward replay + gradient) on every host thread
+    over an evenly spaced pixel sample at the configuration's spp; ms per
+    forward+backward iteration extrapolated to the whole film."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    orc = oracle.OracleScene(data, scene.export("sobol"), params)
+    W, H = data.film
+
+    def run(k):
+        dimg = np.zeros((W * H, 3), np.float32)
+        pix = np.linspace(0, W * H - 1, k).astype(np.int64)
+        dimg[pix] = 1e-3
+        t0 = time.perf_counter()
+        orc.diff_grad(data, spp, dimg.reshape(H, W, 3))
+        return time.perf_counter() - t0
+
+    dt = run(64)
+    k = int(min(W * H, max(64, 64 * target_s / max(dt, 1e-3))))
+    dt = run(k)
+    ms_iter = dt / k * W * H * 1e3
+    return {"ms_per_iteration": round(ms_iter, 1), "samples_per_s": round(k * spp / dt, 1), "cores": nthreads,
+            "kind": "port", "sample": f"FP64 oracle adjoint over {k} evenly spaced pixels x {spp} spp ({dt:.2f}s), "
+                                      f"extrapolated to the {W}x{H} film"}
+
+
+def cpu_baseline(scenes, specs, sample: int):
+    """The oracle traversal on every host thread over the first `sample` rays
+    of each launch (the rays the reference arm traces)."""
     import oracle
 
     nthreads = os.cpu_count() or 1
@@ -781,34 +907,37 @@ def cpu_baseline(scenes, specs, target_s: float):
         p = acc.export()
         packed[N] = (p.bounds, p.hitTable, v, idx)
 
-    def run(sample):
+    def run(n):
         rays = 0
         t0 = time.perf_counter()
         for sp in specs:
             b, h, v, idx = packed[sp["N"]]
-            o = sp["o_host"][:sample]
-            d = sp["d_host"][:sample]
+            o = sp["o_host"][:n]
+            d = sp["d_host"][:n]
             if sp["query"] == "closest":
                 oracle.trace(b, h, v, idx, o, d, nthreads=nthreads)
             else:
-                tm = sp["tmax"][:sample].cpu().numpy()
+                tm = sp["tmax"][:n].cpu().numpy()
                 oracle.trace(b, h, v, idx, o, d, tmax=tm, any_hit=True, nthreads=nthreads)
             rays += o.shape[0]
         return rays, time.perf_counter() - t0
 
-    probe = 2048
     run(256)  # warm: loads the oracle library
-    r, s = run(probe)
-    sample = int(min(specs[0]["o_host"].shape[0], max(probe, probe * target_s / max(s, 1e-3))))
+    sample = min(sample, specs[0]["o_host"].shape[0])
     r, s = run(sample)
     return {"value": round(r / s / 1e6, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"first {sample} rays of each of the {len(specs)} launches ({r} rays, {s:.1f}s) on the "
-                      f"oracle restatement with {nthreads} threads"}
+                      f"oracle restatement with {nthreads} threads; the reference arm traces the same rays"}
 
 
 def run_reference(args):
-    """CPU reference arm: the oracle restatement (the reference's own traversal is
-    GLSL behind OpenGL, unavailable on this machine) on a bounded sample of the workload."""
+    """CPU reference arm: the oracle restatement (the reference's own traversal
+    is GLSL behind OpenGL, unavailable on this machine) on the host cores, over the
+    same twelve ray sets as the GPU arm: the same soups, the 2^24 coherent
+    primary rays and the incoherent rays made from their closest hits, the same
+    any-hit distances.  Each step traces the first --ref-rays rays (contiguous
+    rows of the primary image) of each of the twelve launches, with every host
+    thread; the rays are the ones the GPU arm's cpu_baseline leg samples."""
     import oracle
     from zillumgl_gb300.synthetic import incoherent_rays, primary_rays, shadow_tmax
 
@@ -818,28 +947,30 @@ def run_reference(args):
     nthreads = os.cpu_count() or 1
     sizes = [SIZES[s] for s in args.sizes.split(",")]
     side = args.side
+    nray = side * side
+    S = min(args.ref_rays, nray)
     o_p, d_p = primary_rays(side, side)
-    sample = 16384
-    rng = np.random.default_rng(0)
-    sel = np.sort(rng.choice(o_p.shape[0], sample, replace=False))
     work = []
+    t_setup = time.time()
     for N in sizes:
+        seed = SEEDS.get(N, 7)
         v, idx = build_scene(N)
         b, h, _ = oracle.bvh_build(v, idx)
-        o, d = o_p[sel], d_p[sel]
-        hid, ht, _, _ = oracle.trace(b, h, v, idx, o, d, nthreads=nthreads)
-        o_i, d_i = incoherent_rays(v, idx, o, d, hid, ht, seed=SEEDS.get(N, 7) + 1)
-        tm_p = 1.0 + shadow_tmax(sample, SEEDS.get(N, 7) + 2)
-        tm_i = shadow_tmax(sample, SEEDS.get(N, 7) + 3)
-        work.append((b, h, v, idx, o, d, o_i, d_i, tm_p, tm_i))
+        hid, ht, _, _ = oracle.trace(b, h, v, idx, o_p, d_p, nthreads=nthreads)
+        o_i, d_i = incoherent_rays(v, idx, o_p, d_p, hid, ht, seed=seed + 1)
+        tm_p = 1.0 + shadow_tmax(nray, seed + 2)
+        tm_i = shadow_tmax(nray, seed + 3)
+        for oo, dd, tm in ((o_p, d_p, tm_p), (o_i, d_i, tm_i)):
+            work.append((b, h, v, idx, oo[:S].copy(), dd[:S].copy(), tm[:S].copy()))
+        del hid, ht, o_i, d_i
+    log(f"[bench] reference arm setup {time.time() - t_setup:.1f}s")
 
     def step():
         rays = 0
-        for b, h, v, idx, o, d, o_i, d_i, tm_p, tm_i in work:
-            for oo, dd, tm in ((o, d, tm_p), (o_i, d_i, tm_i)):
-                oracle.trace(b, h, v, idx, oo, dd, nthreads=nthreads)
-                oracle.trace(b, h, v, idx, oo, dd, tmax=tm, any_hit=True, nthreads=nthreads)
-                rays += 2 * oo.shape[0]
+        for b, h, v, idx, oo, dd, tm in work:
+            oracle.trace(b, h, v, idx, oo, dd, nthreads=nthreads)
+            oracle.trace(b, h, v, idx, oo, dd, tmax=tm, any_hit=True, nthreads=nthreads)
+            rays += 2 * oo.shape[0]
         return rays
 
     for _ in range(args.warmup):
@@ -848,16 +979,18 @@ def run_reference(args):
     rays = sum(step() for _ in range(args.steps))
     dt = time.perf_counter() - t0
     value = rays / dt / 1e6
+    sample = (f"first {S} rays (the top {S // side} rows of the primary image, and their incoherent rays) of each "
+              f"of the {2 * len(work)} launches per step, oracle restatement on {nthreads} threads (the reference "
+              f"traversal is GLSL/OpenGL, unavailable on this box)")
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": {"workload": "MTBVH traversal microbench (triangle soups, 2^24 coherent primary + 2^24 "
                                    "incoherent rays, closest-hit and any-hit)",
-                       "triangles": sizes, "rays_per_launch": side * side, "parallelism": "host threads"},
+                       "triangles": sizes, "rays_per_launch": nray, "launches_per_step": 2 * len(work),
+                       "rays_traced_per_launch": S, "parallelism": "host threads"},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{sample} sampled primary rays + their incoherent rays per scene, closest "
-                                       f"and any-hit, oracle restatement (the reference traversal is GLSL/OpenGL, "
-                                       f"unavailable on this box)"},
+                             "sample": sample},
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

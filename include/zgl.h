@@ -104,11 +104,12 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices,
 
 /* Trace kernel schedule of an accelerator: ZGL_TRACE_AUTO (0, default),
  * ZGL_TRACE_THREAD_PER_RAY (1: one thread per ray, neighbouring rays share a
- * warp) or ZGL_TRACE_PERSISTENT (2: persistent warps that refill idle lanes
- * by atomic fetch).  Results are identical; only speed differs.  The
- * reference has one fixed schedule (one invocation per pixel or path,
- * src/integrator/NaivePath.cpp:94-100). */
-enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2 };
+ * warp), ZGL_TRACE_PERSISTENT (2: persistent warps that refill idle lanes
+ * by atomic fetch) or ZGL_TRACE_DEFERRED (3: one thread per ray with leaf
+ * triangle tests deferred and run warp-wide).  Results are identical; only
+ * speed differs.  The reference has one fixed schedule (one invocation per
+ * pixel or path, src/integrator/NaivePath.cpp:94-100). */
+enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2, ZGL_TRACE_DEFERRED = 3 };
 zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule);
 
 /* Closest hit of n rays (origins/dirs float[n*3]): hit_id int32[n] (primitive
@@ -134,16 +135,21 @@ zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const f
 /* Allocation-free variant of zgl_trace_closest, for callers that must not
  * let the library allocate device memory (a frame loop under a fixed memory
  * budget, or an application whose own pool allocator owns the device).  No
- * counterpart in the reference.  The kernel's scratch (the persistent work
- * counter) and the staging area for host arrays live in one static device
- * array of 8 MiB + 256 B that every GPU loading the library holds until the
- * process exits; the call makes no cudaMalloc or cudaFree.  n is limited to
- * 262144 rays per call (larger n returns ZGL_ERR_INVALID_ARG); arrays may be
- * host or device memory, as for zgl_trace_closest.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current, so make that first call before any stream capture.  All calls
- * share the array: calls whose GPU work overlaps (other streams, other host
- * threads) race on it and must be serialised by the caller. */
+ * counterpart in the reference.  It runs the schedule set with
+ * zgl_accel_set_trace_schedule, like zgl_trace_closest; the persistent
+ * schedule's work counter and the staging area for host arrays live in one
+ * static device array of 8 MiB + 256 B, and the call makes no cudaMalloc or
+ * cudaFree.  n is limited to 262144 rays per call (larger n returns
+ * ZGL_ERR_INVALID_ARG); arrays may be host or device memory, as for
+ * zgl_trace_closest.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current.  Under CUDA's lazy
+ * module loading that lookup is also when the device reserves the array, so
+ * the first call can fail with ZGL_ERR_CUDA when the device is out of memory:
+ * make one warm-up call (n = 1) on each device before a budgeted frame loop
+ * and before any stream capture.  From then on every GPU that loaded the
+ * library holds the array until the process exits.  All calls share the
+ * array: calls whose GPU work overlaps (other streams, other host threads)
+ * race on it and must be serialised by the caller. */
 zgl_status zgl_trace_closest_noalloc(const zgl_accel* accel, const float* origins, const float* dirs,
                                      size_t n, int32_t* hit_id, float* hit_t, void* stream);
 

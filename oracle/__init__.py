@@ -230,6 +230,9 @@ def _render_lib():
         L.orc_render_triple.restype = None
         L.orc_render_triple.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                         C.c_void_p]
+        L.orc_render_mt.restype = None
+        L.orc_render_mt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_void_p, C.c_int32]
         L.orc_alias_build.restype = None
         L.orc_alias_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.orc_transc.restype = None
@@ -455,6 +458,17 @@ class OracleScene:
         W, H = self.s.filmW, self.s.filmH
         film = np.zeros((H, W, 3), np.float32)
         _render_lib().orc_render_triple(C.byref(self.s), spp0, passes, fc0, blocks, loops, _p(film))
+        return film
+
+    def render_threaded(self, kind, passes, blocks, loops=1, spp0=0, fc0=1, nthreads=None):
+        """Light tracer (kind "light") or triple integrator (kind "triple")
+        passes on `nthreads` host threads with per-thread films: the CPU
+        baseline's timing path.  Equal to render_lt / render_triple up to the
+        order of float additions."""
+        W, H = self.s.filmW, self.s.filmH
+        film = np.zeros((H, W, 3), np.float32)
+        _render_lib().orc_render_mt(C.byref(self.s), 0 if kind == "light" else 1, spp0, passes, fc0, blocks, loops,
+                                    _p(film), nthreads or threads())
         return film
 
     def diff_grad(self, data, spp, dimage, nthreads=None):

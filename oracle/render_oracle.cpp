@@ -1699,6 +1699,73 @@ void orc_render_triple(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t
     }
 }
 
+// The same passes on `nthreads` host threads, for timing the oracle as a CPU
+// baseline: camera pixels by rows, light paths in contiguous ranges, each
+// thread splatting into its own film; the films are summed at the end, so
+// the result equals the sequential one up to the order of float additions.
+static void camera_rows(const OrcScene* sc, int spp, int fc, int y0, int y1, float* film) {
+    for (int py = y0; py < y1; py++)
+        for (int px = 0; px < sc->filmW; px++) {
+            vec2 texSize((float)sc->filmW, (float)sc->filmH);
+            vec2 scr = vec2((float)px, (float)py) / texSize;
+            vec2 nc = noiseTexture(*sc, scr);
+            nc = noiseTexture(*sc, nc);
+            vec2 tc = texSize * nc;
+            Rng g;
+            g.randSeed = f2u(tc.x) * (uint32_t)fc + f2u(tc.y);
+            g.sampleSeed = f2u(tc.x) * f2u(tc.y);
+            int off = (int)((uint32_t)spp * 256u);
+            if (off > 131072 * 256) off -= 131072 * 256;
+            g.sampleOffset = off;
+            int s = 0;
+            float u0 = sample1D(*sc, g, s), u1 = sample1D(*sc, g, s), u2 = sample1D(*sc, g, s), u3 = sample1D(*sc, g, s);
+            Ray ray = thinLensCameraSampleRay(*sc, scr, u0, u1, u2, u3);
+            vec3 r = traceCameraPath(*sc, ray, g, s);
+            if (!hasNan(r)) {
+                float* p = film + 3 * ((size_t)py * sc->filmW + px);
+                p[0] += r.x;
+                p[1] += r.y;
+                p[2] += r.z;
+            }
+        }
+}
+
+void orc_render_mt(const OrcScene* sc, int32_t kind, int32_t spp0, int32_t passes, int32_t fc0, int32_t blocks,
+                   int32_t loops, float* film, int32_t nthreads) {
+    const int T = std::max(1, (int)nthreads);
+    const size_t npix = (size_t)sc->filmW * sc->filmH * 3;
+    std::vector<std::vector<float>> part((size_t)T, std::vector<float>(npix, 0.0f));
+    const uint32_t paths = 1536u * (uint32_t)blocks;
+    const uint32_t group = kind == 0 ? paths : paths * (uint32_t)loops;
+    const float uScale = (float)(sc->filmW * sc->filmH) / (float)(blocks * loops * 1536);
+    auto work = [&](int t) {
+        float* f = part[(size_t)t].data();
+        for (int k = 0; k < passes; k++) {
+            const uint32_t spp = (uint32_t)(spp0 + k), fc = (uint32_t)(fc0 + k);
+            if (kind == 1) {
+                const int y0 = (int)((int64_t)sc->filmH * t / T), y1 = (int)((int64_t)sc->filmH * (t + 1) / T);
+                camera_rows(sc, (int)spp, (int)fc, y0, y1, f);
+            }
+            const uint32_t g0 = (uint32_t)((uint64_t)paths * t / T), g1 = (uint32_t)((uint64_t)paths * (t + 1) / T);
+            for (uint32_t gid = g0; gid < g1; gid++) {
+                Rng g;
+                g.randSeed = spp * group + gid + fc;
+                g.sampleSeed = 0;
+                g.sampleOffset = 0;
+                if (kind == 0)
+                    lightIntegTrace(*sc, g, f);
+                else
+                    for (int i = 0; i < loops; i++) traceLightPath(*sc, g, f, uScale);
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; t++) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+    for (int t = 0; t < T; t++)
+        for (size_t i = 0; i < npix; i++) film[i] += part[(size_t)t][i];
+}
+
 // ----------------------------------------------------------- host tables
 
 // Light power split and alias table (Scene.cpp:200-243, AliasTable.h:12-54).

@@ -11,18 +11,21 @@ recurrence (Bratley & Fox; Joe & Kuo 2008)
 that reproduces the columns V_i = m_i << (32 - i), checks that regenerating
 the matrices gives the table back bit for bit, and writes the compact
 direction numbers to ``zillumgl_gb300/csrc/sobol_dirnums.inc``.  The library
-regenerates the matrices from them (csrc/tables.cpp).  Run once in a tree that
-has the reference sources; the output is committed.
+regenerates the matrices from them (csrc/scene.cpp), and tests/test_tables.py
+checks the result against the reference table's SHA-256.  Run once where the
+reference sources are present ($ZGL_REFERENCE_TREE names the tree); the
+output is committed.
 """
 from __future__ import annotations
 
+import os
 import re
 import sys
 from pathlib import Path
 
-HERE = Path(__file__).resolve().parent
-OUT = HERE.parent / "csrc" / "sobol_dirnums.inc"
-SRC = Path("/root/reference/src/math/SobolMatrices256x32.h")
+ROOT = Path(__file__).resolve().parents[2]
+OUT = ROOT / "zillumgl_gb300" / "csrc" / "sobol_dirnums.inc"
+SRC = Path(os.environ.get("ZGL_REFERENCE_TREE", "/root/reference")) / "src" / "math" / "SobolMatrices256x32.h"
 
 
 def read_matrices(path: Path) -> list[list[int]]:
@@ -64,7 +67,7 @@ def main() -> int:
     lines = [
         "// sobol_dirnums.inc — direction numbers of Sobol dimensions 1..255:",
         "// {degree s, coefficient bits a, m_1 .. m_s}.  Dimension 0 is the",
-        "// van der Corput sequence.  Generated by zillumgl_gb300/data/make_sobol_dirnums.py;",
+        "// van der Corput sequence.  Generated by tests/golden/make_sobol_dirnums.py;",
         "// the matrices they generate equal the renderer's 256x32 table bit for bit.",
     ]
     for s, a, mi in rows:

@@ -2,7 +2,8 @@
 
 * Traversal (1M / 4M / 16M triangle soups, seeds 101 / 104 / 116): the
   device-built PackedBVH equals the oracle's quickBuild + buildHitTable bit
-  for bit, and every one of the 2^24 rays of each of the four ray sets the
+  for bit and hashes to the PackedBVH of the reference's own BVH::build()
+  (tests/golden/reference_pins.json), and every one of the 2^24 rays of each of the four ray sets the
   benchmark traces (coherent primary and incoherent; closest-hit and any-hit)
   gives the oracle's hit id, distance, occlusion flag and per-ray visit / test
   counters bit for bit (src/shader/intersection.glsl:367-427).
@@ -22,17 +23,21 @@
 from __future__ import annotations
 
 import gc
+import json
+from pathlib import Path
 
 import numpy as np
 import pytest
 
 import oracle
+from tests.reference_pin_cases import sha256
 from zillumgl_gb300 import BVH
 from zillumgl_gb300.synthetic import (TRAVERSAL_SEEDS, city_scene, cornell_scene, diff_scene, incoherent_rays,
                                       primary_rays, shadow_tmax, triangle_soup)
 
 pytestmark = pytest.mark.gpu
 
+PINS = json.loads((Path(__file__).resolve().parent / "golden" / "reference_pins.json").read_text())
 REL_TOL = 1e-4
 GRAD_ABS = 2e-3
 GRAD_REL = 1e-3
@@ -60,6 +65,8 @@ def test_traversal_configuration_all_rays(zgl_lib, cuda, size):
     assert _same_bits(packed.bounds, ob), "device-built bounds differ from the oracle's quickBuild"
     assert np.array_equal(packed.hitTable, oh), "device-built hit tables differ from the oracle's buildHitTable"
     del ob, oh
+    assert sha256(packed.bounds, packed.hitTable) == PINS["soups"][f"soup_{size}"]["sha256"], \
+        "device-built PackedBVH differs from the reference's BVH::build()"
     n = 4096 * 4096
     o_p, d_p = primary_rays(4096, 4096)
     sets = []

@@ -55,16 +55,21 @@ def soup(zgl_lib, cuda):
     acc.close()
 
 
-def test_primary_and_incoherent_closest_bit_exact(soup, cuda):
+@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "deferred"])
+def test_primary_and_incoherent_closest_bit_exact(soup, cuda, schedule):
     acc, packed, v, idx = soup
-    o, d = primary_rays(96, 96)
-    hid, ht = _check_closest(acc, packed, v, idx, o, d, cuda)
-    assert (hid >= 0).mean() > 0.2
-    o2, d2 = incoherent_rays(v, idx, o, d, hid, ht, seed=9)
-    _check_closest(acc, packed, v, idx, o2, d2, cuda)
+    acc.set_trace_schedule(schedule)
+    try:
+        o, d = primary_rays(96, 96)
+        hid, ht = _check_closest(acc, packed, v, idx, o, d, cuda)
+        assert (hid >= 0).mean() > 0.2
+        o2, d2 = incoherent_rays(v, idx, o, d, hid, ht, seed=9)
+        _check_closest(acc, packed, v, idx, o2, d2, cuda)
+    finally:
+        acc.set_trace_schedule("auto")
 
 
-@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent"])
+@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent", "deferred"])
 def test_mixed_rays_closest_bit_exact(soup, cuda, schedule):
     acc, packed, v, idx = soup
     acc.set_trace_schedule(schedule)
@@ -75,7 +80,7 @@ def test_mixed_rays_closest_bit_exact(soup, cuda, schedule):
         acc.set_trace_schedule("auto")
 
 
-@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent"])
+@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent", "deferred"])
 def test_any_hit_bit_exact(soup, cuda, schedule):
     import torch
 

@@ -77,6 +77,33 @@ trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __
     tests[i] = t;
 }
 
+// Deferred-leaf schedule (traverse_deferred): one ray per thread, neighbouring
+// rays in one warp; the warp runs the general-direction loop unless one of
+// its rays needs the axis-dominant or near-zero-component box test.
+constexpr int kDeferQueue = 3;
+
+template <bool ANY>
+__global__ void __launch_bounds__(kTraceBlock)
+trace_deferred_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                      const float* __restrict__ tmax, int64_t n, int32_t* __restrict__ hit_id,
+                      float* __restrict__ hit_t, uint8_t* __restrict__ occ) {
+    const int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    const bool active = i < n;
+    const int64_t j = active ? i : n - 1;
+    const TraceRay r = make_trace_ray(load3(org, j), load3(dir, j));
+    float dist = ANY ? tmax[j] : 1e8f;
+    const bool general = __all_sync(0xffffffffu, !active || r.mode == 3);
+    const int res = general ? traverse_deferred<ANY, kDeferQueue, 3>(a, r, active, dist)
+                            : traverse_deferred<ANY, kDeferQueue, -1>(a, r, active, dist);
+    if (!active) return;
+    if (ANY) {
+        occ[i] = (uint8_t)res;
+    } else {
+        hit_id[i] = res;
+        hit_t[i] = dist;
+    }
+}
+
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 // ---------------------------------------------------------------------------
@@ -206,9 +233,15 @@ cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M
 }
 
 cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
-                                 int32_t* hit_id, float* hit_t, unsigned long long* counter, cudaStream_t s) {
+                                 int32_t* hit_id, float* hit_t, int schedule, unsigned long long* counter,
+                                 cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M == 0 || counter == nullptr) {
+    if (a.M > 0 && schedule == ZGL_TRACE_DEFERRED) {
+        trace_deferred_kernel<false><<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, nullptr, n, hit_id,
+                                                                                      hit_t, nullptr);
+        return cudaGetLastError();
+    }
+    if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
         trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
         return cudaGetLastError();
     }
@@ -223,9 +256,14 @@ cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* d
 }
 
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
-                             int64_t n, uint8_t* occ, unsigned long long* counter, cudaStream_t s) {
+                             int64_t n, uint8_t* occ, int schedule, unsigned long long* counter, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M == 0 || counter == nullptr) {
+    if (a.M > 0 && schedule == ZGL_TRACE_DEFERRED) {
+        trace_deferred_kernel<true><<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, nullptr,
+                                                                                     nullptr, occ);
+        return cudaGetLastError();
+    }
+    if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
         trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
         return cudaGetLastError();
     }
@@ -370,10 +408,10 @@ private:
     int prev_ = 0, dev_ = 0;
 };
 
-// The auto schedule is thread-per-ray: neighbouring rays of a batch stay in
-// one warp, which keeps their node fetches coalesced.
-unsigned long long* persistent_counter(const zgl_accel* a) {
-    return a->trace_schedule == ZGL_TRACE_PERSISTENT ? a->d_counter : nullptr;
+// The schedule a trace call runs.  Auto is one thread per ray: neighbouring
+// rays of a batch stay in one warp, which keeps their node fetches coalesced.
+int trace_schedule(const zgl_accel* a) {
+    return a->trace_schedule == ZGL_TRACE_AUTO ? ZGL_TRACE_THREAD_PER_RAY : a->trace_schedule;
 }
 
 int host_threads() {
@@ -580,7 +618,7 @@ zgl_status zgl_accel_destroy(zgl_accel* accel) {
 zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule) {
     ZGL_API_BEGIN
     if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: NULL accel");
-    if (schedule < ZGL_TRACE_AUTO || schedule > ZGL_TRACE_PERSISTENT)
+    if (schedule < ZGL_TRACE_AUTO || schedule > ZGL_TRACE_DEFERRED)
         fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: unknown schedule %d", schedule);
     accel->trace_schedule = schedule;
     ZGL_API_END
@@ -600,7 +638,8 @@ zgl_status zgl_trace_closest(const zgl_accel* accel, const float* origins, const
     int si = st.add(hit_id, 4 * n, false, true), sx = st.add(hit_t, 4 * n, false, true);
     st.commit();
     ZGL_CUDA(launch_trace_closest(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
-                                  (int64_t)n, (int32_t*)st.ptr(si), (float*)st.ptr(sx), persistent_counter(accel), s));
+                                  (int64_t)n, (int32_t*)st.ptr(si), (float*)st.ptr(sx), trace_schedule(accel),
+                                  accel->d_counter, s));
     st.finish();
     ZGL_API_END
 }
@@ -619,8 +658,8 @@ zgl_status zgl_trace_any(const zgl_accel* accel, const float* origins, const flo
     int sm = st.add(tmax, 4 * n, true, false), sc = st.add(occluded, n, false, true);
     st.commit();
     ZGL_CUDA(launch_trace_any(device_view(accel), (const float*)st.ptr(so), (const float*)st.ptr(sd),
-                              (const float*)st.ptr(sm), (int64_t)n, (uint8_t*)st.ptr(sc), persistent_counter(accel),
-                              s));
+                              (const float*)st.ptr(sm), (int64_t)n, (uint8_t*)st.ptr(sc), trace_schedule(accel),
+                              accel->d_counter, s));
     st.finish();
     ZGL_API_END
 }
@@ -656,9 +695,9 @@ zgl_status zgl_trace_count(const zgl_accel* accel, const float* origins, const f
 // memory to its own pool allocator, cannot afford an allocation that may fail
 // mid-frame or that synchronises the whole device.  zgl_trace_closest_noalloc
 // serves them: the persistent trace kernel's scratch (its work counter) and
-// the staging area for host arrays live in one file-scope device array that
-// the library holds from the moment it is loaded until the process exits, on
-// every GPU that loads it.
+// the staging area for host arrays live in one file-scope device array.  With
+// lazy module loading a device reserves it when the first call looks up its
+// address; from then on the device holds it until the process exits.
 // ---------------------------------------------------------------------------
 namespace zgl {
 namespace {
@@ -722,11 +761,11 @@ zgl_status zgl_trace_closest_noalloc(const zgl_accel* accel, const float* origin
     float* d_t = ht ? reinterpret_cast<float*>(base + kNoAllocDist) : hit_t;
     if (ho) ZGL_CUDA(cudaMemcpyAsync(base + kNoAllocOrigins, origins, 12 * n, cudaMemcpyHostToDevice, s));
     if (hd) ZGL_CUDA(cudaMemcpyAsync(base + kNoAllocDirs, dirs, 12 * n, cudaMemcpyHostToDevice, s));
-    // the persistent schedule with its counter in the static array (reset here:
-    // the array keeps the previous call's contents); an empty accelerator
-    // takes the counter-free kernel
-    ZGL_CUDA(launch_trace_closest(device_view(accel), d_org, d_dir, (int64_t)n, d_id, d_t,
-                                  accel->M > 0 ? counter : nullptr, s));
+    // the accelerator's schedule; the persistent one keeps its work counter in
+    // the static array (the launcher resets it on the stream, since the array
+    // keeps the previous call's contents)
+    ZGL_CUDA(launch_trace_closest(device_view(accel), d_org, d_dir, (int64_t)n, d_id, d_t, trace_schedule(accel),
+                                  counter, s));
     if (hi) ZGL_CUDA(cudaMemcpyAsync(hit_id, d_id, 4 * n, cudaMemcpyDeviceToHost, s));
     if (ht) ZGL_CUDA(cudaMemcpyAsync(hit_t, d_t, 4 * n, cudaMemcpyDeviceToHost, s));
     if (ho || hd || hi || ht) ZGL_CUDA(cudaStreamSynchronize(s));

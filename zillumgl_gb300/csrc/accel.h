@@ -59,11 +59,14 @@ inline DeviceAccel device_view(const zgl_accel* a) {
 // Kernel launchers (accel.cu).  All pointers are device pointers.
 cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
                               cudaStream_t s);
-// `counter` non-null selects the persistent schedule.
+// `schedule` is ZGL_TRACE_THREAD_PER_RAY, ZGL_TRACE_PERSISTENT (which needs
+// `counter`, a device word it resets on the stream) or ZGL_TRACE_DEFERRED.
 cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
-                                 int32_t* hit_id, float* hit_t, unsigned long long* counter, cudaStream_t s);
+                                 int32_t* hit_id, float* hit_t, int schedule, unsigned long long* counter,
+                                 cudaStream_t s);
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
-                             int64_t n, uint8_t* occluded, unsigned long long* counter, cudaStream_t s);
+                             int64_t n, uint8_t* occluded, int schedule, unsigned long long* counter,
+                             cudaStream_t s);
 cudaError_t launch_trace_count(DeviceAccel a, const float* org, const float* dir, const float* tmax,
                                int64_t n, int any_hit, int32_t* visits, int32_t* tests,
                                cudaStream_t s);

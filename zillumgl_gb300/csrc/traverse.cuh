@@ -176,6 +176,87 @@ __device__ __forceinline__ int traverse_m(const DeviceAccel& a, const TraceRay& 
     return ANY ? (closest >= 0 ? 1 : 0) : closest;
 }
 
+// One table step of the deferred traversal: the box test of entry k with the
+// lane's current distance; a leaf that passes is queued instead of tested.
+template <int MODE>
+__device__ __forceinline__ bool deferred_box(const float4 lo, const float4 hi, const TraceRay& r, float& tmin) {
+    return MODE < 0 ? box_hit(lo, hi, r, tmin) : box_hit_m<MODE>(lo, hi, r, tmin);
+}
+
+// Warp-synchronous bvhHit / bvhTest with deferred leaf tests.  Every lane of
+// the warp must call it together (lanes without a ray pass active = false).
+//
+// A lane box-tests table entries in the reference order and, when a leaf
+// passes, queues (entry, primitive) and goes on to entry + 1 as if the
+// triangle missed.  The warp tests the queued triangles together, each lane
+// in its own queue order, once half of the lanes still at work have a queued
+// leaf, a queue is full, or a lane has reached the end of the table with
+// leaves queued.  A closest-hit lane whose queued triangle hits with t < dist
+// takes the new distance and restarts right after that leaf, dropping the
+// steps and leaves it took after it with the old distance; so every lane
+// replays exactly the reference's sequence of box tests and triangle tests
+// (the leaf's own box passed, so the reference's next entry is leaf + 1 in
+// both cases).  An any-hit lane keeps one distance throughout and stops at
+// the first hit.  The triangle branch, taken by a few lanes per step in the
+// one-thread-per-ray loop, now runs once for many lanes.
+template <bool ANY, int Q, int MODE>
+__device__ __forceinline__ int traverse_deferred(const DeviceAccel& a, const TraceRay& r, bool active,
+                                                 float& dist) {
+    const unsigned kAll = 0xffffffffu;
+    const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
+    const int M = a.M;
+    int k = active ? 0 : M;
+    int closest = -1;
+    int cnt = 0;
+    int qk[Q], qp[Q];
+#pragma unroll
+    for (int j = 0; j < Q; j++) qk[j] = qp[j] = 0;
+    for (;;) {
+        if (k < M) {
+            const float4 lo = __ldg(base + 2 * k);
+            const float4 hi = __ldg(base + 2 * k + 1);
+            float tmin;
+            const bool h = deferred_box<MODE>(lo, hi, r, tmin) && !(tmin > dist);
+            const int prim = __float_as_int(lo.w);
+            if (h && prim >= 0) {
+#pragma unroll
+                for (int j = 0; j < Q; j++)
+                    if (j == cnt) {
+                        qk[j] = k;
+                        qp[j] = prim;
+                    }
+                cnt++;
+            }
+            k = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+        }
+        const unsigned pend = __ballot_sync(kAll, cnt > 0);
+        const unsigned must = __ballot_sync(kAll, cnt == Q || (cnt > 0 && k >= M));
+        const unsigned work = __ballot_sync(kAll, k < M);
+        if (must != 0u || (pend != 0u && 2 * __popc(pend) >= __popc(work | pend))) {
+            bool stop = false;
+#pragma unroll
+            for (int j = 0; j < Q; j++) {
+                if (!stop && j < cnt) {
+                    float t;
+                    if (tri_hit(a.tris, qp[j], r, t) && t < dist) {
+                        closest = qp[j];
+                        stop = true;
+                        if (ANY) {
+                            k = M;
+                        } else {
+                            dist = t;
+                            k = qk[j] + 1;
+                        }
+                    }
+                }
+            }
+            cnt = 0;
+        }
+        if (__ballot_sync(kAll, k < M || cnt > 0) == 0u) break;
+    }
+    return ANY ? (closest >= 0 ? 1 : 0) : closest;
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ int traverse(const DeviceAccel& a, const TraceRay& r, float& dist, int& visits,
                                         int& tests) {
