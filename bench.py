@@ -740,12 +740,50 @@ def run_diff(args, stream, dev):
     ef[2].record(stream)
     stream.synchronize()
     loss_first, loss_last = float(losses[0]), float(losses[-1])
+    # the fused step (zgl_diff_step_l2): forward, loss, adjoint in one kernel
+    gimg = torch.empty_like(img)
+    gbuf = torch.empty(p.numel(), dtype=torch.float32, device=dev)
+    lbuf = torch.empty(1, dtype=torch.float32, device=dev)
+    for _ in range(2):
+        dr.step_l2(target, image=gimg, grad=gbuf, loss=lbuf, stream=stream)
+    fe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    for k in range(n):
+        fe[k][0].record(stream)
+        dr.step_l2(target, image=gimg, grad=gbuf, loss=lbuf, stream=stream)
+        fe[k][1].record(stream)
+    stream.synchronize()
+    fused_ms = sorted(a.elapsed_time(b) for a, b in fe)[n // 2]
+    # a full Adam iteration on the fused step
+    losses_f = []
+
+    def fused_iteration():
+        dr.set_params(p.detach())
+        dr.step_l2(target, image=gimg, grad=gbuf, loss=lbuf, stream=stream)
+        with torch.cuda.stream(stream):
+            p.grad = gbuf
+            opt.step()
+            with torch.no_grad():
+                p.clamp_(0.01, 100.0)
+        losses_f.append(lbuf.clone())
+
+    fused_iteration()
+    stream.synchronize()
+    e0.record(stream)
+    for _ in range(n):
+        fused_iteration()
+    e1.record(stream)
+    stream.synchronize()
+    fused_it_ms = e0.elapsed_time(e1) / n
     dr.close()
     scene.close()
     res = {"film": [W, H], "spp": spp, "params": params, "n_params": int(p.numel()),
            "fwd_bwd_ms": round(fb_ms, 2), "iteration_ms": round(it_ms, 2),
            "forward_ms": round(ef[0].elapsed_time(ef[1]), 2), "backward_ms": round(ef[1].elapsed_time(ef[2]), 2),
            "samples_per_s_fwd_bwd": round(W * H * spp / (fb_ms * 1e-3), 1),
+           "fused_step_ms": round(fused_ms, 2), "fused_iteration_ms": round(fused_it_ms, 2),
+           "fused_samples_per_s": round(W * H * spp / (fused_ms * 1e-3), 1),
+           "fused_note": "zgl_diff_step_l2: forward, L2 loss and adjoint in one kernel, ray casts kept between the "
+                         "forward and the replay; iteration = parameter upload + step + Adam",
            "loss_first": loss_first, "loss_last": loss_last, "iterations": len(losses)}
     res["grad_check"] = diff_grad_check()
     if not args.no_cpu_baseline:

@@ -452,6 +452,21 @@ zgl_status zgl_diff_forward(zgl_diff* diff, float* image, void* stream);
  * param_count floats, overwritten with the gradient.  Uses the per-sample
  * radiance kept by the last zgl_diff_forward. */
 zgl_status zgl_diff_backward(zgl_diff* diff, const float* d_image, float* d_params, void* stream);
+
+/* One inverse-rendering step of the image loss
+ *   loss = loss_scale * sum over pixels and channels of (image - target)^2
+ * in a single kernel (new, no counterpart in the reference): every
+ * (pixel, sample) path is traced once, the image (as zgl_diff_forward makes
+ * it), the loss and dloss/dimage = 2 loss_scale (image - target) are formed
+ * per pixel, and the paths are replayed from their sampler states with the
+ * ray-cast results kept from the forward pass in thread-local memory (hit ids,
+ * distances and light-sample occlusion of up to 8 bounces; deeper bounces are
+ * traced again).  d_params receives the gradient as zgl_diff_backward would
+ * for that d_image (up to the order of the float atomics), `loss` one float.
+ * target and image are device float[H*W*3]; spp must be at most 128.  Does
+ * not touch the per-sample buffer of zgl_diff_forward / zgl_diff_backward. */
+zgl_status zgl_diff_step_l2(zgl_diff* diff, const float* target, float loss_scale, float* image,
+                            float* d_params, float* loss, void* stream);
 zgl_status zgl_diff_destroy(zgl_diff* diff);
 
 /* ------------------------------------------------------------------------ */

@@ -187,3 +187,40 @@ def test_parameter_validation(zgl_lib, cuda):
     dr.set_params(q)
     img2 = dr.forward()
     assert np.allclose(img2.cpu().numpy(), 2 * img1.cpu().numpy(), rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("spp,depth", [(32, 6), (3, 4), (40, 5), (4, 11)])
+def test_fused_l2_step_equals_forward_then_backward(zgl_lib, cuda, spp, depth):
+    """zgl_diff_step_l2: the image equals zgl_diff_forward's bit for bit, the
+    loss the mean squared error, and the gradient zgl_diff_backward's for
+    dL/dimage = 2 (image - target) / numel up to the order of the float
+    atomics (relative 5e-5 of the largest component); one chunk of 32
+    samples, a partial chunk, two chunks, and paths deeper than the
+    recorded ray casts (traced again)."""
+    import torch
+
+    d = diff_scene(seed=28, width=24, height=20)
+    params = dict(max_depth=depth, russian_roulette=1, rr_start_depth=3) if depth > 8 else dict(max_depth=depth)
+    sc = Scene(d)
+    dr = DiffRenderer(sc, spp, **params)
+    rng = np.random.default_rng(29)
+    target = torch.from_numpy(rng.uniform(0.0, 0.6, (20, 24, 3)).astype(np.float32)).cuda()
+    img, grad, loss = dr.step_l2(target)
+    torch.cuda.synchronize()
+    ref_img = dr.forward()
+    assert torch.equal(img.view(torch.int32), ref_img.view(torch.int32))
+    diff = ref_img - target
+    ref_loss = float((diff.double() ** 2).mean())
+    assert abs(float(loss) - ref_loss) <= 1e-5 * ref_loss
+    ref_grad = dr.backward(diff * (2.0 / diff.numel())).cpu().numpy().astype(np.float64)
+    g = grad.cpu().numpy().astype(np.float64)
+    assert np.abs(g - ref_grad).max() <= 5e-5 * np.abs(ref_grad).max() + 1e-12, \
+        f"max diff {np.abs(g - ref_grad).max():.3g} of {np.abs(ref_grad).max():.3g}"
+    assert np.abs(ref_grad).max() > 0
+    orc = oracle.OracleScene(d, sc.export("sobol"), params)
+    dimg = (diff * (2.0 / diff.numel())).cpu().numpy()
+    o = orc.diff_grad(d, spp, dimg)
+    tol = GRAD_ABS * np.abs(o).max() + GRAD_REL * np.abs(o)
+    assert np.all(np.abs(g - o) <= tol)
+    dr.close()
+    sc.close()

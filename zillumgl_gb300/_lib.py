@@ -89,6 +89,8 @@ SIGNATURES: dict[str, tuple] = {
     "zgl_diff_set_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "zgl_diff_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "zgl_diff_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "zgl_diff_step_l2": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
     "zgl_diff_destroy": (C.c_int32, [C.c_void_p]),
     "zgl_postprocess": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
                                     C.c_void_p]),

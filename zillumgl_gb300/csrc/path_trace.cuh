@@ -20,8 +20,9 @@ struct PathParams {
     float portion;
 };
 
-__device__ __forceinline__ LiSample sampleLightAndEnv(const DeviceScene& sc, const PathParams& pp, v3 x, float ud,
-                                                      float u0, float u1, float u2, float u3) {
+template <class Vis>
+__device__ __forceinline__ LiSample sampleLightAndEnvV(const DeviceScene& sc, const PathParams& pp, v3 x, float ud,
+                                                       float u0, float u1, float u2, float u3, const Vis& vis) {
     float pdfSampleLight = 0.0f;  // light.glsl:221-235
     if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
     bool sampleLight = ud < pdfSampleLight;
@@ -29,13 +30,17 @@ __device__ __forceinline__ LiSample sampleLightAndEnv(const DeviceScene& sc, con
     LiSample s;
     if (sampleLight) {
         int id = lightSampleOne(sc, mk2(u0, u1));
-        s = lightSampleLi(sc, id, x, mk2(u2, u3));
+        s = lightSampleLiV(sc, id, x, mk2(u2, u3), vis);
     } else {
-        s = envSampleLi(sc, x, u0, u1, u2, u3);
+        s = envSampleLiV(sc, x, u0, u1, u2, u3, vis);
     }
     s.coef = s.coef / pdfSelect;
     s.pdf *= pdfSelect;
     return s;
+}
+__device__ __forceinline__ LiSample sampleLightAndEnv(const DeviceScene& sc, const PathParams& pp, v3 x, float ud,
+                                                      float u0, float u1, float u2, float u3) {
+    return sampleLightAndEnvV(sc, pp, x, ud, u0, u1, u2, u3, TraceVis{});
 }
 
 __device__ __forceinline__ float pdfSelectLight(const DeviceScene& sc, const PathParams& pp, int id) {
@@ -47,11 +52,24 @@ __device__ __forceinline__ float pdfSelectEnv(const DeviceScene& sc, const PathP
     return pp.uniformSel ? (1.0f - pp.portion) : sc.envSum / (sc.lightSum + sc.envSum);
 }
 
-// pathIntegTrace (path_integ_naive.glsl:35-143)
-template <bool FULL>
-__device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g) {
+// Ray casts of a path: closest hits in path order (`hit`) and the light
+// samples' occlusion tests (operator(), the TraceVis interface).  DirectCast
+// traverses the accelerator for both.
+struct DirectCast {
+    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
+        return bvhHit(sc, r, dist);
+    }
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        return bvhTest(sc, r, dist);
+    }
+};
+
+// pathIntegTrace (path_integ_naive.glsl:35-143) with the ray casts of `rc`
+template <bool FULL, class RC>
+__device__ __forceinline__ v3 pathTraceRC(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g,
+                                          const RC& rc) {
     float primDist;
-    int id = bvhHit(sc, ray, primDist);
+    int id = rc.hit(sc, ray, primDist);
     v3 pos = rayPoint(ray, primDist);
     if (id == -1) return envLe(sc, ray.dir);
     if (id - sc.objPrimCount >= 0) return lightLe(sc, id - sc.objPrimCount, pos, -ray.dir);
@@ -72,7 +90,7 @@ __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sa
         if (pp.sampleLight) {
             float ud = sample1D(g);
             float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
-            LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
+            LiSample ls = sampleLightAndEnvV(sc, pp, pos, ud, u0, u1, u2, u3, rc);
             if (ls.pdf > 0.0f) {
                 v3 f = materialBSDF<FULL>(matType, mp, wo, ls.wi, surf.ns);
                 float fpdf = materialPdf<FULL>(matType, mp, wo, ls.wi, surf.ns);
@@ -89,7 +107,7 @@ __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sa
         throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
         ray = rayOffseted(pos, wi);
         float dist;
-        int nextId = bvhHit(sc, ray, dist);
+        int nextId = rc.hit(sc, ray, dist);
         int lightId = nextId - sc.objPrimCount;
         v3 nextPos = rayPoint(ray, dist);
         if (nextId == -1) {
@@ -121,6 +139,11 @@ __device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sa
         wo = -wi;
     }
     return result;
+}
+
+template <bool FULL>
+__device__ v3 pathTrace(const DeviceScene& sc, const PathParams& pp, Ray ray, Sampler& g) {
+    return pathTraceRC<FULL>(sc, pp, ray, g, DirectCast{});
 }
 
 __device__ __forceinline__ void load_sobol_row(const DeviceScene& sc, uint32_t sampleOffset, uint32_t* row) {

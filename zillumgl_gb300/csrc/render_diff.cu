@@ -165,60 +165,27 @@ __device__ __forceinline__ int power_grad(const DiffInfo& di, const float* param
     return base;
 }
 
-// Backward: one thread per (pixel, sample), blockIdx.y = sample.  The replay
-// of pathIntegTrace (path_integ_naive.glsl:35-143) runs in warp lockstep, one
-// bounce per iteration of a warp-uniform loop, so that each iteration's
-// gradients (one material, up to two light instances per lane) are reduced
-// across the warp before the shared-memory atomics.
-template <bool FULL>
-__global__ void __launch_bounds__(kTileX* kTileY, 16)
-diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
-                     int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
-                     float* __restrict__ grad) {
-    __shared__ uint32_t row[256];
-    __shared__ float sg[kMaxDiffParams];
-    for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY) sg[i] = 0.0f;
-    const int32_t s = blockIdx.y;
-    const uint32_t off = sample_offset(s);
-    load_sobol_row(sc, off, row);  // includes the barrier that publishes sg
-    const int tile = blockIdx.x;
-    const int px = (tile % tilesX) * kTileX + threadIdx.x;
-    const int py = (tile / tilesX) * kTileY + threadIdx.y;
-
-    bool alive = px < sc.filmW && py < sc.filmH;
-    v3 Lrem = mk3(0.0f), Ltot = mk3(0.0f), delta = mk3(0.0f);
-    size_t pix = 0;
-    if (alive) {
-        const size_t npix = (size_t)sc.filmW * sc.filmH;
-        pix = (size_t)py * sc.filmW + px;
-        const float* L = samples + 3 * ((size_t)s * npix + pix);
-        Lrem = mk3(L[0], L[1], L[2]);
-        Ltot = Lrem;
-        const float inv = 1.0f / (float)spp;
-        delta = mk3(dimage[3 * pix] * inv, dimage[3 * pix + 1] * inv, dimage[3 * pix + 2] * inv);
-        // NaN samples are left out of the image; zero adjoints need no replay
-        alive = !hasNan(Lrem) && (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f);
-    }
-    Sampler g;
-    Ray ray;
+// The replay of one path (pathIntegTrace, path_integ_naive.glsl:35-143) with
+// its gradient contributions, in warp lockstep: one bounce per iteration of a
+// warp-uniform loop, so that each iteration's gradients (one material, up to
+// two light instances per lane) are reduced across the warp before the
+// shared-memory atomics.  All 32 lanes of the warp call it together; a lane
+// with alive == false only takes part in the reductions.  `g` is the sample's
+// sampler right after its four camera dimensions, `ray` its camera ray, `L`
+// its radiance and `delta` dL/d(radiance) of the sample.  The ray casts come
+// from `rc` (traversal, or the results recorded by the forward pass).
+template <bool FULL, class RC>
+__device__ __forceinline__ void replayPath(const DeviceScene& sc, const PathParams& pp, const DiffInfo& di,
+                                           const float* __restrict__ params, float* sg, bool alive, Sampler& g,
+                                           Ray ray, v3 L, v3 delta, const RC& rc) {
+    v3 Lrem = L, Ltot = L;
     int id = -1;
     v3 pos = mk3(0.0f), wo = mk3(0.0f), throughput = mk3(1.0f);
     float pw[3];
     int pkey = -1;
     if (alive) {
-        const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
-        g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
-        g.sampleSeed = seed.x * seed.y;
-        g.sampleOffset = off;
-        g.dim = 0;
-        g.mode = sc.sampler;
-        g.rowCache = row;
-        g.mats = sc.sobol;
-        v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
-        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
-        ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
         float primDist;
-        id = bvhHit(sc, ray, primDist);
+        id = rc.hit(sc, ray, primDist);
         pos = rayPoint(ray, primDist);
         wo = -ray.dir;
         if (id == -1) {
@@ -260,7 +227,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 float pdfSampleLight = 0.0f;  // the light pick of sampleLightAndEnv
                 if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
                 const int lid = ud < pdfSampleLight ? lightSampleOne(sc, mk2(u0, u1)) : -1;
-                const LiSample ls = sampleLightAndEnv(sc, pp, pos, ud, u0, u1, u2, u3);
+                const LiSample ls = sampleLightAndEnvV(sc, pp, pos, ud, u0, u1, u2, u3, rc);
                 if (ls.pdf > 0.0f) {
                     BsdfGrad bg;
                     if (diffMat) bg = bsdfGrad(matType, mp, wo, ls.wi, surf.ns);
@@ -290,7 +257,7 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
                 throughput = throughput * (bs.bsdf / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
                 ray = rayOffseted(pos, wi);
                 float dist;
-                const int nextId = bvhHit(sc, ray, dist);
+                const int nextId = rc.hit(sc, ray, dist);
                 const int lightId = nextId - sc.objPrimCount;
                 const v3 nextPos = rayPoint(ray, dist);
                 if (nextId == -1) {
@@ -322,9 +289,221 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
         warp_flush<3>(sg, nkey, npw);
         warp_flush<3>(sg, hkey, hpw);
     }
+}
+
+// Backward: one thread per (pixel, sample), blockIdx.y = sample; the replay
+// traverses the accelerator again.
+template <bool FULL>
+__global__ void __launch_bounds__(kTileX* kTileY, 16)
+diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
+                     int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
+                     float* __restrict__ grad) {
+    __shared__ uint32_t row[256];
+    __shared__ float sg[kMaxDiffParams];
+    for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY) sg[i] = 0.0f;
+    const int32_t s = blockIdx.y;
+    const uint32_t off = sample_offset(s);
+    load_sobol_row(sc, off, row);  // includes the barrier that publishes sg
+    const int tile = blockIdx.x;
+    const int px = (tile % tilesX) * kTileX + threadIdx.x;
+    const int py = (tile / tilesX) * kTileY + threadIdx.y;
+
+    bool alive = px < sc.filmW && py < sc.filmH;
+    v3 L = mk3(0.0f), delta = mk3(0.0f);
+    size_t pix = 0;
+    if (alive) {
+        const size_t npix = (size_t)sc.filmW * sc.filmH;
+        pix = (size_t)py * sc.filmW + px;
+        const float* Ls = samples + 3 * ((size_t)s * npix + pix);
+        L = mk3(Ls[0], Ls[1], Ls[2]);
+        const float inv = 1.0f / (float)spp;
+        delta = mk3(dimage[3 * pix] * inv, dimage[3 * pix + 1] * inv, dimage[3 * pix + 2] * inv);
+        // NaN samples are left out of the image; zero adjoints need no replay
+        alive = !hasNan(L) && (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f);
+    }
+    Sampler g;
+    Ray ray;
+    if (alive) {
+        const uint2 seed = __ldg(&sc.pixelSeeds[pix]);
+        g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
+        g.sampleSeed = seed.x * seed.y;
+        g.sampleOffset = off;
+        g.dim = 0;
+        g.mode = sc.sampler;
+        g.rowCache = row;
+        g.mats = sc.sobol;
+        v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+        ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    }
+    replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, L, delta, DirectCast{});
     __syncthreads();
     for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY)
         if (sg[i] != 0.0f) atomicAdd(&grad[i], sg[i]);
+}
+
+// ----------------------------------------------------------------------------
+// Fused forward + adjoint of an image loss L = s * sum over pixels and
+// channels of (image - target)^2.  One warp per pixel, lane l carrying sample
+// 32 c + l of chunk c (up to kFuseChunks chunks of 32 samples).  Each lane
+// traces its sample once and keeps the path's ray-cast results (closest hits
+// and light-sample occlusion, kCastCache records) in thread-local memory; the
+// warp then forms the pixel's image value (samples summed in sample order,
+// NaN samples dropped, as zgl_diff_forward), the loss term and
+// dL/d(image) = 2 s (image - target), and replays every sample from its
+// sampler state with the recorded casts (traversal only past the cache).
+// The Sobol rows of the chunk's 32 sample indices sit in shared memory, one
+// padded row per lane.
+constexpr int kFuseWarps = 16;
+constexpr int kFuseMaxChunks = 4;  // spp <= 128
+constexpr int kCastCache = 9;  // closest hits of the camera ray and 8 bounces
+constexpr int kRowPad = 257;
+
+struct CastRecord {
+    int2 hit[kCastCache];  // primitive id, distance bits
+    uint32_t vis;          // light-sample occlusion, one bit per test in order
+    int32_t nhit, nvis;
+};
+
+// Records the casts of a traced path.
+struct RecordCast {
+    CastRecord* rec;
+    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
+        const int id = bvhHit(sc, r, dist);
+        if (rec->nhit < kCastCache) rec->hit[rec->nhit] = make_int2(id, __float_as_int(dist));
+        rec->nhit++;
+        return id;
+    }
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        const bool occ = bvhTest(sc, r, dist);
+        if (rec->nvis < 32 && occ) rec->vis |= 1u << rec->nvis;
+        rec->nvis++;
+        return occ;
+    }
+};
+
+// Plays the recorded casts back in the same order; casts beyond the record
+// are traced again.
+struct ReplayCast {
+    CastRecord* rec;
+    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
+        const int k = rec->nhit++;
+        if (k < kCastCache) {
+            const int2 h = rec->hit[k];
+            dist = __int_as_float(h.y);
+            return h.x;
+        }
+        return bvhHit(sc, r, dist);
+    }
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        const int k = rec->nvis++;
+        if (k < 32) return (rec->vis >> k) & 1u;
+        return bvhTest(sc, r, dist);
+    }
+};
+
+template <bool FULL, int CH>
+__global__ void __launch_bounds__(32 * kFuseWarps, 4)
+diff_fused_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t spp,
+                  const float* __restrict__ target, float lossScale, float* __restrict__ image,
+                  float* __restrict__ grad, float* __restrict__ loss) {
+    __shared__ uint32_t rows[32 * kRowPad];
+    __shared__ float sg[kMaxDiffParams];
+    __shared__ float sloss[kFuseWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < di.nparams; i += 32 * kFuseWarps) sg[i] = 0.0f;
+    const int64_t npix = (int64_t)sc.filmW * sc.filmH;
+    const int64_t pix = (int64_t)blockIdx.x * kFuseWarps + warp;
+    const bool pixOk = pix < npix;
+    const int px = pixOk ? (int)(pix % sc.filmW) : 0, py = pixOk ? (int)(pix / sc.filmW) : 0;
+    const uint2 seed = pixOk ? __ldg(&sc.pixelSeeds[pix]) : make_uint2(0u, 0u);
+    const v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
+    const int nchunks = CH;  // (spp + 31) / 32
+    CastRecord rec[CH];
+    v3 Ls[CH];
+
+    // Sobol rows of samples 32 c .. 32 c + 31, row l at rows[l * kRowPad]
+    auto load_rows = [&](int c) {
+        __syncthreads();
+        if (sc.sampler == 1)
+            for (int i = threadIdx.x; i < 32 * 256; i += 32 * kFuseWarps) {
+                const int l = i >> 8, d = i & 255;
+                rows[l * kRowPad + d] = sobol_value(sc.sobol, sample_offset(32 * c + l) >> 8, (uint32_t)d);
+            }
+        __syncthreads();
+    };
+    auto start = [&](int s, Sampler& g) {
+        g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
+        g.sampleSeed = seed.x * seed.y;
+        g.sampleOffset = sample_offset(s);
+        g.dim = 0;
+        g.mode = sc.sampler;
+        g.rowCache = rows + lane * kRowPad;
+        g.mats = sc.sobol;
+        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
+        return thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
+    };
+
+    // forward: every sample once, recording its casts
+#pragma unroll
+    for (int c = 0; c < nchunks; c++) {
+        load_rows(c);
+        const int s = 32 * c + lane;
+        rec[c].nhit = rec[c].nvis = 0;
+        rec[c].vis = 0u;
+        Ls[c] = mk3(0.0f);
+        if (pixOk && s < spp) {
+            Sampler g;
+            const Ray ray = start(s, g);
+            Ls[c] = pathTraceRC<FULL>(sc, pp, ray, g, RecordCast{&rec[c]});
+        }
+    }
+    // the pixel's image value: samples added in sample order, NaN dropped
+    v3 img = mk3(0.0f);
+#pragma unroll
+    for (int c = 0; c < nchunks; c++)
+        for (int l = 0; l < 32; l++) {
+            const v3 x = mk3(__shfl_sync(kFullMask, Ls[c].x, l), __shfl_sync(kFullMask, Ls[c].y, l),
+                             __shfl_sync(kFullMask, Ls[c].z, l));
+            if (32 * c + l < spp && !hasNan(x)) img = img + x;
+        }
+    img = img / (float)spp;
+    v3 delta = mk3(0.0f);
+    if (pixOk) {
+        const v3 t = mk3(__ldg(&target[3 * pix]), __ldg(&target[3 * pix + 1]), __ldg(&target[3 * pix + 2]));
+        const v3 diff = img - t;
+        const float two = 2.0f * lossScale;
+        delta = (diff * two) * (1.0f / (float)spp);
+        if (lane == 0) {
+            image[3 * pix] = img.x;
+            image[3 * pix + 1] = img.y;
+            image[3 * pix + 2] = img.z;
+            sloss[warp] = (diff.x * diff.x + diff.y * diff.y + diff.z * diff.z) * lossScale;
+        }
+    } else if (lane == 0) {
+        sloss[warp] = 0.0f;
+    }
+    const bool anyDelta = delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f;
+    // adjoint: replay every sample with its recorded casts
+#pragma unroll
+    for (int c = 0; c < nchunks; c++) {
+        if (nchunks > 1) load_rows(c);
+        const int s = 32 * c + lane;
+        const bool alive = pixOk && s < spp && anyDelta && !hasNan(Ls[c]);
+        Sampler g;
+        Ray ray;
+        if (alive) ray = start(s, g);
+        rec[c].nhit = rec[c].nvis = 0;
+        replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, Ls[c], delta, ReplayCast{&rec[c]});
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < di.nparams; i += 32 * kFuseWarps)
+        if (sg[i] != 0.0f) atomicAdd(&grad[i], sg[i]);
+    if (threadIdx.x == 0) {
+        float sl = 0.0f;
+        for (int w = 0; w < kFuseWarps; w++) sl += sloss[w];
+        if (sl != 0.0f) atomicAdd(loss, sl);
+    }
 }
 
 }  // namespace
@@ -467,6 +646,42 @@ zgl_status zgl_diff_backward(zgl_diff* d, const float* d_image, float* d_params,
     else
         diff_backward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
                                                                 d->spp, d->d_samples, d_image, d_params);
+    ZGL_CUDA(cudaGetLastError());
+    ZGL_API_END
+}
+
+zgl_status zgl_diff_step_l2(zgl_diff* d, const float* target, float loss_scale, float* image, float* d_params,
+                            float* loss, void* stream) {
+    ZGL_API_BEGIN
+    ZGL_RANGE("zgl_diff_step_l2");
+    if (!d || !target || !image || !d_params || !loss) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: NULL");
+    if (!device_ptr(target) || !device_ptr(image) || !device_ptr(d_params) || !device_ptr(loss))
+        fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: arrays must be device memory");
+    if (!std::isfinite(loss_scale)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: non-finite loss scale");
+    if (d->spp > 32 * kFuseMaxChunks)
+        fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: %d samples per pixel exceed %d", d->spp, 32 * kFuseMaxChunks);
+    const zgl_scene* s = d->scene;
+    cudaStream_t st = (cudaStream_t)stream;
+    ZGL_CUDA(cudaMemsetAsync(d_params, 0, sizeof(float) * (size_t)d->nparams, st));
+    ZGL_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), st));
+    DiffInfo di{d->nmat, d->nparams, d->d_lightInst};
+    const int64_t npix = (int64_t)s->filmW * s->filmH;
+    const unsigned grid = (unsigned)((npix + kFuseWarps - 1) / kFuseWarps);
+    const int ch = (d->spp + 31) / 32;
+    const PathParams pp = path_params(d->params);
+#define ZGL_FUSE(F, C)                                                                                         \
+    diff_fused_kernel<F, C><<<grid, 32 * kFuseWarps, 0, st>>>(s->view(), pp, di, d->d_values, d->spp, target, \
+                                                               loss_scale, image, d_params, loss)
+    if (s->fullMaterials) {
+        if (ch == 1) ZGL_FUSE(true, 1);
+        else if (ch == 2) ZGL_FUSE(true, 2);
+        else ZGL_FUSE(true, 4);
+    } else {
+        if (ch == 1) ZGL_FUSE(false, 1);
+        else if (ch == 2) ZGL_FUSE(false, 2);
+        else ZGL_FUSE(false, 4);
+    }
+#undef ZGL_FUSE
     ZGL_CUDA(cudaGetLastError());
     ZGL_API_END
 }

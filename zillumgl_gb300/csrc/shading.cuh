@@ -770,7 +770,18 @@ __device__ __forceinline__ float lightPdfLi(const DeviceScene& sc, int id, v3 x,
     lightPowerOf(sc, id, area);
     return distSquare(x, y) / (area * cosTheta);
 }
-__device__ __forceinline__ LiSample lightSampleLi(const DeviceScene& sc, int id, v3 x, v2 u) {  // light.glsl:122-155
+// The light sample's occlusion test.  TraceVis traces the shadow ray; other
+// visibility sources (the adjoint's replay) return a result recorded when the
+// same sample was first traced.
+struct TraceVis {
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        return bvhTest(sc, r, dist);
+    }
+};
+
+template <class Vis>
+__device__ __forceinline__ LiSample lightSampleLiV(const DeviceScene& sc, int id, v3 x, v2 u,
+                                                   const Vis& vis) {  // light.glsl:122-155
     int triId = id + sc.objPrimCount;
     TriShade t = loadTri(sc, triId);
     v3 y = sampleTriangleUniform(t.a, t.b, t.c, u);
@@ -784,11 +795,14 @@ __device__ __forceinline__ LiSample lightSampleLi(const DeviceScene& sc, int id,
     v3 pw = lightPowerOf(sc, id, area);
     float pdf = dist * dist / (area * cosTheta);
     float testDist = dist - 1e-4f - 1e-6f;
-    if (bvhTest(sc, lightRay, testDist) || pdf < 1e-8f) return invalidLi();
+    if (vis(sc, lightRay, testDist) || pdf < 1e-8f) return invalidLi();
     v3 weight = lightLe(sc, id, y, -wi);
     float pdfSample = luminance(pw) / sc.lightSum;
     pdf *= pdfSample;
     return LiSample{wi, weight / pdf, pdf};
+}
+__device__ __forceinline__ LiSample lightSampleLi(const DeviceScene& sc, int id, v3 x, v2 u) {
+    return lightSampleLiV(sc, id, x, u, TraceVis{});
 }
 
 __device__ __forceinline__ v3 envTexel(const DeviceScene& sc, int x, int y) {
@@ -820,7 +834,9 @@ __device__ __forceinline__ float envPdfLi(const DeviceScene& sc, v3 wi) {  // li
     if (sc.envSum == 0.0f) return 0.0f;
     return envGetPortion(sc, wi) * (float)sc.envW * (float)sc.envH * 0.5f * sq(kPiInv);
 }
-__device__ __forceinline__ LiSample envSampleLi(const DeviceScene& sc, v3 x, float ux, float uy, float uz, float uw) {
+template <class Vis>
+__device__ __forceinline__ LiSample envSampleLiV(const DeviceScene& sc, v3 x, float ux, float uy, float uz, float uw,
+                                                 const Vis& vis) {
     if (sc.envTexels == nullptr) return invalidLi();  // light.glsl:181-219
     int w = sc.envW, h = sc.envH;
     int rx = min(zf2i((float)h * ux), h - 1);
@@ -834,8 +850,11 @@ __device__ __forceinline__ LiSample envSampleLi(const DeviceScene& sc, v3 x, flo
     wi = rotateZ(wi, sc.envRotation);
     float pdf = envGetPortion(sc, wi) * (float)w * (float)h * 0.5f * sq(kPiInv);
     Ray ray = rayOffseted(x, wi);
-    if (bvhTest(sc, ray, 1e8f) || pdf == 0.0f) return invalidLi();
+    if (vis(sc, ray, 1e8f) || pdf == 0.0f) return invalidLi();
     return LiSample{wi, envLe(sc, wi) / pdf, pdf};
+}
+__device__ __forceinline__ LiSample envSampleLi(const DeviceScene& sc, v3 x, float ux, float uy, float uz, float uw) {
+    return envSampleLiV(sc, x, ux, uy, uz, uw, TraceVis{});
 }
 __device__ __forceinline__ float pdfSampleLightSel(const DeviceScene& sc, int uniform, float portion) {
     return uniform ? portion : sc.lightSum / (sc.lightSum + sc.envSum);

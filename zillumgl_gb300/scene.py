@@ -555,6 +555,28 @@ class DiffRenderer:
         call("zgl_diff_backward", self._h, _ptr(d_image), _ptr(out), _stream_handle(stream))
         return out
 
+    def step_l2(self, target, loss_scale=None, image=None, grad=None, loss=None, stream=None):
+        """Fused forward + adjoint of loss = loss_scale * sum((image - target)^2)
+        (zgl_diff_step_l2; loss_scale defaults to 1 / target.numel(), the
+        mean squared error).  Returns (image, grad, loss) as CUDA tensors."""
+        import torch
+
+        from .accel import _ptr, _stream_handle
+
+        target = target.contiguous()
+        W, H = self.scene.film
+        if loss_scale is None:
+            loss_scale = 1.0 / target.numel()
+        if image is None:
+            image = torch.empty((H, W, 3), dtype=torch.float32, device=target.device)
+        if grad is None:
+            grad = torch.empty(self.n_params, dtype=torch.float32, device=target.device)
+        if loss is None:
+            loss = torch.empty(1, dtype=torch.float32, device=target.device)
+        call("zgl_diff_step_l2", self._h, _ptr(target), float(loss_scale), _ptr(image), _ptr(grad), _ptr(loss),
+             _stream_handle(stream))
+        return image, grad, loss
+
     def close(self):
         if self._h:
             call("zgl_diff_destroy", self._h)
