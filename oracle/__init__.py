@@ -225,6 +225,9 @@ def _render_lib():
         L.orc_render_pt.restype = None
         L.orc_render_pt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                     C.c_void_p, C.c_int32]
+        L.orc_render_pt_frozen.restype = None
+        L.orc_render_pt_frozen.argtypes = [C.POINTER(OrcScene), C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]
         L.orc_render_lt.restype = None
         L.orc_render_lt.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
         L.orc_render_triple.restype = None
@@ -399,6 +402,18 @@ class OracleScene:
         out = np.zeros((pix.size, 3), np.float32)
         _render_lib().orc_render_pt(C.byref(self.s), spp0, passes, fc0, _p(pix), pix.size, _p(out),
                                     nthreads or threads())
+        return out
+
+    def render_pt_frozen(self, materials, pixels, passes, spp0=0, fc0=1, nthreads=None):
+        """render_pt with every sampling decision of this scene but the BSDF
+        values of `materials` (n, 16): the detached-sampling estimator whose
+        finite differences check the adjoint's material gradients."""
+        mat = np.ascontiguousarray(materials, np.float32)
+        assert mat.size == self.materials.size
+        pix = np.ascontiguousarray(pixels, np.int32)
+        out = np.zeros((pix.size, 3), np.float32)
+        _render_lib().orc_render_pt_frozen(C.byref(self.s), _p(mat), spp0, passes, fc0, _p(pix), pix.size, _p(out),
+                                           nthreads or threads())
         return out
 
     def glsl_render_pt(self, pixels, passes, spp0=0, fc0=1, nthreads=None):

@@ -917,6 +917,92 @@ vec3 pathIntegTrace(const OrcScene& sc, Ray ray, int& s, Rng& g) {  // :35-143
     return result;
 }
 
+// The path of pathIntegTrace with every sampling decision of the scene `sc`
+// (directions, lobe picks, pdfs, MIS weights, Russian roulette) but the BSDF
+// values of the materials `mat1`: the estimator whose derivative in mat1 the
+// path-replay adjoint computes (sampling detached).  Finite differences of it
+// over mat1 check the adjoint's material gradients, roughness and metallic
+// included, independently of its own formulation.
+vec3 pathFrozen(const OrcScene& sc, const float* mat1, Ray ray, int& s, Rng& g) {
+    OrcScene sc1 = sc;
+    sc1.materials = mat1;
+    float primDist;
+    int id = bvhHit(sc, ray, primDist);
+    vec3 pos = rayPoint(ray, primDist);
+    if (id == -1) return envLe(sc, ray.dir);
+    if (id - sc.objPrimCount >= 0) return lightLe(sc, id - sc.objPrimCount, pos, -ray.dir);
+    vec3 wo = -ray.dir;
+    vec3 result(0.0f), throughput(1.0f);
+    for (int bounce = 1; bounce <= sc.maxDepth; bounce++) {
+        SurfaceInfo surf = triangleSurfaceInfo(sc, id, pos);
+        int matTexId = sc.matTexIndex[id];
+        int matId = matTexId & 0x0000ffff;
+        uint32_t matType = loadMaterialType(sc, matId);
+        if (matType != Dielectric && matType != ThinDielectric) {
+            if (dot(surf.ns, wo) < 0.0f) {
+                surf.ns = -surf.ns;
+                surf.ng = -surf.ng;
+            }
+        }
+        BSDFParam mp = loadMaterial(sc, matType, matId);
+        BSDFParam mp1 = loadMaterial(sc1, matType, matId);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp);
+        applyTexture(sc, sc.matTexIndex[id], surf, mp1);
+        if (sc.sampleLight) {
+            float ud = sample1D(sc, g, s);
+            float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
+            LightLiSample ls = sampleLightAndEnv(sc, pos, ud, u0, u1, u2, u3);
+            if (ls.pdf > 0.0f) {
+                vec3 f1 = materialBSDF(matType, mp1, wo, ls.wi, surf.ns);
+                float fpdf = materialPdf(matType, mp, wo, ls.wi, surf.ns);
+                float weight = biHeuristic(ls.pdf, fpdf);
+                result = result + f1 * throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+            }
+        }
+        float b0 = sample1D(sc, g, s), b1 = sample1D(sc, g, s), b2 = sample1D(sc, g, s);
+        BSDFSample bs = materialSample(matType, mp, surf.ns, wo, vec3(b0, b1, b2), g);
+        vec3 wi = bs.wi;
+        float bsdfPdf = bs.pdf;
+        bool deltaBsdf = (bs.flag == SpecRefl || bs.flag == SpecTrans);
+        if (bsdfPdf < 1e-8f) break;
+        vec3 bsdf1 = deltaBsdf ? bs.bsdf : materialBSDF(matType, mp1, wo, wi, surf.ns);
+        throughput = throughput * (bsdf1 / bsdfPdf * (deltaBsdf ? 1.0f : absDot(surf.ns, wi)));
+        ray = rayOffseted(pos, wi);
+        float dist;
+        int nextId = bvhHit(sc, ray, dist);
+        int lightId = nextId - sc.objPrimCount;
+        vec3 nextPos = rayPoint(ray, dist);
+        if (nextId == -1) {
+            vec3 radiance = envLe(sc, wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float envPdf = envPdfLi(sc, wi) * pdfSelectEnv(sc);
+                weight = (envPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, envPdf);
+            }
+            result = result + radiance * throughput * weight;
+            break;
+        } else if (lightId >= 0) {
+            vec3 radiance = lightLe(sc, lightId, nextPos, -wi);
+            float weight = 1.0f;
+            if (sc.sampleLight && !deltaBsdf) {
+                float lightPdf = lightPdfLi(sc, lightId, pos, nextPos) * pdfSelectLight(sc, lightId);
+                weight = (lightPdf <= 0.0f) ? 0.0f : biHeuristic(bsdfPdf, lightPdf);
+            }
+            result = result + radiance * throughput * weight;
+            break;
+        }
+        if (sc.russianRoulette && bounce >= sc.rrStartDepth) {
+            float continueProb = fmin_(maxComponent(bs.bsdf / bsdfPdf), 0.95f);
+            if (sample1D(sc, g, s) >= continueProb) break;
+            throughput = throughput / continueProb;
+        }
+        id = nextId;
+        pos = nextPos;
+        wo = -wi;
+    }
+    return result;
+}
+
 // ---------------------------------------------- camera importance (camera.glsl)
 inline bool inFilmBound(vec2 uv) { return uv.x >= 0.0f && uv.x <= 1.0f && uv.y >= 0.0f && uv.y <= 1.0f; }
 inline bool thinLensCameraDelta(const OrcScene& sc) { return sc.lensRadius <= 1e-6f; }
@@ -1321,7 +1407,8 @@ inline vec2 noiseTexture(const OrcScene& sc, vec2 st) {
 }
 
 // main() of path_integ_naive.glsl:145-174 for one pixel and one pass.
-vec3 renderPixel(const OrcScene& sc, int px, int py, int spp, int freeCounter, bool& valid) {
+vec3 renderPixel(const OrcScene& sc, int px, int py, int spp, int freeCounter, bool& valid,
+                 const float* frozenMat = nullptr) {
     vec2 texSize((float)sc.filmW, (float)sc.filmH);
     vec2 scr = vec2((float)px, (float)py) / texSize;
     vec2 nc = noiseTexture(sc, scr);
@@ -1337,7 +1424,7 @@ vec3 renderPixel(const OrcScene& sc, int px, int py, int spp, int freeCounter, b
     int s = 0;
     float u0 = sample1D(sc, g, s), u1 = sample1D(sc, g, s), u2 = sample1D(sc, g, s), u3 = sample1D(sc, g, s);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    vec3 r = pathIntegTrace(sc, ray, s, g);
+    vec3 r = frozenMat ? pathFrozen(sc, frozenMat, ray, s, g) : pathIntegTrace(sc, ray, s, g);
     valid = !hasNan(r);
     return r;
 }
@@ -1607,8 +1694,8 @@ extern "C" {
 // freeCounter = fc0 + p) of the MIS path tracer for the listed pixels and
 // accumulates into out_rgb[npix*3] like imageStore(lastRes + result) does,
 // skipping NaN samples.
-void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, const int32_t* pixels, int64_t npix,
-                   float* out_rgb, int32_t nthreads) {
+static void render_pt_impl(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, const int32_t* pixels,
+                           int64_t npix, float* out_rgb, int32_t nthreads, const float* frozenMat) {
     std::atomic<int64_t> next{0};
     auto work = [&]() {
         for (;;) {
@@ -1621,7 +1708,7 @@ void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0
                 vec3 acc(out_rgb[3 * i], out_rgb[3 * i + 1], out_rgb[3 * i + 2]);
                 for (int k = 0; k < passes; k++) {
                     bool ok;
-                    vec3 r = renderPixel(*sc, px, py, spp0 + k, fc0 + k, ok);
+                    vec3 r = renderPixel(*sc, px, py, spp0 + k, fc0 + k, ok, frozenMat);
                     if (ok) acc = acc + r;
                 }
                 out_rgb[3 * i] = acc.x;
@@ -1637,6 +1724,18 @@ void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; t++) th.emplace_back(work);
     for (auto& t : th) t.join();
+}
+
+void orc_render_pt(const OrcScene* sc, int32_t spp0, int32_t passes, int32_t fc0, const int32_t* pixels, int64_t npix,
+                   float* out_rgb, int32_t nthreads) {
+    render_pt_impl(sc, spp0, passes, fc0, pixels, npix, out_rgb, nthreads, nullptr);
+}
+
+// render_pt with the sampling of `sc` and the BSDF values of materials mat1
+// (pathFrozen).
+void orc_render_pt_frozen(const OrcScene* sc, const float* mat1, int32_t spp0, int32_t passes, int32_t fc0,
+                          const int32_t* pixels, int64_t npix, float* out_rgb, int32_t nthreads) {
+    render_pt_impl(sc, spp0, passes, fc0, pixels, npix, out_rgb, nthreads, mat1);
 }
 
 // Light tracer passes (light_path_integ.glsl:148-158): `blocks` x 1536 light

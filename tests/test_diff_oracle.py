@@ -2,12 +2,15 @@
 finite differences of the oracle's own forward render (common random numbers:
 every sample reuses its seeds).
 
-Only parameters that leave every sampling decision unchanged can be checked
-this way: baseColor and specular (no pdf depends on them) and light power
-(with one light and no environment the selection probabilities do not
-change).  Roughness and metallic steer the lobe choice and the GGX sample,
-so a finite difference of the frozen-sample estimator jumps; their
-derivatives are checked on the GPU against this oracle instead.
+Plain finite differences only check parameters that leave every sampling
+decision unchanged: baseColor and specular (no pdf depends on them) and light
+power (with one light and no environment the selection probabilities do not
+change).  Roughness and metallic also steer the GGX sample and the lobe
+choice, so they are checked against finite differences of the frozen-sampling
+estimator (OracleScene.render_pt_frozen): every direction, lobe pick, pdf, MIS
+weight and Russian-roulette decision is the one taken at the unperturbed
+parameters and only the BSDF values move, which is the estimator the
+detached-sampling adjoint differentiates.
 """
 from __future__ import annotations
 
@@ -78,3 +81,35 @@ def test_oracle_gradient_is_linear_in_the_image_adjoint(setup):
     g2 = orc.diff_grad(d, SPP, 4.0 * dimage, nthreads=4)
     np.testing.assert_allclose(g2, 4.0 * g1, rtol=1e-12, atol=1e-15)
     assert np.abs(g1).max() > 0
+
+
+def _frozen_loss(orc, d, materials, dimage):
+    W, H = d.film
+    img = orc.render_pt_frozen(materials, np.arange(W * H), SPP).astype(np.float64) / SPP
+    return float(np.sum(img.reshape(H, W, 3) * dimage))
+
+
+def test_oracle_gradient_matches_frozen_sampling_differences(setup):
+    """Roughness (raw, before the 0.0134 remap of material_loader.glsl:46) and
+    metallic (which also drives the lobe pick of material.glsl:537-540) of
+    every principled material, and baseColor / specular as a cross-check."""
+    d, sobol, dimage = setup
+    orc = oracle.OracleScene(d, sobol, PARAMS)
+    g = orc.diff_grad(d, SPP, dimage, nthreads=4)
+    nmat = d.materials.shape[0]
+    slots = [6 * m + 3 for m in range(nmat)] + [6 * m + 4 for m in range(nmat)] + [0, 6 * 2 + 5]
+    checked = 0
+    for slot in slots:
+        m, i = divmod(slot, 6)
+        col = [0, 1, 2, 3, 5, 6][i]
+        base = float(d.materials[m, col])
+        h = H_FD * max(1.0, abs(base))
+        mp, mm = d.materials.copy(), d.materials.copy()
+        mp[m, col] += np.float32(h)
+        mm[m, col] -= np.float32(h)
+        hh = (float(mp[m, col]) - float(mm[m, col])) / 2
+        fd = (_frozen_loss(orc, d, mp, dimage) - _frozen_loss(orc, d, mm, dimage)) / (2 * hh)
+        scale = max(abs(fd), 1e-3 * np.abs(g).max())
+        assert abs(g[slot] - fd) <= 5e-3 * scale, f"slot {slot}: oracle {g[slot]:.6g} fd {fd:.6g}"
+        checked += abs(fd) > 1e-3 * np.abs(g).max()
+    assert checked >= nmat  # most of the roughness / metallic derivatives are not negligible
