@@ -44,12 +44,12 @@ UNIT = "Mrays/s"
 # as the library does
 KERNELS = {"thread_per_ray": {"closest": "trace_closest_kernel", "any": "trace_any_kernel"},
            "persistent": {"closest": "trace_persistent_kernel<false>", "any": "trace_persistent_kernel<true>"},
-           "deferred": {"closest": "trace_deferred_kernel<false>", "any": "trace_deferred_kernel<true>"}}
-AUTO_SCHEDULE = "thread_per_ray"
+           "prefetch": {"closest": "trace_prefetch_kernel<false, false>", "any": "trace_prefetch_kernel<true, false>"},
+           "auto": {"closest": "trace_prefetch_kernel<false, true>", "any": "trace_prefetch_kernel<true, true>"}}
 
 
 def resolved_schedule(schedule: str) -> str:
-    return AUTO_SCHEDULE if schedule == "auto" else schedule
+    return schedule
 
 
 def parse_args():
@@ -64,7 +64,7 @@ def parse_args():
     ap.add_argument("--ref-rays", type=int, default=1 << 20, help="rays per launch traced by --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent", "deferred"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "thread_per_ray", "persistent", "prefetch"])
     ap.add_argument("--only", default="", help="comma list of launch-name substrings to keep (profiling)")
     ap.add_argument("--render", default="cornell,city,batch,diff", help="render workloads to time ('' for none)")
     ap.add_argument("--render-passes", type=int, default=4, help="timed passes per render workload")
@@ -499,7 +499,8 @@ def run_render(args, stream, dev):
             ms = e0.elapsed_time(e1) / args.render_passes
             if kind == "light":
                 paths = 32 * 1536
-                res[kind] = {"ms_per_pass": round(ms, 3), "light_paths_per_s": round(paths / (ms * 1e-3), 1)}
+                res[kind] = {"ms_per_pass": round(ms, 3), "light_paths_per_s": round(paths / (ms * 1e-3), 1),
+                             "blocks_per_pass": 32}
             else:
                 res[kind] = {"ms_per_pass": round(ms, 3), "samples_per_s": round(W * H / (ms * 1e-3), 1)}
                 if kind == "triple":
@@ -524,6 +525,25 @@ def run_render(args, stream, dev):
                                          "to 16 single passes"}
             integ.close()
         if name == "city":
+            # the light tracer at a block count that fills the GPU (the reference's
+            # default of 32 blocks of 1536 paths holds 49,152 threads)
+            nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+            full = -(-nsm * 2048 // 1536)
+            integ = LightIntegrator(scene, **dict(runs[1][2], blocks_per_pass=full))
+            integ.render_one_pass(stream)
+            stream.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.render_passes):
+                integ.render_one_pass(stream)
+            e1.record(stream)
+            stream.synchronize()
+            lms = e0.elapsed_time(e1) / args.render_passes
+            res["light_full_gpu"] = {"ms_per_pass": round(lms, 3), "blocks_per_pass": full,
+                                     "light_paths_per_s": round(full * 1536 / (lms * 1e-3), 1),
+                                     "note": f"{nsm} SMs x 2048 resident threads / 1536 paths per block"}
+            integ.close()
             # the display pass (tone map + gamma) on the 1080p frame: 16 B in, 16 B out per pixel
             from zillumgl_gb300.image import TONE_FILMIC, postprocess
 

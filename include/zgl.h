@@ -102,14 +102,19 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices,
                               const uint32_t* indices, size_t n_triangles,
                               float* bounds, int32_t* hit_table);
 
-/* Trace kernel schedule of an accelerator: ZGL_TRACE_AUTO (0, default),
- * ZGL_TRACE_THREAD_PER_RAY (1: one thread per ray, neighbouring rays share a
- * warp), ZGL_TRACE_PERSISTENT (2: persistent warps that refill idle lanes
- * by atomic fetch) or ZGL_TRACE_DEFERRED (3: one thread per ray with leaf
- * triangle tests deferred and run warp-wide).  Results are identical; only
- * speed differs.  The reference has one fixed schedule (one invocation per
- * pixel or path, src/integrator/NaivePath.cpp:94-100). */
-enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2, ZGL_TRACE_DEFERRED = 3 };
+/* Trace kernel schedule of an accelerator.  All give identical results;
+ * only speed differs.  The reference has one fixed schedule (one invocation
+ * per pixel or path, src/integrator/NaivePath.cpp:94-100).
+ *   ZGL_TRACE_AUTO (0, default): one thread per ray; a warp whose rays share
+ *     one origin (camera rays) runs the plain loop, other warps request both
+ *     possible successors of a node ahead when a face's node table outgrows
+ *     the L2 cache.
+ *   ZGL_TRACE_THREAD_PER_RAY (1): one thread per ray, plain loop.
+ *   ZGL_TRACE_PERSISTENT (2): persistent warps that refill idle lanes by
+ *     atomic fetch.
+ *   ZGL_TRACE_PREFETCH (3): one thread per ray, every warp requests both
+ *     successors ahead. */
+enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2, ZGL_TRACE_PREFETCH = 3 };
 zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule);
 
 /* Closest hit of n rays (origins/dirs float[n*3]): hit_id int32[n] (primitive

@@ -96,7 +96,7 @@ def test_traversal_equals_reference_shader(zgl_lib, cuda):
     assert sha256(p.bounds, p.hitTable) == pin["bvh_sha256"]
     o, d = mixed_rays(np.random.default_rng(rseed), nray)
     to, td = torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda)
-    for schedule in ("thread_per_ray", "persistent", "deferred"):
+    for schedule in ("auto", "thread_per_ray", "persistent", "prefetch"):
         acc.set_trace_schedule(schedule)
         hid, ht = acc.trace_closest(to, td)
         torch.cuda.synchronize()

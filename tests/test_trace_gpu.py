@@ -55,7 +55,7 @@ def soup(zgl_lib, cuda):
     acc.close()
 
 
-@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "deferred"])
+@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "prefetch"])
 def test_primary_and_incoherent_closest_bit_exact(soup, cuda, schedule):
     acc, packed, v, idx = soup
     acc.set_trace_schedule(schedule)
@@ -69,7 +69,7 @@ def test_primary_and_incoherent_closest_bit_exact(soup, cuda, schedule):
         acc.set_trace_schedule("auto")
 
 
-@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent", "deferred"])
+@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "prefetch"])
 def test_mixed_rays_closest_bit_exact(soup, cuda, schedule):
     acc, packed, v, idx = soup
     acc.set_trace_schedule(schedule)
@@ -80,7 +80,7 @@ def test_mixed_rays_closest_bit_exact(soup, cuda, schedule):
         acc.set_trace_schedule("auto")
 
 
-@pytest.mark.parametrize("schedule", ["thread_per_ray", "persistent", "deferred"])
+@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "prefetch"])
 def test_any_hit_bit_exact(soup, cuda, schedule):
     import torch
 

@@ -25,7 +25,7 @@ pytestmark = pytest.mark.gpu
 MAX_RAYS = 1 << 18
 
 
-@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "deferred"])
+@pytest.mark.parametrize("schedule", ["auto", "thread_per_ray", "persistent", "prefetch"])
 def test_noalloc_matches_trace_closest_on_two_calls(zgl_lib, cuda, schedule):
     import torch
 

@@ -116,7 +116,7 @@ class Accelerator:
         call("zgl_accel_export", self._h, _ptr(bounds), _ptr(hit))
         return PackedBVH(bounds, hit)
 
-    SCHEDULES = {"auto": 0, "thread_per_ray": 1, "persistent": 2, "deferred": 3}
+    SCHEDULES = {"auto": 0, "thread_per_ray": 1, "persistent": 2, "prefetch": 3}
 
     def set_trace_schedule(self, schedule: str) -> None:
         """Select the trace kernel schedule (results are identical)."""

@@ -77,25 +77,35 @@ trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __
     tests[i] = t;
 }
 
-// Deferred-leaf schedule (traverse_deferred): one ray per thread, neighbouring
-// rays in one warp; the warp runs the general-direction loop unless one of
-// its rays needs the axis-dominant or near-zero-component box test.
-constexpr int kDeferQueue = 3;
-
-template <bool ANY>
+// Prefetching schedule: one thread per ray with the node loads of
+// traverse_v.  ADAPT (the auto schedule): a warp whose rays share one origin
+// (camera rays: coherent, their nodes come from L1 and L2) runs the plain
+// loop, and so does every warp when one face's table fits in L2; otherwise a
+// warp requests both successors ahead (PF) with a 256-byte L2 prefetch hint,
+// so that DRAM latency overlaps the tests.  Without ADAPT every warp takes
+// the PF loop.  Measured on the GB300 (2^24 rays per launch): the PF loop
+// takes the 16M incoherent launches from 93.7 / 57.8 ms to 79.1 / 48.7 ms
+// (closest / any) and the 4M ones from 29.4 to 27.5 ms, and costs 30-50% on
+// camera rays and on the L2-resident 1M tables.
+template <bool ANY, bool ADAPT>
 __global__ void __launch_bounds__(kTraceBlock)
-trace_deferred_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
-                      const float* __restrict__ tmax, int64_t n, int32_t* __restrict__ hit_id,
+trace_prefetch_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
+                      const float* __restrict__ tmax, int64_t n, int far, int32_t* __restrict__ hit_id,
                       float* __restrict__ hit_t, uint8_t* __restrict__ occ) {
     const int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
-    const bool active = i < n;
-    const int64_t j = active ? i : n - 1;
-    const TraceRay r = make_trace_ray(load3(org, j), load3(dir, j));
-    float dist = ANY ? tmax[j] : 1e8f;
-    const bool general = __all_sync(0xffffffffu, !active || r.mode == 3);
-    const int res = general ? traverse_deferred<ANY, kDeferQueue, 3>(a, r, active, dist)
-                            : traverse_deferred<ANY, kDeferQueue, -1>(a, r, active, dist);
-    if (!active) return;
+    const bool valid = i < n;
+    const float3 o = valid ? load3(org, i) : make_float3(0.0f, 0.0f, 0.0f);
+    bool plain = false;
+    if (ADAPT) {
+        const unsigned m = 0xffffffffu;
+        const float ox = __shfl_sync(m, o.x, 0), oy = __shfl_sync(m, o.y, 0), oz = __shfl_sync(m, o.z, 0);
+        plain = !far || __all_sync(m, !valid || (o.x == ox && o.y == oy && o.z == oz));
+    }
+    if (!valid) return;
+    const TraceRay r = make_trace_ray(o, load3(dir, i));
+    float dist = ANY ? tmax[i] : 1e8f;
+    int v = 0, t = 0;
+    const int res = plain ? traverse<ANY, false>(a, r, dist, v, t) : traverse_vm<ANY, true, 256>(a, r, dist);
     if (ANY) {
         occ[i] = (uint8_t)res;
     } else {
@@ -104,7 +114,29 @@ trace_deferred_kernel(DeviceAccel a, const float* __restrict__ org, const float*
     }
 }
 
+// Whether one face's node table (M records of 32 bytes) outgrows the L2 of
+// the current device.
+int tables_beyond_l2(int64_t M) {
+    int dev = 0, l2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    return (int64_t)32 * M > (int64_t)l2 ? 1 : 0;
+}
+
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+template <bool ANY>
+cudaError_t launch_trace_prefetch(bool adapt, DeviceAccel a, const float* org, const float* dir,
+                                  const float* tmax, int64_t n, int32_t* hit_id, float* hit_t, uint8_t* occ,
+                                  cudaStream_t s) {
+    const unsigned g = grid_for(n, kTraceBlock);
+    const int far = tables_beyond_l2(a.M);
+    if (adapt)
+        trace_prefetch_kernel<ANY, true><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, far, hit_id, hit_t, occ);
+    else
+        trace_prefetch_kernel<ANY, false><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, far, hit_id, hit_t, occ);
+    return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------
 // Persistent traversal: each warp keeps its lanes busy by refilling a lane
@@ -236,11 +268,9 @@ cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* d
                                  int32_t* hit_id, float* hit_t, int schedule, unsigned long long* counter,
                                  cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M > 0 && schedule == ZGL_TRACE_DEFERRED) {
-        trace_deferred_kernel<false><<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, nullptr, n, hit_id,
-                                                                                      hit_t, nullptr);
-        return cudaGetLastError();
-    }
+    if (a.M > 0 && (schedule == ZGL_TRACE_AUTO || schedule == ZGL_TRACE_PREFETCH))
+        return launch_trace_prefetch<false>(schedule == ZGL_TRACE_AUTO, a, org, dir, nullptr, n, hit_id, hit_t,
+                                            nullptr, s);
     if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
         trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
         return cudaGetLastError();
@@ -258,11 +288,9 @@ cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* d
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
                              int64_t n, uint8_t* occ, int schedule, unsigned long long* counter, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M > 0 && schedule == ZGL_TRACE_DEFERRED) {
-        trace_deferred_kernel<true><<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, nullptr,
-                                                                                     nullptr, occ);
-        return cudaGetLastError();
-    }
+    if (a.M > 0 && (schedule == ZGL_TRACE_AUTO || schedule == ZGL_TRACE_PREFETCH))
+        return launch_trace_prefetch<true>(schedule == ZGL_TRACE_AUTO, a, org, dir, tmax, n, nullptr, nullptr, occ,
+                                           s);
     if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
         trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
         return cudaGetLastError();
@@ -408,11 +436,9 @@ private:
     int prev_ = 0, dev_ = 0;
 };
 
-// The schedule a trace call runs.  Auto is one thread per ray: neighbouring
-// rays of a batch stay in one warp, which keeps their node fetches coalesced.
-int trace_schedule(const zgl_accel* a) {
-    return a->trace_schedule == ZGL_TRACE_AUTO ? ZGL_TRACE_THREAD_PER_RAY : a->trace_schedule;
-}
+// The schedule a trace call runs (ZGL_TRACE_AUTO is the adaptive prefetching
+// kernel).
+int trace_schedule(const zgl_accel* a) { return a->trace_schedule; }
 
 int host_threads() {
     unsigned n = std::thread::hardware_concurrency();
@@ -618,7 +644,7 @@ zgl_status zgl_accel_destroy(zgl_accel* accel) {
 zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule) {
     ZGL_API_BEGIN
     if (!accel) fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: NULL accel");
-    if (schedule < ZGL_TRACE_AUTO || schedule > ZGL_TRACE_DEFERRED)
+    if (schedule < ZGL_TRACE_AUTO || schedule > ZGL_TRACE_PREFETCH)
         fail(ZGL_ERR_INVALID_ARG, "zgl_accel_set_trace_schedule: unknown schedule %d", schedule);
     accel->trace_schedule = schedule;
     ZGL_API_END

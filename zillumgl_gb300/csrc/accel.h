@@ -59,8 +59,8 @@ inline DeviceAccel device_view(const zgl_accel* a) {
 // Kernel launchers (accel.cu).  All pointers are device pointers.
 cudaError_t launch_pack_nodes(const float* bounds, const int32_t* hit, int64_t M, float4* nodes,
                               cudaStream_t s);
-// `schedule` is ZGL_TRACE_THREAD_PER_RAY, ZGL_TRACE_PERSISTENT (which needs
-// `counter`, a device word it resets on the stream) or ZGL_TRACE_DEFERRED.
+// `schedule` is a ZGL_TRACE_* value; ZGL_TRACE_PERSISTENT needs `counter`, a
+// device word it resets on the stream.
 cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* dir, int64_t n,
                                  int32_t* hit_id, float* hit_t, int schedule, unsigned long long* counter,
                                  cudaStream_t s);

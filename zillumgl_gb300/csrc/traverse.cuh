@@ -176,85 +176,83 @@ __device__ __forceinline__ int traverse_m(const DeviceAccel& a, const TraceRay& 
     return ANY ? (closest >= 0 ? 1 : 0) : closest;
 }
 
-// One table step of the deferred traversal: the box test of entry k with the
-// lane's current distance; a leaf that passes is queued instead of tested.
-template <int MODE>
-__device__ __forceinline__ bool deferred_box(const float4 lo, const float4 hi, const TraceRay& r, float& tmin) {
-    return MODE < 0 ? box_hit(lo, hi, r, tmin) : box_hit_m<MODE>(lo, hi, r, tmin);
+// A node-record load, optionally with an L2 prefetch-size hint (the L2 then
+// fetches the aligned 128 or 256 bytes around the record from DRAM: the
+// next entries of a descent are the next records of the table).
+template <int HINT>
+__device__ __forceinline__ float4 load_node(const float4* p) {
+    if (HINT == 0) return __ldg(p);
+    float4 v;
+    if (HINT == 256)
+        asm("ld.global.nc.L2::256B.v4.f32 {%0, %1, %2, %3}, [%4];"
+            : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+            : "l"(p));
+    else
+        asm("ld.global.nc.L2::128B.v4.f32 {%0, %1, %2, %3}, [%4];"
+            : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+            : "l"(p));
+    return v;
 }
 
-// Warp-synchronous bvhHit / bvhTest with deferred leaf tests.  Every lane of
-// the warp must call it together (lanes without a ray pass active = false).
-//
-// A lane box-tests table entries in the reference order and, when a leaf
-// passes, queues (entry, primitive) and goes on to entry + 1 as if the
-// triangle missed.  The warp tests the queued triangles together, each lane
-// in its own queue order, once half of the lanes still at work have a queued
-// leaf, a queue is full, or a lane has reached the end of the table with
-// leaves queued.  A closest-hit lane whose queued triangle hits with t < dist
-// takes the new distance and restarts right after that leaf, dropping the
-// steps and leaves it took after it with the old distance; so every lane
-// replays exactly the reference's sequence of box tests and triangle tests
-// (the leaf's own box passed, so the reference's next entry is leaf + 1 in
-// both cases).  An any-hit lane keeps one distance throughout and stops at
-// the first hit.  The triangle branch, taken by a few lanes per step in the
-// one-thread-per-ray loop, now runs once for many lanes.
-template <bool ANY, int Q, int MODE>
-__device__ __forceinline__ int traverse_deferred(const DeviceAccel& a, const TraceRay& r, bool active,
-                                                 float& dist) {
-    const unsigned kAll = 0xffffffffu;
+// bvhHit / bvhTest (ANY) in the reference's visiting order with the node
+// loads arranged for memory-level parallelism.  PF: both possible
+// successors of entry k (k + 1 after a box hit, the miss link after a box
+// miss) are requested before the box and triangle tests of k, so their
+// latency overlaps that work; the test result then picks one.  HINT: L2
+// prefetch size of the node loads (0: none).  Results are those of
+// traverse_m.
+template <bool ANY, int MODE, bool PF, int HINT>
+__device__ __forceinline__ int traverse_v(const DeviceAccel& a, const TraceRay& r, float& dist) {
     const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
     const int M = a.M;
-    int k = active ? 0 : M;
     int closest = -1;
-    int cnt = 0;
-    int qk[Q], qp[Q];
-#pragma unroll
-    for (int j = 0; j < Q; j++) qk[j] = qp[j] = 0;
+    if (M <= 0) return ANY ? 0 : -1;
+    int k = 0;
+    float4 lo = load_node<HINT>(base), hi = load_node<HINT>(base + 1);
     for (;;) {
-        if (k < M) {
-            const float4 lo = __ldg(base + 2 * k);
-            const float4 hi = __ldg(base + 2 * k + 1);
-            float tmin;
-            const bool h = deferred_box<MODE>(lo, hi, r, tmin) && !(tmin > dist);
-            const int prim = __float_as_int(lo.w);
-            if (h && prim >= 0) {
-#pragma unroll
-                for (int j = 0; j < Q; j++)
-                    if (j == cnt) {
-                        qk[j] = k;
-                        qp[j] = prim;
-                    }
-                cnt++;
-            }
-            k = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+        const int prim = __float_as_int(lo.w);
+        const int skip = max(__float_as_int(hi.w), k + 1);
+        float4 alo, ahi, blo, bhi;
+        if (PF) {
+            const int ka = min(k + 1, M - 1), kb = min(skip, M - 1);
+            alo = load_node<HINT>(base + 2 * ka);
+            ahi = load_node<HINT>(base + 2 * ka + 1);
+            blo = load_node<HINT>(base + 2 * kb);
+            bhi = load_node<HINT>(base + 2 * kb + 1);
         }
-        const unsigned pend = __ballot_sync(kAll, cnt > 0);
-        const unsigned must = __ballot_sync(kAll, cnt == Q || (cnt > 0 && k >= M));
-        const unsigned work = __ballot_sync(kAll, k < M);
-        if (must != 0u || (pend != 0u && 2 * __popc(pend) >= __popc(work | pend))) {
-            bool stop = false;
-#pragma unroll
-            for (int j = 0; j < Q; j++) {
-                if (!stop && j < cnt) {
-                    float t;
-                    if (tri_hit(a.tris, qp[j], r, t) && t < dist) {
-                        closest = qp[j];
-                        stop = true;
-                        if (ANY) {
-                            k = M;
-                        } else {
-                            dist = t;
-                            k = qk[j] + 1;
-                        }
-                    }
-                }
+        float tmin;
+        const bool h = box_hit_m<MODE>(lo, hi, r, tmin) && !(tmin > dist);
+        const int next = h ? k + 1 : skip;
+        if (h && prim >= 0) {
+            float t;
+            if (tri_hit(a.tris, prim, r, t) && t < dist) {
+                closest = prim;
+                if (ANY) break;
+                dist = t;
             }
-            cnt = 0;
         }
-        if (__ballot_sync(kAll, k < M || cnt > 0) == 0u) break;
+        if (next >= M) break;
+        if (PF) {
+            lo = h ? alo : blo;
+            hi = h ? ahi : bhi;
+        } else {
+            lo = load_node<HINT>(base + 2 * next);
+            hi = load_node<HINT>(base + 2 * next + 1);
+        }
+        k = next;
     }
     return ANY ? (closest >= 0 ? 1 : 0) : closest;
+}
+
+template <bool ANY, bool PF, int HINT>
+__device__ __forceinline__ int traverse_vm(const DeviceAccel& a, const TraceRay& r, float& dist) {
+    switch (r.mode) {
+        case 3: return traverse_v<ANY, 3, PF, HINT>(a, r, dist);
+        case 4: return traverse_v<ANY, 4, PF, HINT>(a, r, dist);
+        case 0: return traverse_v<ANY, 0, PF, HINT>(a, r, dist);
+        case 1: return traverse_v<ANY, 1, PF, HINT>(a, r, dist);
+        default: return traverse_v<ANY, 2, PF, HINT>(a, r, dist);
+    }
 }
 
 template <bool ANY, bool COUNT>
