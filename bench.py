@@ -74,7 +74,7 @@ def parse_args():
     ap.add_argument("--diff-spp", type=int, default=32, help="samples per pixel of the differentiable workload")
     ap.add_argument("--batch-requests", type=int, default=64, help="requests of the batched workload")
     ap.add_argument("--batch-no-autotune", action="store_true", help="batched workload with the default schedule")
-    ap.add_argument("--batch-schedule", default="", choices=["", "flat", "persistent"],
+    ap.add_argument("--batch-schedule", default="", choices=["", "flat", "persistent", "queue"],
                     help="batched workload with this schedule instead of the autotuned one")
     return ap.parse_args()
 
@@ -607,8 +607,10 @@ def run_render(args, stream, dev):
 def run_batch(args, stream, dev):
     """Batched serving: 64 seeded requests (1k-500k triangles, 128^2-1024^2,
     4-64 spp, depth 4-8).  Plain = one path-tracer launch per request per
-    pass; batched = the persistent wavefront renderer (autotuned, graph).
-    Both produce the same frames bit for bit."""
+    pass, and one multi-pass launch per request (the stronger baseline);
+    batched = the batched renderer (autotuned, graph).  All produce the same
+    frames bit for bit.  `speedup` is the median of three timings of one
+    multi-pass launch per request over the median of three batched renders."""
     import torch
 
     from zillumgl_gb300.scene import BatchRenderer, PathIntegrator, Scene
@@ -646,17 +648,24 @@ def run_batch(args, stream, dev):
         it.render_passes(spp, stream)  # warm-up: allocates each pass buffer
         it.reset()
     stream.synchronize()
-    e0.record(stream)
-    for it, (_, spp, _) in zip(multi, reqs):
-        it.render_passes(spp, stream)
-    e1.record(stream)
-    stream.synchronize()
-    multi_ms = e0.elapsed_time(e1)
+    multi_runs = []
+    for _ in range(3):
+        for it in multi:
+            it.reset()
+        stream.synchronize()
+        e0.record(stream)
+        for it, (_, spp, _) in zip(multi, reqs):
+            it.render_passes(spp, stream)
+        e1.record(stream)
+        stream.synchronize()
+        multi_runs.append(e0.elapsed_time(e1))
+    multi_ms = statistics.median(multi_runs)
     for it in multi:
         it.close()
     del multi
     # batched
-    sched = {"": {}, "flat": {"schedule": 1}, "persistent": {"schedule": 2}}[args.batch_schedule]
+    sched = {"": {}, "flat": {"schedule": 1}, "persistent": {"schedule": 2}, "queue": {"schedule": 3}}[
+        args.batch_schedule]
     batch = BatchRenderer([(sc, spp, params, fr) for sc, (_, spp, params), fr in zip(scenes, reqs, frames)],
                           **sched)
     t1 = time.time()
@@ -664,11 +673,30 @@ def run_batch(args, stream, dev):
     tune_s = time.time() - t1
     batch.render(stream)  # captures the graph
     stream.synchronize()
-    e0.record(stream)
-    batch.render(stream)
-    e1.record(stream)
-    stream.synchronize()
-    batch_ms = e0.elapsed_time(e1)
+    batch_runs = []
+    for _ in range(3):
+        e0.record(stream)
+        batch.render(stream)
+        e1.record(stream)
+        stream.synchronize()
+        batch_runs.append(e0.elapsed_time(e1))
+    batch_ms = statistics.median(batch_runs)
+    # the other schedules of the batched renderer, for the record
+    others = {}
+    for nm, sv in (("flat", 1), ("persistent", 2), ("queue", 3)):
+        if sv == tuned.get("schedule"):
+            continue
+        cfg = {"schedule": sv} if sv == 1 else {"schedule": sv, "block_size": 256 if sv == 3 else 128,
+                                                 "queue_capacity": 32, "regen_threshold": 16}
+        batch.set_config(**cfg)
+        batch.render(stream)
+        stream.synchronize()
+        e0.record(stream)
+        batch.render(stream)
+        e1.record(stream)
+        stream.synchronize()
+        others[nm] = {"ms": round(e0.elapsed_time(e1), 2), "config": cfg}
+    batch.set_config(**tuned)
     # spot check: the batched frames equal the plain ones
     same = 0
     for it, fr in zip(integs[:4], frames[:4]):
@@ -683,12 +711,17 @@ def run_batch(args, stream, dev):
     return {"requests": len(reqs), "samples": total, "cpu_baseline": cpu,
             "plain": {"ms": round(plain_ms, 2), "samples_per_s": round(total / (plain_ms * 1e-3), 1),
                       "launches": launches_plain},
-            "plain_one_launch_per_request": {"ms": round(multi_ms, 2),
+            "plain_one_launch_per_request": {"ms": round(multi_ms, 2), "runs_ms": [round(x, 2) for x in multi_runs],
                                              "samples_per_s": round(total / (multi_ms * 1e-3), 1),
                                              "launches": 2 * len(reqs)},
-            "batched": {"ms": round(batch_ms, 2), "samples_per_s": round(total / (batch_ms * 1e-3), 1),
+            "batched": {"ms": round(batch_ms, 2), "runs_ms": [round(x, 2) for x in batch_runs],
+                        "samples_per_s": round(total / (batch_ms * 1e-3), 1),
                         "config": tuned, "autotune_s": round(tune_s, 2)},
-            "speedup": round(plain_ms / batch_ms, 3), "frames_bit_identical_checked": f"{same}/4"}
+            "other_schedules": others,
+            "speedup": round(multi_ms / batch_ms, 3),
+            "speedup_note": "median of 3 one-multi-pass-launch-per-request timings over the median of 3 batched renders",
+            "speedup_vs_per_pass_launches": round(plain_ms / batch_ms, 3),
+            "frames_bit_identical_checked": f"{same}/4"}
 
 
 def run_diff(args, stream, dev):

@@ -383,15 +383,20 @@ typedef struct zgl_render_request {
 /* Schedule of the batched renderer; 0 picks the default (or, after
  * zgl_batch_autotune, the tuned value).  schedule: ZGL_BATCH_FLAT (one grid of
  * 16x8 pixel tiles over every sample of every request, straight-line path
- * code per thread; the default) or ZGL_BATCH_PERSISTENT (persistent warps
- * with per-bounce path state and path regeneration).  For the persistent
- * schedule: block_size 64, 128 or 256 threads; queue_capacity: work items a
- * warp claims per atomic fetch; regen_threshold: idle lanes a warp waits for
- * before refilling them (1-32).  Either schedule renders every sample of a
+ * code per thread; the default), ZGL_BATCH_PERSISTENT (persistent warps
+ * with per-bounce path state and path regeneration) or ZGL_BATCH_QUEUE
+ * (persistent blocks of 256 threads whose paths put their closest-hit and
+ * shadow rays into dense queues in shared memory, traced by the whole block
+ * between shading rounds; the reference's nearest relative is
+ * src/shader/pt_shared_queue.glsl).  For the persistent and queue
+ * schedules: block_size 64, 128 or 256 threads (256 for the queue);
+ * queue_capacity: work items a warp claims per atomic fetch;
+ * regen_threshold: idle lanes a warp waits for before refilling them
+ * (1-32).  Every schedule renders every sample of a
  * group of up to 64 requests in one launch (chunks of sample indices when the
  * per-sample scratch would exceed scratch_mib), followed by the in-order frame
  * updates; the CUDA graph holds these launches. */
-enum { ZGL_BATCH_DEFAULT = 0, ZGL_BATCH_FLAT = 1, ZGL_BATCH_PERSISTENT = 2 };
+enum { ZGL_BATCH_DEFAULT = 0, ZGL_BATCH_FLAT = 1, ZGL_BATCH_PERSISTENT = 2, ZGL_BATCH_QUEUE = 3 };
 typedef struct zgl_batch_config {
     int32_t block_size;
     int32_t queue_capacity;

@@ -5,7 +5,8 @@ frame of a fresh ZGL_INTEGRATOR_PATH integrator after `spp` passes: the
 batched schedule changes which lane renders which sample and when, not the
 arithmetic, the RNG streams or the per-pixel summation order.  Checked for
 uneven requests (scenes, film sizes, spp, depth, Russian roulette, sampler),
-for several schedules (block size, queue capacity, regeneration threshold)
+for every schedule (flat, persistent, shared-memory queues) and several
+settings (block size, queue capacity, regeneration threshold)
 and after autotuning and graph replay.
 """
 from __future__ import annotations
@@ -68,7 +69,7 @@ def _check(reqs, refs):
         assert bad == 0, f"request {i}: {bad} pixels differ from the plain integrator"
 
 
-FLAT, PERSISTENT = 1, 2
+FLAT, PERSISTENT, QUEUE = 1, 2, 3
 
 
 @pytest.mark.parametrize("cfg", [
@@ -80,6 +81,10 @@ FLAT, PERSISTENT = 1, 2
     dict(schedule=PERSISTENT, block_size=128, queue_capacity=1, regen_threshold=8),
     dict(schedule=FLAT, scratch_mib=1),        # chunks of a few sample indices
     dict(schedule=PERSISTENT, scratch_mib=1),
+    dict(schedule=QUEUE),
+    dict(schedule=QUEUE, block_size=256, queue_capacity=1, regen_threshold=1),
+    dict(schedule=QUEUE, block_size=256, queue_capacity=128, regen_threshold=32),
+    dict(schedule=QUEUE, scratch_mib=1),
 ])
 def test_batch_equals_plain_integrator(batch_setup, cfg):
     reqs, refs = batch_setup
@@ -96,7 +101,7 @@ def test_autotune_then_render(batch_setup):
     reqs, refs = batch_setup
     b = BatchRenderer(reqs)
     chosen = b.autotune()
-    assert chosen["schedule"] in (FLAT, PERSISTENT)
+    assert chosen["schedule"] in (FLAT, PERSISTENT, QUEUE)
     assert chosen["block_size"] in (64, 128, 256)
     assert b.config() == chosen
     b.render()
@@ -122,7 +127,7 @@ def test_autotune_cache_reuses_the_choice(batch_setup, tmp_path):
     b2.close()
 
 
-@pytest.mark.parametrize("schedule", [FLAT, PERSISTENT])
+@pytest.mark.parametrize("schedule", [FLAT, PERSISTENT, QUEUE])
 def test_batch_in_sample_chunks(zgl_lib, cuda, schedule):
     """A 1 MiB scratch budget forces one sample index per launch for a 256^2
     request; frames still equal the plain integrator's bit for bit."""

@@ -72,8 +72,10 @@ struct BatchLaunch {
 };
 static_assert(sizeof(BatchLaunch) <= 32000, "kernel parameter block too large");
 
+template <class Vis>
 __device__ __forceinline__ LiSample sampleLightAndEnvB(const DeviceScene& sc, const BatchPathParams& pp, v3 x,
-                                                       float ud, float u0, float u1, float u2, float u3) {
+                                                       float ud, float u0, float u1, float u2, float u3,
+                                                       const Vis& vis) {
     float pdfSampleLight = 0.0f;  // light.glsl:221-235
     if (sc.nLight > 0) pdfSampleLight = pdfSampleLightSel(sc, pp.uniformSel, pp.portion);
     bool sampleLight = ud < pdfSampleLight;
@@ -81,9 +83,9 @@ __device__ __forceinline__ LiSample sampleLightAndEnvB(const DeviceScene& sc, co
     LiSample s;
     if (sampleLight) {
         int id = lightSampleOne(sc, mk2(u0, u1));
-        s = lightSampleLi(sc, id, x, mk2(u2, u3));
+        s = lightSampleLiV(sc, id, x, mk2(u2, u3), vis);
     } else {
-        s = envSampleLi(sc, x, u0, u1, u2, u3);
+        s = envSampleLiV(sc, x, u0, u1, u2, u3, vis);
     }
     s.coef = s.coef / pdfSelect;
     s.pdf *= pdfSelect;
@@ -128,15 +130,37 @@ __device__ __forceinline__ void start_sample(const BatchRequest& rq, const Batch
     st.bounce = 0;
 }
 
-// One step of pathIntegTrace: trace the pending ray, account for what it hits,
-// and, if the path continues, shade the new vertex (light sample + BSDF
-// sample) to produce the next pending ray.  Returns false when the path ends.
-template <bool FULL>
-__device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, PathState& st) {
+// The light sample of a vertex whose occlusion test is left to a later
+// trace: the shadow ray and the contribution the sample makes if nothing
+// blocks it.
+struct PendingShadow {
+    v3 o, d, C;
+    float tmax;
+    bool pending;
+};
+
+// Visibility source that records the shadow ray instead of tracing it and
+// answers "not occluded"; the contribution is added after the trace.
+struct DeferVis {
+    PendingShadow* ps;
+    __device__ __forceinline__ bool operator()(const DeviceScene&, const Ray& r, float dist) const {
+        ps->o = r.ori;
+        ps->d = r.dir;
+        ps->tmax = dist;
+        return false;
+    }
+};
+
+// One step of pathIntegTrace after the pending ray has been traced (closest
+// hit `id` at `dist`): account for what it hits and, if the path continues,
+// shade the new vertex (light sample + BSDF sample) to produce the next
+// pending ray.  Returns false when the path ends.  DEFER: the light sample's
+// occlusion test is recorded in `ps` for a later trace instead of run here.
+template <bool FULL, bool DEFER>
+__device__ __forceinline__ bool path_step_hit(const BatchRequest& rq, Sampler& g, PathState& st, int id, float dist,
+                                              PendingShadow* ps) {
     const DeviceScene& sc = rq.sc;
     const BatchPathParams& pp = rq.pp;
-    float dist;
-    int id = bvhHit(sc, st.ray, dist);
     v3 hitPos = rayPoint(st.ray, dist);
     if (st.bounce == 0) {
         // primary hit (path_integ_naive.glsl:37-44)
@@ -199,12 +223,20 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, Pa
         float ud = sample1D(g);
         float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g),
               u3 = sample1D(g);
-        LiSample ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3);
+        LiSample ls;
+        if (DEFER) ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3, DeferVis{ps});
+        else ls = sampleLightAndEnvB(sc, pp, hitPos, ud, u0, u1, u2, u3, TraceVis{});
         if (ls.pdf > 0.0f) {
             v3 f = materialBSDF<FULL>(matType, mp, st.wo, ls.wi, surf.ns);
             float fpdf = materialPdf<FULL>(matType, mp, st.wo, ls.wi, surf.ns);
             float weight = biHeuristic(ls.pdf, fpdf);
-            st.result = st.result + f * st.throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+            const v3 C = f * st.throughput * satDot(surf.ns, ls.wi) * ls.coef * weight;
+            if (DEFER) {
+                ps->C = C;
+                ps->pending = true;
+            } else {
+                st.result = st.result + C;
+            }
         }
     }
     float b0 = sample1D(g), b1 = sample1D(g), b2 = sample1D(g);
@@ -216,6 +248,14 @@ __device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, Pa
     st.bsdfOverPdf = bs.bsdf / bs.pdf;
     st.ray = rayOffseted(hitPos, bs.wi);
     return true;
+}
+
+// One step with the pending ray traced here.
+template <bool FULL>
+__device__ __forceinline__ bool path_step(const BatchRequest& rq, Sampler& g, PathState& st) {
+    float dist;
+    const int id = bvhHit(rq.sc, st.ray, dist);
+    return path_step_hit<FULL, false>(rq, g, st, id, dist, nullptr);
 }
 
 __device__ __forceinline__ int find_request(const BatchLaunch& L, int64_t item) {
@@ -305,6 +345,166 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK) batch_kernel(const __grid
     }
 }
 
+// ----------------------------------------------------------------------------
+// Queue schedule: persistent blocks whose paths trade rays through queues
+// staged in shared memory (the design of the reference's experiment
+// src/shader/pt_shared_queue.glsl:45-50, 193-241, with each path's own
+// sampler state kept, so the sample dimensions follow the naive schedule).
+// Each thread owns a path slot.  One round of the block:
+//   1. idle slots of a warp take new work items (one atomicAdd per warp,
+//      handed out with __ballot_sync / __popc) and start their camera ray;
+//   2. every live slot appends its pending ray to the closest-hit queue and,
+//      when its last vertex left a light sample, that sample's shadow ray to
+//      the occlusion queue (warp-aggregated shared-memory atomics, so both
+//      queues are dense);
+//   3. thread t traces closest-hit entry t and occlusion entry t;
+//   4. every live slot adds its light sample if it was not occluded, then
+//      takes its hit: emission and MIS, Russian roulette, and the next
+//      vertex's light sample (shadow ray recorded, not traced) and BSDF
+//      sample.
+// The contributions are added in the order of the plain path tracer (a
+// vertex's light sample before the emission its extension ray finds), so
+// every sample equals the plain integrator's bit for bit.
+// ----------------------------------------------------------------------------
+constexpr int kQueueBlock = 256;
+
+template <bool FULL>
+__global__ void __launch_bounds__(kQueueBlock, 4) batch_queue_kernel(const __grid_constant__ BatchLaunch L) {
+    __shared__ float4 cqO[kQueueBlock], cqD[kQueueBlock];  // closest-hit queue: origin + request, direction
+    __shared__ float4 sqO[kQueueBlock], sqD[kQueueBlock];  // occlusion queue: origin + request, direction + tmax
+    __shared__ int16_t cOwner[kQueueBlock], sOwner[kQueueBlock];
+    __shared__ int cId[kQueueBlock];
+    __shared__ float cT[kQueueBlock];
+    __shared__ uint8_t sOcc[kQueueBlock];
+    __shared__ int nc, ns;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    if (tid == 0) nc = ns = 0;
+    int64_t qnext = 0, qend = 0;  // warp-uniform: claimed items not yet handed out
+    bool exhausted = false;       // warp-uniform
+    bool live = false;
+    int rid = 0, px = 0, py = 0, js = 0;
+    Sampler g;
+    PathState st;
+    PendingShadow ps;
+    ps.pending = false;
+    for (;;) {
+        // 1. refill idle slots
+        const unsigned idle = __ballot_sync(kFull, !live);
+        const int nidle = __popc(idle);
+        const int64_t tail = qend - qnext;
+        if (nidle != 0 && (nidle >= L.regenThreshold || nidle == 32) && (!exhausted || tail > 0)) {
+            int64_t nb = 0, nlen = 0;
+            if (!exhausted && tail < nidle) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(L.counter, (unsigned long long)L.queueCap);
+                b = __shfl_sync(kFull, b, 0);
+                if ((int64_t)b >= L.nitems) {
+                    exhausted = true;
+                } else {
+                    nb = (int64_t)b;
+                    nlen = min((int64_t)L.queueCap, L.nitems - nb);
+                }
+            }
+            if (!live) {
+                const int r = __popc(idle & lt);
+                int64_t item = -1;
+                if (r < tail) item = qnext + r;
+                else if (r - tail < nlen) item = nb + (r - tail);
+                if (item >= 0) {
+                    rid = find_request(L, item);
+                    const BatchRequest& rq = L.req[rid];
+                    const int64_t local = item - rq.itemBase;
+                    js = (int)(local / rq.perSample);
+                    const int64_t inSample = local - (int64_t)js * rq.perSample;
+                    js += L.j0;
+                    const int64_t tile = inSample >> 5;
+                    const int w = (int)(inSample & 31);
+                    px = (int)(tile % rq.tilesX) * 8 + (w & 7);
+                    py = (int)(tile / rq.tilesX) * 4 + (w >> 3);
+                    if (px < rq.sc.filmW && py < rq.sc.filmH) {
+                        live = true;
+                        ps.pending = false;
+                        start_sample(rq, L, js, px, py, g, st);
+                    }
+                }
+            }
+            const int64_t used = min((int64_t)nidle, tail + nlen);
+            if (used <= tail) {
+                qnext += used;
+            } else {
+                qnext = nb + (used - tail);
+                qend = nb + nlen;
+            }
+        }
+        // the block ends when no slot is live and no warp can claim more
+        if (!__syncthreads_or(live || !exhausted || qnext < qend)) break;
+        // 2. queue the rays (dense, one shared atomic per warp and queue)
+        {
+            const unsigned m = __ballot_sync(kFull, live);
+            int base = 0;
+            if (lane == 0 && m) base = atomicAdd(&nc, __popc(m));
+            base = __shfl_sync(kFull, base, 0);
+            if (live) {
+                const int e = base + __popc(m & lt);
+                cqO[e] = make_float4(st.ray.ori.x, st.ray.ori.y, st.ray.ori.z, __int_as_float(rid));
+                cqD[e] = make_float4(st.ray.dir.x, st.ray.dir.y, st.ray.dir.z, 0.0f);
+                cOwner[e] = (int16_t)tid;
+            }
+            const bool shadow = live && ps.pending;
+            const unsigned ms = __ballot_sync(kFull, shadow);
+            int sbase = 0;
+            if (lane == 0 && ms) sbase = atomicAdd(&ns, __popc(ms));
+            sbase = __shfl_sync(kFull, sbase, 0);
+            if (shadow) {
+                const int e = sbase + __popc(ms & lt);
+                sqO[e] = make_float4(ps.o.x, ps.o.y, ps.o.z, __int_as_float(rid));
+                sqD[e] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.tmax);
+                sOwner[e] = (int16_t)tid;
+            }
+        }
+        __syncthreads();
+        // 3. trace the queues
+        {
+            const int n1 = nc, n2 = ns;
+            if (tid < n1) {
+                const float4 o = cqO[tid], d = cqD[tid];
+                const DeviceScene& sc = L.req[__float_as_int(o.w)].sc;
+                float dist;
+                const int id = bvhHit(sc, Ray{mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z)}, dist);
+                const int own = cOwner[tid];
+                cId[own] = id;
+                cT[own] = dist;
+            }
+            if (tid < n2) {
+                const float4 o = sqO[tid], d = sqD[tid];
+                const DeviceScene& sc = L.req[__float_as_int(o.w)].sc;
+                sOcc[sOwner[tid]] = bvhTest(sc, Ray{mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z)}, d.w) ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) nc = ns = 0;
+        // 4. take the results
+        if (live) {
+            const BatchRequest& rq = L.req[rid];
+            if (ps.pending) {
+                if (!sOcc[tid]) st.result = st.result + ps.C;
+                ps.pending = false;
+            }
+            if (!path_step_hit<FULL, true>(rq, g, st, cId[tid], cT[tid], &ps)) {
+                float* o = rq.scratch + 3 * ((size_t)(js - L.j0) * rq.npix + (size_t)py * rq.sc.filmW + px);
+                o[0] = st.result.x;
+                o[1] = st.result.y;
+                o[2] = st.result.z;
+                live = false;
+                ps.pending = false;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Adds the chunk's samples [j0, j1) of every request to its frame in sample
 // order, as consecutive path-tracer passes do (main(),
 // path_integ_naive.glsl:166-173): sample 0 starts from zero, a NaN sample
@@ -361,6 +561,16 @@ void launch_batch_t(const BatchLaunch& a, int block, cudaStream_t st) {
             batch_kernel<128, FULL><<<occupancy_grid((const void*)batch_kernel<128, FULL>, 128), 128, 0, st>>>(a);
             break;
     }
+}
+
+cudaError_t launch_batch_queue(const BatchLaunch& a, bool full, cudaStream_t st) {
+    if (full)
+        batch_queue_kernel<true><<<occupancy_grid((const void*)batch_queue_kernel<true>, kQueueBlock), kQueueBlock, 0,
+                                   st>>>(a);
+    else
+        batch_queue_kernel<false><<<occupancy_grid((const void*)batch_queue_kernel<false>, kQueueBlock), kQueueBlock,
+                                    0, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch(const BatchLaunch& a, int block, bool full, cudaStream_t st) {
@@ -423,7 +633,8 @@ void check_config(const zgl_batch_config& c) {
     if (c.queue_capacity < 0 || c.queue_capacity > 4096) fail(ZGL_ERR_INVALID_ARG, "batch: queue_capacity out of range");
     if (c.regen_threshold < 0 || c.regen_threshold > 32) fail(ZGL_ERR_INVALID_ARG, "batch: regen_threshold out of range");
     if (c.scratch_mib < 0) fail(ZGL_ERR_INVALID_ARG, "batch: negative scratch budget");
-    if (c.schedule != ZGL_BATCH_DEFAULT && c.schedule != ZGL_BATCH_FLAT && c.schedule != ZGL_BATCH_PERSISTENT)
+    if (c.schedule != ZGL_BATCH_DEFAULT && c.schedule != ZGL_BATCH_FLAT && c.schedule != ZGL_BATCH_PERSISTENT &&
+        c.schedule != ZGL_BATCH_QUEUE)
         fail(ZGL_ERR_INVALID_ARG, "batch: unknown schedule %d", c.schedule);
 }
 
@@ -476,6 +687,9 @@ void enqueue_render(zgl_batch* b, const zgl_batch_config& c, cudaStream_t st, in
             if (c.schedule == ZGL_BATCH_PERSISTENT) {
                 ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
                 ZGL_CUDA(launch_batch(L, c.block_size, b->fullMaterials, st));
+            } else if (c.schedule == ZGL_BATCH_QUEUE) {
+                ZGL_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(unsigned long long), st));
+                ZGL_CUDA(launch_batch_queue(L, b->fullMaterials, st));
             } else {
                 FlatLaunch F;
                 std::memset(&F, 0, sizeof(F));
@@ -711,6 +925,15 @@ zgl_status zgl_batch_autotune(zgl_batch* b, void* stream, zgl_batch_config* chos
                     c.regen_threshold = th;
                     trial(c);
                 }
+        for (int cap : caps)
+            for (int th : thresholds) {
+                zgl_batch_config c = b->cfg;
+                c.schedule = ZGL_BATCH_QUEUE;
+                c.block_size = kQueueBlock;
+                c.queue_capacity = cap;
+                c.regen_threshold = th;
+                trial(c);
+            }
     } catch (...) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
