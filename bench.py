@@ -45,7 +45,9 @@ UNIT = "Mrays/s"
 KERNELS = {"thread_per_ray": {"closest": "trace_closest_kernel", "any": "trace_any_kernel"},
            "persistent": {"closest": "trace_persistent_kernel<false>", "any": "trace_persistent_kernel<true>"},
            "prefetch": {"closest": "trace_prefetch_kernel<false, false>", "any": "trace_prefetch_kernel<true, false>"},
-           "auto": {"closest": "trace_prefetch_kernel<false, true>", "any": "trace_prefetch_kernel<true, true>"}}
+           "auto": {"closest": "trace_prefetch_kernel<false, true> (trace_closest_kernel where one face's table "
+                               "fits in L2)",
+                    "any": "trace_prefetch_kernel<true, true> (trace_any_kernel where one face's table fits in L2)"}}
 
 
 def resolved_schedule(schedule: str) -> str:
@@ -793,7 +795,7 @@ def run_diff(args, stream, dev):
     ef[2].record(stream)
     stream.synchronize()
     loss_first, loss_last = float(losses[0]), float(losses[-1])
-    # the fused step (zgl_diff_step_l2): forward, loss, adjoint in one kernel
+    # the loss step (zgl_diff_step_l2): forward, L2 loss and adjoint queued in one call
     gimg = torch.empty_like(img)
     gbuf = torch.empty(p.numel(), dtype=torch.float32, device=dev)
     lbuf = torch.empty(1, dtype=torch.float32, device=dev)
@@ -835,8 +837,9 @@ def run_diff(args, stream, dev):
            "samples_per_s_fwd_bwd": round(W * H * spp / (fb_ms * 1e-3), 1),
            "fused_step_ms": round(fused_ms, 2), "fused_iteration_ms": round(fused_it_ms, 2),
            "fused_samples_per_s": round(W * H * spp / (fused_ms * 1e-3), 1),
-           "fused_note": "zgl_diff_step_l2: forward, L2 loss and adjoint in one kernel, ray casts kept between the "
-                         "forward and the replay; iteration = parameter upload + step + Adam",
+           "fused_note": "zgl_diff_step_l2: forward (each path's ray casts kept in HBM), L2 loss and adjoint "
+                         "(replayed from the kept casts) queued in one call; iteration = parameter upload + step + "
+                         "Adam",
            "loss_first": loss_first, "loss_last": loss_last, "iterations": len(losses)}
     res["grad_check"] = diff_grad_check()
     if not args.no_cpu_baseline:

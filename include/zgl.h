@@ -456,25 +456,27 @@ zgl_status zgl_diff_get_params(const zgl_diff* diff, float* out);
  * all work queued on the device first (it may read the scene or produce
  * `params`). */
 zgl_status zgl_diff_set_params(zgl_diff* diff, const float* params);
-/* Renders the image: `image` is a DEVICE buffer of filmW*filmH RGB floats. */
+/* Renders the image: `image` is a DEVICE buffer of filmW*filmH RGB floats.
+ * Besides the per-sample radiance, keeps each path's ray-cast results in
+ * device memory (hit triangle and distance of its first 9 bounces, one
+ * occlusion bit per light sample) when they fit in 4 GiB, so that the next
+ * zgl_diff_backward replays the paths without tracing them again. */
 zgl_status zgl_diff_forward(zgl_diff* diff, float* image, void* stream);
 /* d_image: DEVICE filmW*filmH RGB adjoint of the image; d_params: DEVICE
  * param_count floats, overwritten with the gradient.  Uses the per-sample
- * radiance kept by the last zgl_diff_forward. */
+ * radiance and the ray casts kept by the last zgl_diff_forward (bounces past
+ * the kept ones, or all of them when the casts did not fit or
+ * zgl_diff_set_params ran since, are traced again; the gradient is the same
+ * either way up to float atomic order). */
 zgl_status zgl_diff_backward(zgl_diff* diff, const float* d_image, float* d_params, void* stream);
 
 /* One inverse-rendering step of the image loss
  *   loss = loss_scale * sum over pixels and channels of (image - target)^2
- * in a single kernel (new, no counterpart in the reference): every
- * (pixel, sample) path is traced once, the image (as zgl_diff_forward makes
- * it), the loss and dloss/dimage = 2 loss_scale (image - target) are formed
- * per pixel, and the paths are replayed from their sampler states with the
- * ray-cast results kept from the forward pass in thread-local memory (hit ids,
- * distances and light-sample occlusion of up to 8 bounces; deeper bounces are
- * traced again).  d_params receives the gradient as zgl_diff_backward would
- * for that d_image (up to the order of the float atomics), `loss` one float.
- * target and image are device float[H*W*3]; spp must be at most 128.  Does
- * not touch the per-sample buffer of zgl_diff_forward / zgl_diff_backward. */
+ * (new, no counterpart in the reference): zgl_diff_forward into `image`,
+ * the loss and dloss/dimage = 2 loss_scale (image - target) in one
+ * elementwise kernel, then zgl_diff_backward of that adjoint, all queued on
+ * `stream` with no host synchronisation.  d_params receives the gradient,
+ * `loss` one float.  target and image are device float[H*W*3]. */
 zgl_status zgl_diff_step_l2(zgl_diff* diff, const float* target, float loss_scale, float* image,
                             float* d_params, float* loss, void* stream);
 zgl_status zgl_diff_destroy(zgl_diff* diff);

@@ -194,9 +194,8 @@ def test_fused_l2_step_equals_forward_then_backward(zgl_lib, cuda, spp, depth):
     """zgl_diff_step_l2: the image equals zgl_diff_forward's bit for bit, the
     loss the mean squared error, and the gradient zgl_diff_backward's for
     dL/dimage = 2 (image - target) / numel up to the order of the float
-    atomics (relative 5e-5 of the largest component); one chunk of 32
-    samples, a partial chunk, two chunks, and paths deeper than the
-    recorded ray casts (traced again)."""
+    atomics (relative 5e-5 of the largest component); several sample
+    counts, and paths deeper than the 9 kept ray casts (traced again)."""
     import torch
 
     d = diff_scene(seed=28, width=24, height=20)
@@ -222,6 +221,31 @@ def test_fused_l2_step_equals_forward_then_backward(zgl_lib, cuda, spp, depth):
     o = orc.diff_grad(d, spp, dimg)
     tol = GRAD_ABS * np.abs(o).max() + GRAD_REL * np.abs(o)
     assert np.all(np.abs(g - o) <= tol)
+    dr.close()
+    sc.close()
+
+
+@pytest.mark.parametrize("depth", [6, 11])
+def test_replay_from_kept_casts_equals_traced_replay(zgl_lib, cuda, depth):
+    """zgl_diff_backward replays the paths from the ray casts zgl_diff_forward
+    kept; after zgl_diff_set_params (same values) the casts are dropped and
+    every ray is traced again.  Both gradients agree up to the order of the
+    float atomics (relative 5e-5 of the largest component), with the
+    full-material scene and paths deeper than the 9 kept casts."""
+    import torch
+
+    d = diff_scene(seed=31, width=40, height=24)
+    params = dict(max_depth=depth, russian_roulette=1, rr_start_depth=3) if depth > 8 else dict(max_depth=depth)
+    sc = Scene(d)
+    dr = DiffRenderer(sc, 8, **params)
+    img = dr.forward()
+    rng = np.random.default_rng(32)
+    dimg = torch.from_numpy(rng.uniform(-1e-3, 1e-3, tuple(img.shape)).astype(np.float32)).cuda()
+    g_kept = dr.backward(dimg).cpu().numpy().astype(np.float64)
+    dr.set_params(dr.params())
+    g_traced = dr.backward(dimg).cpu().numpy().astype(np.float64)
+    assert np.abs(g_kept).max() > 0
+    assert np.abs(g_kept - g_traced).max() <= 5e-5 * np.abs(g_traced).max() + 1e-12
     dr.close()
     sc.close()
 

@@ -131,6 +131,13 @@ cudaError_t launch_trace_prefetch(bool adapt, DeviceAccel a, const float* org, c
                                   cudaStream_t s) {
     const unsigned g = grid_for(n, kTraceBlock);
     const int far = tables_beyond_l2(a.M);
+    if (adapt && !far) {  // L2-resident tables: the plain kernels (fewer registers, more warps)
+        if (ANY)
+            trace_any_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
+        else
+            trace_closest_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
+        return cudaGetLastError();
+    }
     if (adapt)
         trace_prefetch_kernel<ANY, true><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, far, hit_id, hit_t, occ);
     else

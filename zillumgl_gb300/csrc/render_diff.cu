@@ -36,6 +36,12 @@ struct zgl_diff {
     int32_t spp = 0;
     int32_t nmat = 0, ninst = 0, nparams = 0;
     float* d_samples = nullptr;   // spp * npix * 3 per-sample radiance
+    // ray casts of the last forward, kept for the replay (null when they
+    // would exceed the budget; the replay then traverses again)
+    int2* d_hits = nullptr;       // kCastDepth * spp * npix (primitive id, distance bits)
+    uint32_t* d_vis = nullptr;    // spp * npix light-sample occlusion bits
+    bool castsValid = false;
+    float* d_dimage = nullptr;    // npix * 3, zgl_diff_step_l2's dloss/dimage
     int32_t* d_lightInst = nullptr;  // per light triangle: instance index
     float* d_values = nullptr;       // current parameter values
     std::vector<uint32_t> lightFirst;
@@ -54,6 +60,62 @@ struct DiffInfo {
     const int32_t* lightInst;
 };
 
+// ----------------------------------------------------------------------------
+// Ray casts kept between the forward pass and the replay.  The forward
+// records, per (sample, pixel) path, the closest hits of its camera ray and
+// first kCastDepth - 1 extension rays (primitive id and distance) and the
+// occlusion answers of its first 32 light samples; the replay takes them in
+// the same order instead of traversing again (casts past the record are
+// traced).  Layout: hits[(k * spp + s) * npix + pix], vis[s * npix + pix], so
+// that a warp's lanes (neighbouring pixels of one sample) store and load
+// consecutive words.  8 bytes per cast: 640 MB for 512^2 pixels x 32 spp.
+// ----------------------------------------------------------------------------
+constexpr int kCastDepth = 9;
+constexpr size_t kCastBudget = (size_t)4 << 30;  // bytes of cast records a renderer may keep
+
+struct CastCursor {
+    int nhit, nvis;
+    uint32_t vis;
+};
+
+struct RecordCast {
+    int2* hits;   // this path's first record; record k at hits[k * stride]
+    size_t stride;
+    CastCursor* cur;
+    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
+        const int id = bvhHit(sc, r, dist);
+        if (cur->nhit < kCastDepth) hits[(size_t)cur->nhit * stride] = make_int2(id, __float_as_int(dist));
+        cur->nhit++;
+        return id;
+    }
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        const bool occ = bvhTest(sc, r, dist);
+        if (cur->nvis < 32 && occ) cur->vis |= 1u << cur->nvis;
+        cur->nvis++;
+        return occ;
+    }
+};
+
+struct ReplayCast {
+    const int2* hits;
+    size_t stride;
+    CastCursor* cur;
+    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
+        const int k = cur->nhit++;
+        if (k < kCastDepth) {
+            const int2 h = __ldg(hits + (size_t)k * stride);
+            dist = __int_as_float(h.y);
+            return h.x;
+        }
+        return bvhHit(sc, r, dist);
+    }
+    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
+        const int k = cur->nvis++;
+        if (k < 32) return (cur->vis >> k) & 1u;
+        return bvhTest(sc, r, dist);
+    }
+};
+
 // forward: one thread per (pixel, sample); blockIdx.y = sample.  Both
 // kernels run at full occupancy (16 blocks of 128 threads per SM, at most 32
 // registers a thread, spills in L1): at 512x512 and 32 spp that measured
@@ -61,7 +123,8 @@ struct DiffInfo {
 // three to four blocks per SM without spills.
 template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY, 16)
-diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, float* __restrict__ samples) {
+diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, int32_t spp, float* __restrict__ samples,
+                    int2* __restrict__ hits, uint32_t* __restrict__ vis) {
     __shared__ uint32_t row[256];
     const int32_t s = blockIdx.y;
     const uint32_t off = sample_offset(s);
@@ -83,7 +146,15 @@ diff_forward_kernel(DeviceScene sc, PathParams pp, int32_t tilesX, float* __rest
     v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
     float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
     Ray ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    v3 r = pathTrace<FULL>(sc, pp, ray, g);
+    v3 r;
+    if (hits) {
+        const size_t npix = (size_t)sc.filmW * sc.filmH, path = (size_t)s * npix + pix;
+        CastCursor cur{0, 0, 0u};
+        r = pathTraceRC<FULL>(sc, pp, ray, g, RecordCast{hits + path, (size_t)spp * npix, &cur});
+        vis[path] = cur.vis;
+    } else {
+        r = pathTrace<FULL>(sc, pp, ray, g);
+    }
     float* o = samples + 3 * ((size_t)s * sc.filmW * sc.filmH + pix);
     o[0] = r.x;
     o[1] = r.y;
@@ -292,12 +363,13 @@ __device__ __forceinline__ void replayPath(const DeviceScene& sc, const PathPara
 }
 
 // Backward: one thread per (pixel, sample), blockIdx.y = sample; the replay
-// traverses the accelerator again.
+// takes the ray casts the forward recorded (`hits` / `vis`), or traverses the
+// accelerator again when there is no record.
 template <bool FULL>
 __global__ void __launch_bounds__(kTileX* kTileY, 16)
 diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t tilesX,
                      int32_t spp, const float* __restrict__ samples, const float* __restrict__ dimage,
-                     float* __restrict__ grad) {
+                     const int2* __restrict__ hits, const uint32_t* __restrict__ vis, float* __restrict__ grad) {
     __shared__ uint32_t row[256];
     __shared__ float sg[kMaxDiffParams];
     for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY) sg[i] = 0.0f;
@@ -336,173 +408,38 @@ diff_backward_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __
         float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
         ray = thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
     }
-    replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, L, delta, DirectCast{});
+    if (hits) {
+        const size_t npix = (size_t)sc.filmW * sc.filmH, path = (size_t)s * npix + pix;
+        CastCursor cur{0, 0, alive ? __ldg(vis + path) : 0u};
+        replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, L, delta,
+                         ReplayCast{hits + path, (size_t)spp * npix, &cur});
+    } else {
+        replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, L, delta, DirectCast{});
+    }
     __syncthreads();
     for (int i = threadIdx.y * kTileX + threadIdx.x; i < di.nparams; i += kTileX * kTileY)
         if (sg[i] != 0.0f) atomicAdd(&grad[i], sg[i]);
 }
 
-// ----------------------------------------------------------------------------
-// Fused forward + adjoint of an image loss L = s * sum over pixels and
-// channels of (image - target)^2.  One warp per pixel, lane l carrying sample
-// 32 c + l of chunk c (up to kFuseChunks chunks of 32 samples).  Each lane
-// traces its sample once and keeps the path's ray-cast results (closest hits
-// and light-sample occlusion, kCastCache records) in thread-local memory; the
-// warp then forms the pixel's image value (samples summed in sample order,
-// NaN samples dropped, as zgl_diff_forward), the loss term and
-// dL/d(image) = 2 s (image - target), and replays every sample from its
-// sampler state with the recorded casts (traversal only past the cache).
-// The Sobol rows of the chunk's 32 sample indices sit in shared memory, one
-// padded row per lane.
-constexpr int kFuseWarps = 16;
-constexpr int kFuseMaxChunks = 4;  // spp <= 128
-constexpr int kCastCache = 9;  // closest hits of the camera ray and 8 bounces
-constexpr int kRowPad = 257;
-
-struct CastRecord {
-    int2 hit[kCastCache];  // primitive id, distance bits
-    uint32_t vis;          // light-sample occlusion, one bit per test in order
-    int32_t nhit, nvis;
-};
-
-// Records the casts of a traced path.
-struct RecordCast {
-    CastRecord* rec;
-    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
-        const int id = bvhHit(sc, r, dist);
-        if (rec->nhit < kCastCache) rec->hit[rec->nhit] = make_int2(id, __float_as_int(dist));
-        rec->nhit++;
-        return id;
+// dloss/dimage = 2 s (image - target) and the loss s * sum (image - target)^2
+// of zgl_diff_step_l2; one atomic per block for the loss.
+__global__ void diff_l2_kernel(const float* __restrict__ image, const float* __restrict__ target, int64_t n,
+                               float scale, float* __restrict__ dimage, float* __restrict__ loss) {
+    __shared__ float part[8];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (i < n) {
+        const float diff = image[i] - target[i];
+        dimage[i] = diff * (2.0f * scale);
+        l = diff * diff * scale;
     }
-    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
-        const bool occ = bvhTest(sc, r, dist);
-        if (rec->nvis < 32 && occ) rec->vis |= 1u << rec->nvis;
-        rec->nvis++;
-        return occ;
-    }
-};
-
-// Plays the recorded casts back in the same order; casts beyond the record
-// are traced again.
-struct ReplayCast {
-    CastRecord* rec;
-    __device__ __forceinline__ int hit(const DeviceScene& sc, const Ray& r, float& dist) const {
-        const int k = rec->nhit++;
-        if (k < kCastCache) {
-            const int2 h = rec->hit[k];
-            dist = __int_as_float(h.y);
-            return h.x;
-        }
-        return bvhHit(sc, r, dist);
-    }
-    __device__ __forceinline__ bool operator()(const DeviceScene& sc, const Ray& r, float dist) const {
-        const int k = rec->nvis++;
-        if (k < 32) return (rec->vis >> k) & 1u;
-        return bvhTest(sc, r, dist);
-    }
-};
-
-template <bool FULL, int CH>
-__global__ void __launch_bounds__(32 * kFuseWarps, 4)
-diff_fused_kernel(DeviceScene sc, PathParams pp, DiffInfo di, const float* __restrict__ params, int32_t spp,
-                  const float* __restrict__ target, float lossScale, float* __restrict__ image,
-                  float* __restrict__ grad, float* __restrict__ loss) {
-    __shared__ uint32_t rows[32 * kRowPad];
-    __shared__ float sg[kMaxDiffParams];
-    __shared__ float sloss[kFuseWarps];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < di.nparams; i += 32 * kFuseWarps) sg[i] = 0.0f;
-    const int64_t npix = (int64_t)sc.filmW * sc.filmH;
-    const int64_t pix = (int64_t)blockIdx.x * kFuseWarps + warp;
-    const bool pixOk = pix < npix;
-    const int px = pixOk ? (int)(pix % sc.filmW) : 0, py = pixOk ? (int)(pix / sc.filmW) : 0;
-    const uint2 seed = pixOk ? __ldg(&sc.pixelSeeds[pix]) : make_uint2(0u, 0u);
-    const v2 scr = mk2((float)px, (float)py) / mk2((float)sc.filmW, (float)sc.filmH);
-    const int nchunks = CH;  // (spp + 31) / 32
-    CastRecord rec[CH];
-    v3 Ls[CH];
-
-    // Sobol rows of samples 32 c .. 32 c + 31, row l at rows[l * kRowPad]
-    auto load_rows = [&](int c) {
-        __syncthreads();
-        if (sc.sampler == 1)
-            for (int i = threadIdx.x; i < 32 * 256; i += 32 * kFuseWarps) {
-                const int l = i >> 8, d = i & 255;
-                rows[l * kRowPad + d] = sobol_value(sc.sobol, sample_offset(32 * c + l) >> 8, (uint32_t)d);
-            }
-        __syncthreads();
-    };
-    auto start = [&](int s, Sampler& g) {
-        g.randSeed = seed.x * (uint32_t)(s + 1) + seed.y;
-        g.sampleSeed = seed.x * seed.y;
-        g.sampleOffset = sample_offset(s);
-        g.dim = 0;
-        g.mode = sc.sampler;
-        g.rowCache = rows + lane * kRowPad;
-        g.mats = sc.sobol;
-        float u0 = sample1D(g), u1 = sample1D(g), u2 = sample1D(g), u3 = sample1D(g);
-        return thinLensCameraSampleRay(sc, scr, u0, u1, u2, u3);
-    };
-
-    // forward: every sample once, recording its casts
-#pragma unroll
-    for (int c = 0; c < nchunks; c++) {
-        load_rows(c);
-        const int s = 32 * c + lane;
-        rec[c].nhit = rec[c].nvis = 0;
-        rec[c].vis = 0u;
-        Ls[c] = mk3(0.0f);
-        if (pixOk && s < spp) {
-            Sampler g;
-            const Ray ray = start(s, g);
-            Ls[c] = pathTraceRC<FULL>(sc, pp, ray, g, RecordCast{&rec[c]});
-        }
-    }
-    // the pixel's image value: samples added in sample order, NaN dropped
-    v3 img = mk3(0.0f);
-#pragma unroll
-    for (int c = 0; c < nchunks; c++)
-        for (int l = 0; l < 32; l++) {
-            const v3 x = mk3(__shfl_sync(kFullMask, Ls[c].x, l), __shfl_sync(kFullMask, Ls[c].y, l),
-                             __shfl_sync(kFullMask, Ls[c].z, l));
-            if (32 * c + l < spp && !hasNan(x)) img = img + x;
-        }
-    img = img / (float)spp;
-    v3 delta = mk3(0.0f);
-    if (pixOk) {
-        const v3 t = mk3(__ldg(&target[3 * pix]), __ldg(&target[3 * pix + 1]), __ldg(&target[3 * pix + 2]));
-        const v3 diff = img - t;
-        const float two = 2.0f * lossScale;
-        delta = (diff * two) * (1.0f / (float)spp);
-        if (lane == 0) {
-            image[3 * pix] = img.x;
-            image[3 * pix + 1] = img.y;
-            image[3 * pix + 2] = img.z;
-            sloss[warp] = (diff.x * diff.x + diff.y * diff.y + diff.z * diff.z) * lossScale;
-        }
-    } else if (lane == 0) {
-        sloss[warp] = 0.0f;
-    }
-    const bool anyDelta = delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f;
-    // adjoint: replay every sample with its recorded casts
-#pragma unroll
-    for (int c = 0; c < nchunks; c++) {
-        if (nchunks > 1) load_rows(c);
-        const int s = 32 * c + lane;
-        const bool alive = pixOk && s < spp && anyDelta && !hasNan(Ls[c]);
-        Sampler g;
-        Ray ray;
-        if (alive) ray = start(s, g);
-        rec[c].nhit = rec[c].nvis = 0;
-        replayPath<FULL>(sc, pp, di, params, sg, alive, g, ray, Ls[c], delta, ReplayCast{&rec[c]});
-    }
+    l = warp_sum(l);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = l;
     __syncthreads();
-    for (int i = threadIdx.x; i < di.nparams; i += 32 * kFuseWarps)
-        if (sg[i] != 0.0f) atomicAdd(&grad[i], sg[i]);
     if (threadIdx.x == 0) {
-        float sl = 0.0f;
-        for (int w = 0; w < kFuseWarps; w++) sl += sloss[w];
-        if (sl != 0.0f) atomicAdd(loss, sl);
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+        if (t != 0.0f) atomicAdd(loss, t);
     }
 }
 
@@ -552,6 +489,11 @@ zgl_status zgl_diff_create(zgl_scene* scene, const zgl_integrator_params* params
         if (d->nparams > kMaxDiffParams) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_create: %d parameters exceed %d", d->nparams, kMaxDiffParams);
         size_t npix = (size_t)scene->filmW * scene->filmH;
         ZGL_CUDA(cudaMalloc(&d->d_samples, sizeof(float) * 3 * npix * (size_t)spp));
+        const size_t paths = npix * (size_t)spp;
+        if ((sizeof(int2) * kCastDepth + sizeof(uint32_t)) * paths <= kCastBudget) {
+            ZGL_CUDA(cudaMalloc(&d->d_hits, sizeof(int2) * kCastDepth * paths));
+            ZGL_CUDA(cudaMalloc(&d->d_vis, sizeof(uint32_t) * paths));
+        }
         std::vector<int32_t> inst((size_t)std::max(scene->nLight, 1), 0);
         for (int k = 0; k < d->ninst; k++)
             for (uint32_t t = d->lightFirst[(size_t)k]; t < d->lightFirst[(size_t)k + 1]; t++) inst[t] = k;
@@ -569,6 +511,8 @@ zgl_status zgl_diff_create(zgl_scene* scene, const zgl_integrator_params* params
         ZGL_CUDA(cudaMemcpy(d->d_values, d->params_host.data(), sizeof(float) * (size_t)d->nparams, cudaMemcpyHostToDevice));
     } catch (...) {
         if (d->d_samples) cudaFree(d->d_samples);
+        if (d->d_hits) cudaFree(d->d_hits);
+        if (d->d_vis) cudaFree(d->d_vis);
         if (d->d_lightInst) cudaFree(d->d_lightInst);
         if (d->d_values) cudaFree(d->d_values);
         delete d;
@@ -603,6 +547,8 @@ zgl_status zgl_diff_set_params(zgl_diff* d, const float* params) {
     for (float v : p)
         if (!std::isfinite(v)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_set_params: non-finite parameter");
     scene_set_diff_params(d->scene, p.data(), d->nmat, d->instPower);
+    // new roughness or metallic values move the sampled directions: the kept casts no longer apply
+    d->castsValid = false;
     d->params_host = p;
     ZGL_CUDA(cudaMemcpy(d->d_values, p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice));
     ZGL_API_END
@@ -618,9 +564,12 @@ zgl_status zgl_diff_forward(zgl_diff* d, float* image, void* stream) {
     int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
     dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
     if (s->fullMaterials)
-        diff_forward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
+        diff_forward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX,
+                                                                         d->spp, d->d_samples, d->d_hits, d->d_vis);
     else
-        diff_forward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX, d->d_samples);
+        diff_forward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), tilesX,
+                                                                          d->spp, d->d_samples, d->d_hits, d->d_vis);
+    d->castsValid = d->d_hits != nullptr;
     ZGL_CUDA(cudaGetLastError());
     int64_t npix = (int64_t)s->filmW * s->filmH;
     diff_reduce_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(d->d_samples, npix, d->spp, image);
@@ -640,12 +589,16 @@ zgl_status zgl_diff_backward(zgl_diff* d, const float* d_image, float* d_params,
     DiffInfo di{d->nmat, d->nparams, d->d_lightInst};
     int tilesX = (s->filmW + kTileX - 1) / kTileX, tilesY = (s->filmH + kTileY - 1) / kTileY;
     dim3 grid((unsigned)(tilesX * tilesY), (unsigned)d->spp);
+    const int2* hits = d->castsValid ? d->d_hits : nullptr;
+    const uint32_t* vis = d->castsValid ? d->d_vis : nullptr;
     if (s->fullMaterials)
-        diff_backward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
-                                                                d->spp, d->d_samples, d_image, d_params);
+        diff_backward_kernel<true><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di,
+                                                                          d->d_values, tilesX, d->spp, d->d_samples,
+                                                                          d_image, hits, vis, d_params);
     else
-        diff_backward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di, d->d_values, tilesX,
-                                                                d->spp, d->d_samples, d_image, d_params);
+        diff_backward_kernel<false><<<grid, dim3(kTileX, kTileY), 0, st>>>(s->view(), path_params(d->params), di,
+                                                                           d->d_values, tilesX, d->spp, d->d_samples,
+                                                                           d_image, hits, vis, d_params);
     ZGL_CUDA(cudaGetLastError());
     ZGL_API_END
 }
@@ -658,31 +611,16 @@ zgl_status zgl_diff_step_l2(zgl_diff* d, const float* target, float loss_scale, 
     if (!device_ptr(target) || !device_ptr(image) || !device_ptr(d_params) || !device_ptr(loss))
         fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: arrays must be device memory");
     if (!std::isfinite(loss_scale)) fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: non-finite loss scale");
-    if (d->spp > 32 * kFuseMaxChunks)
-        fail(ZGL_ERR_INVALID_ARG, "zgl_diff_step_l2: %d samples per pixel exceed %d", d->spp, 32 * kFuseMaxChunks);
     const zgl_scene* s = d->scene;
     cudaStream_t st = (cudaStream_t)stream;
-    ZGL_CUDA(cudaMemsetAsync(d_params, 0, sizeof(float) * (size_t)d->nparams, st));
+    const int64_t n = (int64_t)s->filmW * s->filmH * 3;
+    if (!d->d_dimage) ZGL_CUDA(cudaMalloc(&d->d_dimage, sizeof(float) * (size_t)n));
+    zgl_status r = zgl_diff_forward(d, image, stream);
+    if (r != ZGL_OK) return r;
     ZGL_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), st));
-    DiffInfo di{d->nmat, d->nparams, d->d_lightInst};
-    const int64_t npix = (int64_t)s->filmW * s->filmH;
-    const unsigned grid = (unsigned)((npix + kFuseWarps - 1) / kFuseWarps);
-    const int ch = (d->spp + 31) / 32;
-    const PathParams pp = path_params(d->params);
-#define ZGL_FUSE(F, C)                                                                                         \
-    diff_fused_kernel<F, C><<<grid, 32 * kFuseWarps, 0, st>>>(s->view(), pp, di, d->d_values, d->spp, target, \
-                                                               loss_scale, image, d_params, loss)
-    if (s->fullMaterials) {
-        if (ch == 1) ZGL_FUSE(true, 1);
-        else if (ch == 2) ZGL_FUSE(true, 2);
-        else ZGL_FUSE(true, 4);
-    } else {
-        if (ch == 1) ZGL_FUSE(false, 1);
-        else if (ch == 2) ZGL_FUSE(false, 2);
-        else ZGL_FUSE(false, 4);
-    }
-#undef ZGL_FUSE
+    diff_l2_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(image, target, n, loss_scale, d->d_dimage, loss);
     ZGL_CUDA(cudaGetLastError());
+    return zgl_diff_backward(d, d->d_dimage, d_params, stream);
     ZGL_API_END
 }
 
@@ -690,6 +628,9 @@ zgl_status zgl_diff_destroy(zgl_diff* d) {
     ZGL_API_BEGIN
     if (!d) return ZGL_OK;
     if (d->d_samples) cudaFree(d->d_samples);
+    if (d->d_hits) cudaFree(d->d_hits);
+    if (d->d_vis) cudaFree(d->d_vis);
+    if (d->d_dimage) cudaFree(d->d_dimage);
     if (d->d_lightInst) cudaFree(d->d_lightInst);
     if (d->d_values) cudaFree(d->d_values);
     delete d;
