@@ -42,12 +42,12 @@ UNIT = "Mrays/s"
 
 # kernel of each trace schedule (ZGL_TRACE_* of include/zgl.h); auto resolves
 # as the library does
-KERNELS = {"thread_per_ray": {"closest": "trace_closest_kernel", "any": "trace_any_kernel"},
+KERNELS = {"thread_per_ray": {"closest": "trace_closest_kernel (no lane budget)",
+                              "any": "trace_any_kernel (no lane budget)"},
            "persistent": {"closest": "trace_persistent_kernel<false>", "any": "trace_persistent_kernel<true>"},
-           "prefetch": {"closest": "trace_prefetch_kernel<false, false>", "any": "trace_prefetch_kernel<true, false>"},
-           "auto": {"closest": "trace_prefetch_kernel<false, true> (trace_closest_kernel where one face's table "
-                               "fits in L2)",
-                    "any": "trace_prefetch_kernel<true, true> (trace_any_kernel where one face's table fits in L2)"}}
+           "prefetch": {"closest": "trace_prefetch_kernel<false>", "any": "trace_prefetch_kernel<true>"},
+           "auto": {"closest": "trace_closest_kernel (long rays finished by their warps)",
+                    "any": "trace_any_kernel (long rays finished by their warps)"}}
 
 
 def resolved_schedule(schedule: str) -> str:

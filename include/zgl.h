@@ -105,15 +105,17 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices,
 /* Trace kernel schedule of an accelerator.  All give identical results;
  * only speed differs.  The reference has one fixed schedule (one invocation
  * per pixel or path, src/integrator/NaivePath.cpp:94-100).
- *   ZGL_TRACE_AUTO (0, default): one thread per ray; a warp whose rays share
- *     one origin (camera rays) runs the plain loop, other warps request both
- *     possible successors of a node ahead when a face's node table outgrows
- *     the L2 cache.
- *   ZGL_TRACE_THREAD_PER_RAY (1): one thread per ray, plain loop.
+ *   ZGL_TRACE_AUTO (0, default): one thread per ray; a ray with a
+ *     direction component below 1e-6 in magnitude (boxHit's near-zero
+ *     branch can make it visit tens of thousands of table entries) that has
+ *     not finished after 1024 entries is finished by its whole warp, 32
+ *     consecutive entries at a time.
+ *   ZGL_TRACE_THREAD_PER_RAY (1): one thread per ray, every ray on its own
+ *     lane to the end (the reference's schedule).
  *   ZGL_TRACE_PERSISTENT (2): persistent warps that refill idle lanes by
  *     atomic fetch.
- *   ZGL_TRACE_PREFETCH (3): one thread per ray, every warp requests both
- *     successors ahead. */
+ *   ZGL_TRACE_PREFETCH (3): as ZGL_TRACE_AUTO, with every lane requesting
+ *     both possible successors of a node ahead. */
 enum { ZGL_TRACE_AUTO = 0, ZGL_TRACE_THREAD_PER_RAY = 1, ZGL_TRACE_PERSISTENT = 2, ZGL_TRACE_PREFETCH = 3 };
 zgl_status zgl_accel_set_trace_schedule(zgl_accel* accel, int32_t schedule);
 

@@ -100,6 +100,50 @@ def test_any_hit_bit_exact(soup, cuda, schedule):
     assert np.array_equal(vis.cpu().numpy(), ovis) and np.array_equal(tst.cpu().numpy(), otst)
 
 
+def _long_rays(rng, n):
+    """Rays with one direction component below 1e-6 (boxHit's near-zero
+    branch: every box whose slab holds the origin on that axis is entered),
+    interleaved with ordinary random rays so that warps mix long and short
+    rays."""
+    o = rng.random((n, 3)).astype(np.float32)
+    d = rng.standard_normal((n, 3))
+    axis = rng.integers(0, 3, n)
+    d[np.arange(n), axis] = rng.choice([-1.0, 1.0], n) * rng.uniform(1e-8, 9e-7, n)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    o2, d2 = _rays_mixed(rng, n)
+    oo = np.empty((2 * n, 3), np.float32)
+    dd = np.empty((2 * n, 3), np.float32)
+    oo[0::2], dd[0::2] = o, d
+    oo[1::2], dd[1::2] = o2, d2
+    return oo, dd
+
+
+@pytest.mark.parametrize("schedule", ["auto", "prefetch"])
+@pytest.mark.parametrize("n", [4001, 20000])
+def test_long_rays_finished_by_the_warp_bit_exact(soup, cuda, schedule, n):
+    """Rays that outrun the 1024-entry lane budget are finished by their
+    warps 32 entries at a time: ids, distances and any-hit flags equal the
+    oracle's, with long and short rays in one warp and a partial last warp."""
+    import torch
+
+    acc, packed, v, idx = soup
+    o, d = _long_rays(np.random.default_rng(41), n // 2)
+    o, d = o[:n], d[:n]
+    tmax = shadow_tmax(o.shape[0], 42) * 2.0
+    vis, _ = acc.trace_count(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda))
+    assert int((vis.cpu().numpy() > 1024).sum()) >= 10, "too few rays past the lane budget"
+    acc.set_trace_schedule(schedule)
+    try:
+        _check_closest(acc, packed, v, idx, o, d, cuda)
+        occ = acc.trace_any(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda),
+                            torch.from_numpy(tmax).to(cuda)).cpu().numpy()
+    finally:
+        acc.set_trace_schedule("auto")
+    oocc, _, _, _ = oracle.trace(packed.bounds, packed.hitTable, v, idx, o, d, tmax=tmax, any_hit=True)
+    assert np.array_equal(occ.astype(np.int32), oocc)
+
+
 def test_host_arrays_match_device_arrays(soup, cuda):
     import torch
 

@@ -34,28 +34,50 @@ __device__ __forceinline__ float3 load3(const float* p, int64_t i) {
     return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
 }
 
+// Table entries a ray with a near-zero direction component traverses on its
+// lane before its warp takes it over (finish_long_rays); other rays stay on
+// their lanes (traverse_lane).  The thread-per-ray schedule passes no limit
+// (every ray stays on its lane, the reference's schedule).
+constexpr int kLaneBudget = 1024;
+constexpr int kNoBudget = 0x7fffffff;
+
+__device__ __forceinline__ TraceRay lane_ray(const float* org, const float* dir, int64_t i, bool valid) {
+    return make_trace_ray(valid ? load3(org, i) : make_float3(0.0f, 0.0f, 0.0f),
+                          valid ? load3(dir, i) : make_float3(0.0f, 0.0f, 1.0f));
+}
+
+// One thread per ray; a ray still unfinished after `budget` entries is walked
+// by its warp.  Lanes past n stay until their warp's long rays are done (the
+// warp walks need all 32 lanes); whole warps past n leave at once.
 __global__ void __launch_bounds__(kTraceBlock)
 trace_closest_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
-                     int64_t n, int32_t* __restrict__ hit_id, float* __restrict__ hit_t) {
-    int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
-    if (i >= n) return;
-    TraceRay r = make_trace_ray(load3(org, i), load3(dir, i));
+                     int64_t n, int budget, int32_t* __restrict__ hit_id, float* __restrict__ hit_t) {
+    const int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    const bool valid = i < n;
+    if (__all_sync(0xffffffffu, !valid)) return;
+    const TraceRay r = lane_ray(org, dir, i, valid);
     float dist = 1e8f;
-    int v = 0, t = 0;
-    int id = traverse<false, false>(a, r, dist, v, t);
-    hit_id[i] = id;
-    hit_t[i] = dist;
+    int k = 0, closest = -1;
+    const bool done = !valid || traverse_lane_m<false, false, 0>(a, r, dist, k, closest, budget);
+    finish_long_rays<false>(a, r, dist, k, closest, done);
+    if (valid) {
+        hit_id[i] = closest;
+        hit_t[i] = dist;
+    }
 }
 
 __global__ void __launch_bounds__(kTraceBlock)
 trace_any_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
-                 const float* __restrict__ tmax, int64_t n, uint8_t* __restrict__ occ) {
-    int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
-    if (i >= n) return;
-    TraceRay r = make_trace_ray(load3(org, i), load3(dir, i));
-    float dist = tmax[i];
-    int v = 0, t = 0;
-    occ[i] = (uint8_t)traverse<true, false>(a, r, dist, v, t);
+                 const float* __restrict__ tmax, int64_t n, int budget, uint8_t* __restrict__ occ) {
+    const int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
+    const bool valid = i < n;
+    if (__all_sync(0xffffffffu, !valid)) return;
+    const TraceRay r = lane_ray(org, dir, i, valid);
+    float dist = valid ? tmax[i] : 0.0f;
+    int k = 0, closest = -1;
+    const bool done = !valid || traverse_lane_m<true, false, 0>(a, r, dist, k, closest, budget);
+    finish_long_rays<true>(a, r, dist, k, closest, done);
+    if (valid) occ[i] = (uint8_t)(closest >= 0);
 }
 
 __global__ void __launch_bounds__(kTraceBlock)
@@ -78,72 +100,37 @@ trace_count_kernel(DeviceAccel a, const float* __restrict__ org, const float* __
 }
 
 // Prefetching schedule: one thread per ray with the node loads of
-// traverse_v.  ADAPT (the auto schedule): a warp whose rays share one origin
-// (camera rays: coherent, their nodes come from L1 and L2) runs the plain
-// loop, and so does every warp when one face's table fits in L2; otherwise a
-// warp requests both successors ahead (PF) with a 256-byte L2 prefetch hint,
-// so that DRAM latency overlaps the tests.  Without ADAPT every warp takes
-// the PF loop.  Measured on the GB300 (2^24 rays per launch): the PF loop
-// takes the 16M incoherent launches from 93.7 / 57.8 ms to 79.1 / 48.7 ms
-// (closest / any) and the 4M ones from 29.4 to 27.5 ms, and costs 30-50% on
-// camera rays and on the L2-resident 1M tables.
-template <bool ANY, bool ADAPT>
+// traverse_v: each lane requests both possible successors of an entry ahead
+// (k + 1 and the miss link) with a 256-byte L2 prefetch hint, so that their
+// latency overlaps the tests of the entry; long rays are finished by the
+// warp as in the one-thread-per-ray kernels.  Measured on the GB300 (2^24
+// rays per launch): before long rays went to their warp, this loop took the
+// 16M-triangle incoherent launches from 93.7 / 57.8 ms to 79.1 / 48.7 ms
+// (closest / any), mostly by shortening the few longest rays; with them
+// finished by their warps the plain loop is faster everywhere.
+template <bool ANY>
 __global__ void __launch_bounds__(kTraceBlock)
 trace_prefetch_kernel(DeviceAccel a, const float* __restrict__ org, const float* __restrict__ dir,
-                      const float* __restrict__ tmax, int64_t n, int far, int32_t* __restrict__ hit_id,
+                      const float* __restrict__ tmax, int64_t n, int32_t* __restrict__ hit_id,
                       float* __restrict__ hit_t, uint8_t* __restrict__ occ) {
     const int64_t i = blockIdx.x * (int64_t)kTraceBlock + threadIdx.x;
     const bool valid = i < n;
-    const float3 o = valid ? load3(org, i) : make_float3(0.0f, 0.0f, 0.0f);
-    bool plain = false;
-    if (ADAPT) {
-        const unsigned m = 0xffffffffu;
-        const float ox = __shfl_sync(m, o.x, 0), oy = __shfl_sync(m, o.y, 0), oz = __shfl_sync(m, o.z, 0);
-        plain = !far || __all_sync(m, !valid || (o.x == ox && o.y == oy && o.z == oz));
-    }
+    if (__all_sync(0xffffffffu, !valid)) return;
+    const TraceRay r = lane_ray(org, dir, i, valid);
+    float dist = ANY ? (valid ? tmax[i] : 0.0f) : 1e8f;
+    int k = 0, closest = -1;
+    const bool done = !valid || traverse_lane_m<ANY, true, 256>(a, r, dist, k, closest, kLaneBudget);
+    finish_long_rays<ANY>(a, r, dist, k, closest, done);
     if (!valid) return;
-    const TraceRay r = make_trace_ray(o, load3(dir, i));
-    float dist = ANY ? tmax[i] : 1e8f;
-    int v = 0, t = 0;
-    const int res = plain ? traverse<ANY, false>(a, r, dist, v, t) : traverse_vm<ANY, true, 256>(a, r, dist);
     if (ANY) {
-        occ[i] = (uint8_t)res;
+        occ[i] = (uint8_t)(closest >= 0);
     } else {
-        hit_id[i] = res;
+        hit_id[i] = closest;
         hit_t[i] = dist;
     }
 }
 
-// Whether one face's node table (M records of 32 bytes) outgrows the L2 of
-// the current device.
-int tables_beyond_l2(int64_t M) {
-    int dev = 0, l2 = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
-    return (int64_t)32 * M > (int64_t)l2 ? 1 : 0;
-}
-
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
-
-template <bool ANY>
-cudaError_t launch_trace_prefetch(bool adapt, DeviceAccel a, const float* org, const float* dir,
-                                  const float* tmax, int64_t n, int32_t* hit_id, float* hit_t, uint8_t* occ,
-                                  cudaStream_t s) {
-    const unsigned g = grid_for(n, kTraceBlock);
-    const int far = tables_beyond_l2(a.M);
-    if (adapt && !far) {  // L2-resident tables: the plain kernels (fewer registers, more warps)
-        if (ANY)
-            trace_any_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
-        else
-            trace_closest_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
-        return cudaGetLastError();
-    }
-    if (adapt)
-        trace_prefetch_kernel<ANY, true><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, far, hit_id, hit_t, occ);
-    else
-        trace_prefetch_kernel<ANY, false><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, far, hit_id, hit_t, occ);
-    return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------------------
 // Persistent traversal: each warp keeps its lanes busy by refilling a lane
@@ -275,11 +262,14 @@ cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* d
                                  int32_t* hit_id, float* hit_t, int schedule, unsigned long long* counter,
                                  cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M > 0 && (schedule == ZGL_TRACE_AUTO || schedule == ZGL_TRACE_PREFETCH))
-        return launch_trace_prefetch<false>(schedule == ZGL_TRACE_AUTO, a, org, dir, nullptr, n, hit_id, hit_t,
-                                            nullptr, s);
+    const unsigned g = grid_for(n, kTraceBlock);
+    if (a.M > 0 && schedule == ZGL_TRACE_PREFETCH) {
+        trace_prefetch_kernel<false><<<g, kTraceBlock, 0, s>>>(a, org, dir, nullptr, n, hit_id, hit_t, nullptr);
+        return cudaGetLastError();
+    }
     if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
-        trace_closest_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, n, hit_id, hit_t);
+        const int budget = schedule == ZGL_TRACE_THREAD_PER_RAY ? kNoBudget : kLaneBudget;
+        trace_closest_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, n, budget, hit_id, hit_t);
         return cudaGetLastError();
     }
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
@@ -295,11 +285,14 @@ cudaError_t launch_trace_closest(DeviceAccel a, const float* org, const float* d
 cudaError_t launch_trace_any(DeviceAccel a, const float* org, const float* dir, const float* tmax,
                              int64_t n, uint8_t* occ, int schedule, unsigned long long* counter, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (a.M > 0 && (schedule == ZGL_TRACE_AUTO || schedule == ZGL_TRACE_PREFETCH))
-        return launch_trace_prefetch<true>(schedule == ZGL_TRACE_AUTO, a, org, dir, tmax, n, nullptr, nullptr, occ,
-                                           s);
+    const unsigned g = grid_for(n, kTraceBlock);
+    if (a.M > 0 && schedule == ZGL_TRACE_PREFETCH) {
+        trace_prefetch_kernel<true><<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, nullptr, nullptr, occ);
+        return cudaGetLastError();
+    }
     if (a.M == 0 || schedule != ZGL_TRACE_PERSISTENT || counter == nullptr) {
-        trace_any_kernel<<<grid_for(n, kTraceBlock), kTraceBlock, 0, s>>>(a, org, dir, tmax, n, occ);
+        const int budget = schedule == ZGL_TRACE_THREAD_PER_RAY ? kNoBudget : kLaneBudget;
+        trace_any_kernel<<<g, kTraceBlock, 0, s>>>(a, org, dir, tmax, n, budget, occ);
         return cudaGetLastError();
     }
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
@@ -443,8 +436,8 @@ private:
     int prev_ = 0, dev_ = 0;
 };
 
-// The schedule a trace call runs (ZGL_TRACE_AUTO is the adaptive prefetching
-// kernel).
+// The schedule a trace call runs (ZGL_TRACE_AUTO: one thread per ray, long
+// rays finished by their warps).
 int trace_schedule(const zgl_accel* a) { return a->trace_schedule; }
 
 int host_threads() {

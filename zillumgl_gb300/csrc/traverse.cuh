@@ -255,6 +255,188 @@ __device__ __forceinline__ int traverse_vm(const DeviceAccel& a, const TraceRay&
     }
 }
 
+// ---------------------------------------------------------------------------
+// Long rays.  A few rays visit tens of thousands of table entries: a
+// direction component below 1e-6 takes boxHit's near-zero-component branch,
+// which accepts every box whose slab holds the origin on that axis (on the
+// 4M-triangle soup with 2^24 incoherent rays, 55 such rays visit up to
+// 58,981 entries; the median ray visits 99 and no other ray more than
+// 1,581).  Traversed by one lane, such a ray is a
+// chain of dependent loads that outlasts the rest of its launch.  So a lane
+// traverses alone for a budget of entries (traverse_lane), and a ray still
+// unfinished then is walked by its whole warp (traverse_warp): each lane
+// loads one entry of a window of 32 consecutive entries and evaluates its
+// slab test and, for a leaf, its triangle test, neither of which depends on
+// the running distance; the warp then follows the reference's path through
+// the window in order, applying `!(tmin > dist)` and `t < dist` with the
+// distance as it stands at each step.  Entries visited, tests taken and
+// results are those of traverse_m.
+// ---------------------------------------------------------------------------
+
+// traverse_v from entry k with the running `closest`.  Only rays with a
+// near-zero direction component (MODE 4) get long: on the soups every other
+// ray visits at most about 1,600 entries.  So only their loop counts steps,
+// and stops after `budget` entries; the other modes run to the end without
+// the count.  Returns true when the ray is finished (k >= M, or an any-hit
+// found); otherwise k is the next entry to visit.
+template <bool ANY, int MODE, bool PF, int HINT>
+__device__ __forceinline__ bool traverse_lane(const DeviceAccel& a, const TraceRay& r, float& dist, int& k,
+                                              int& closest, int budget) {
+    const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
+    const int M = a.M;
+    if (MODE != 4) budget = 0x7fffffff;
+    if (!PF) {  // the loop of traverse_m, with a step count in MODE 4
+        for (int step = 0; k < M; step++) {
+            if (MODE == 4 && step == budget) return false;
+            const float4 lo = load_node<HINT>(base + 2 * k);
+            const float4 hi = load_node<HINT>(base + 2 * k + 1);
+            float tmin;
+            const bool h = box_hit_m<MODE>(lo, hi, r, tmin) && !(tmin > dist);
+            const int prim = __float_as_int(lo.w);
+            const int next = h ? k + 1 : max(__float_as_int(hi.w), k + 1);
+            if (h && prim >= 0) {
+                float t;
+                if (tri_hit(a.tris, prim, r, t) && t < dist) {
+                    closest = prim;
+                    if (ANY) return true;
+                    dist = t;
+                }
+            }
+            k = next;
+        }
+        return true;
+    }
+    if (k >= M) return true;
+    float4 lo = load_node<HINT>(base + 2 * k), hi = load_node<HINT>(base + 2 * k + 1);
+    for (int step = 0; MODE != 4 || step < budget; step++) {
+        const int prim = __float_as_int(lo.w);
+        const int skip = max(__float_as_int(hi.w), k + 1);
+        float4 alo, ahi, blo, bhi;
+        if (PF) {
+            const int ka = min(k + 1, M - 1), kb = min(skip, M - 1);
+            alo = load_node<HINT>(base + 2 * ka);
+            ahi = load_node<HINT>(base + 2 * ka + 1);
+            blo = load_node<HINT>(base + 2 * kb);
+            bhi = load_node<HINT>(base + 2 * kb + 1);
+        }
+        float tmin;
+        const bool h = box_hit_m<MODE>(lo, hi, r, tmin) && !(tmin > dist);
+        const int next = h ? k + 1 : skip;
+        if (h && prim >= 0) {
+            float t;
+            if (tri_hit(a.tris, prim, r, t) && t < dist) {
+                closest = prim;
+                if (ANY) return true;
+                dist = t;
+            }
+        }
+        k = next;
+        if (next >= M) return true;
+        if (PF) {
+            lo = h ? alo : blo;
+            hi = h ? ahi : bhi;
+        } else {
+            lo = load_node<HINT>(base + 2 * next);
+            hi = load_node<HINT>(base + 2 * next + 1);
+        }
+    }
+    return false;
+}
+
+template <bool ANY, bool PF, int HINT>
+__device__ __forceinline__ bool traverse_lane_m(const DeviceAccel& a, const TraceRay& r, float& dist, int& k,
+                                                int& closest, int budget) {
+    switch (r.mode) {
+        case 3: return traverse_lane<ANY, 3, PF, HINT>(a, r, dist, k, closest, budget);
+        case 4: return traverse_lane<ANY, 4, PF, HINT>(a, r, dist, k, closest, budget);
+        case 0: return traverse_lane<ANY, 0, PF, HINT>(a, r, dist, k, closest, budget);
+        case 1: return traverse_lane<ANY, 1, PF, HINT>(a, r, dist, k, closest, budget);
+        default: return traverse_lane<ANY, 2, PF, HINT>(a, r, dist, k, closest, budget);
+    }
+}
+
+// The rest of one ray from entry k, walked by all 32 lanes of the warp (ray
+// and state warp-uniform; every lane calls).
+template <bool ANY, int MODE>
+__device__ __forceinline__ void traverse_warp(const DeviceAccel& a, const TraceRay& r, float& dist, int& k,
+                                              int& closest) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
+    const int M = a.M;
+    while (k < M) {
+        const int j = k + lane;
+        float4 lo = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1)), hi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (j < M) {
+            lo = __ldg(base + 2 * (size_t)j);
+            hi = __ldg(base + 2 * (size_t)j + 1);
+        }
+        float tmin = 0.0f, t = 0.0f;
+        const bool geom = j < M && box_hit_m<MODE>(lo, hi, r, tmin);
+        const int prim = __float_as_int(lo.w);
+        const bool tri = geom && prim >= 0 && tri_hit(a.tris, prim, r, t);
+        const int skip = max(__float_as_int(hi.w), j + 1);
+        const unsigned G = __ballot_sync(full, geom), T = __ballot_sync(full, tri);
+        // the path through the window: p only grows, so at most 32 steps
+        int p = 0;
+        for (;;) {
+            const float tm = __shfl_sync(full, tmin, p);
+            const float tt = __shfl_sync(full, t, p);
+            const int pr = __shfl_sync(full, prim, p);
+            const int sk = __shfl_sync(full, skip, p);
+            const bool h = ((G >> p) & 1u) && !(tm > dist);
+            if (h && ((T >> p) & 1u) && tt < dist) {
+                closest = pr;
+                if (ANY) {
+                    k = M;
+                    return;
+                }
+                dist = tt;
+            }
+            const int next = h ? k + p + 1 : sk;
+            if (next >= M || next - k >= 32) {
+                k = next;
+                break;
+            }
+            p = next - k;
+        }
+    }
+}
+
+// Finishes, one at a time with the whole warp, the rays of the warp's lanes
+// that traverse_lane left unfinished (`done` false).  Every lane calls; a
+// lane without a ray passes done = true.
+template <bool ANY>
+__device__ __forceinline__ void finish_long_rays(const DeviceAccel& a, const TraceRay& r, float& dist, int& k,
+                                                 int& closest, bool done) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    unsigned pending = __ballot_sync(full, !done);
+    while (pending) {
+        const int src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const float3 o = make_float3(__shfl_sync(full, r.o.x, src), __shfl_sync(full, r.o.y, src),
+                                     __shfl_sync(full, r.o.z, src));
+        const float3 d = make_float3(__shfl_sync(full, r.d.x, src), __shfl_sync(full, r.d.y, src),
+                                     __shfl_sync(full, r.d.z, src));
+        float wd = __shfl_sync(full, dist, src);
+        int wk = __shfl_sync(full, k, src), wc = __shfl_sync(full, closest, src);
+        const TraceRay w = make_trace_ray(o, d);
+        switch (w.mode) {
+            case 3: traverse_warp<ANY, 3>(a, w, wd, wk, wc); break;
+            case 4: traverse_warp<ANY, 4>(a, w, wd, wk, wc); break;
+            case 0: traverse_warp<ANY, 0>(a, w, wd, wk, wc); break;
+            case 1: traverse_warp<ANY, 1>(a, w, wd, wk, wc); break;
+            default: traverse_warp<ANY, 2>(a, w, wd, wk, wc); break;
+        }
+        if (lane == src) {
+            dist = wd;
+            k = wk;
+            closest = wc;
+        }
+    }
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ int traverse(const DeviceAccel& a, const TraceRay& r, float& dist, int& visits,
                                         int& tests) {
