@@ -38,7 +38,7 @@ __device__ __forceinline__ float3 load3(const float* p, int64_t i) {
 // lane before its warp takes it over (finish_long_rays); other rays stay on
 // their lanes (traverse_lane).  The thread-per-ray schedule passes no limit
 // (every ray stays on its lane, the reference's schedule).
-constexpr int kLaneBudget = 1024;
+constexpr int kLaneBudget = kLongRayBudget;
 constexpr int kNoBudget = 0x7fffffff;
 
 __device__ __forceinline__ TraceRay lane_ray(const float* org, const float* dir, int64_t i, bool valid) {

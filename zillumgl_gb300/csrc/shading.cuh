@@ -704,6 +704,53 @@ struct ClosestHit {
 #else
 #define ZGL_TRACE_CALL __device__ __noinline__
 #endif
+// A ray with a near-zero direction component that outruns kLongRayBudget
+// table entries is finished by the lanes that reach the end of their own
+// traversal together (traverse.cuh: finish_long_rays_group), as the trace
+// kernels do with whole warps.  The walk is a separate out-of-line call,
+// taken only when some lane of the group has such a ray, so that the
+// traversal loop keeps its registers.
+struct LongRayState {
+    float dist;
+    int k, closest;
+};
+template <bool ANY>
+static __device__ __noinline__ LongRayState finishLongRays(unsigned group, DeviceAccel a, float ox, float oy,
+                                                             float oz, float dx, float dy, float dz,
+                                                             LongRayState s, bool done) {
+    const TraceRay tr = make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz));
+    finish_long_rays_group<ANY>(group, a, tr, s.dist, s.k, s.closest, done);
+    return s;
+}
+// Closest-hit / any-hit of one ray.  Rays of modes 0-3 run the plain loops;
+// a MODE 4 ray (near-zero direction component) runs a loop that stops after
+// kLongRayBudget entries, and only that branch keeps what the walk needs, so
+// the common loops carry no extra live values.
+template <bool ANY>
+__device__ __forceinline__ LongRayState traceOne(const DeviceAccel& a, const TraceRay& tr, float dist) {
+    LongRayState s{dist, 0, -1};
+    bool done = true;
+    DeviceAccel wa{nullptr, nullptr, 0};
+    float3 wo = make_float3(0.0f, 0.0f, 0.0f), wd = make_float3(0.0f, 0.0f, 1.0f);
+    if (tr.mode != 4) {
+        int v = 0, t = 0;
+        switch (tr.mode) {
+            case 3: s.closest = traverse_m<ANY, false, 3>(a, tr, s.dist, v, t); break;
+            case 0: s.closest = traverse_m<ANY, false, 0>(a, tr, s.dist, v, t); break;
+            case 1: s.closest = traverse_m<ANY, false, 1>(a, tr, s.dist, v, t); break;
+            default: s.closest = traverse_m<ANY, false, 2>(a, tr, s.dist, v, t); break;
+        }
+        if (ANY) s.closest = s.closest ? 0 : -1;  // traverse_m returns the any-hit flag
+    } else {
+        done = traverse_lane<ANY, 4, false, 0>(a, tr, s.dist, s.k, s.closest, kLongRayBudget);
+        wa = a;
+        wo = tr.o;
+        wd = tr.d;
+    }
+    const unsigned group = __activemask();
+    if (__any_sync(group, !done)) s = finishLongRays<ANY>(group, wa, wo.x, wo.y, wo.z, wd.x, wd.y, wd.z, s, done);
+    return s;
+}
 static ZGL_TRACE_CALL ClosestHit traceClosestCall(DeviceAccel a, float ox, float oy, float oz, float dx, float dy,
                                                     float dz) {
     TraceRay tr = make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz));
@@ -718,6 +765,35 @@ static ZGL_TRACE_CALL bool traceAnyCall(DeviceAccel a, float ox, float oy, float
     int v = 0, t = 0;
     return traverse<true, false>(a, tr, dist, v, t) != 0;
 }
+
+// Long rays cost a tail only in large trees: with fewer entries a face's
+// table stays in L2 and even a ray that visits all of them ends quickly.
+// Translation units that define ZGL_LONG_RAYS (render_long.cu: the
+// integrator kernels for trees of at least kLongRayMinEntries entries) trace
+// through the calls below; every other unit keeps the plain calls above, so
+// the kernels that never meet a long ray keep their register budget and code
+// as they were (sharing one function between both paths made the
+// small-scene, batch and adjoint kernels 2-21% slower).
+constexpr int kLongRayMinEntries = 1 << 21;
+static __device__ __noinline__ ClosestHit traceClosestLong(DeviceAccel a, float ox, float oy, float oz, float dx,
+                                                           float dy, float dz) {
+    const LongRayState s = traceOne<false>(a, make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz)), 1e8f);
+    return ClosestHit{s.closest, s.dist};
+}
+static __device__ __noinline__ bool traceAnyLong(DeviceAccel a, float ox, float oy, float oz, float dx, float dy,
+                                                 float dz, float dist) {
+    return traceOne<true>(a, make_trace_ray(make_float3(ox, oy, oz), make_float3(dx, dy, dz)), dist).closest >= 0;
+}
+#if defined(ZGL_LONG_RAYS) && ZGL_LONG_RAYS
+__device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float& dist) {
+    ClosestHit h = traceClosestLong(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z);
+    dist = h.dist;
+    return h.id;
+}
+__device__ __forceinline__ bool bvhTest(const DeviceScene& sc, const Ray& r, float dist) {
+    return traceAnyLong(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z, dist);
+}
+#else
 __device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float& dist) {
     ClosestHit h = traceClosestCall(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z);
     dist = h.dist;
@@ -726,6 +802,7 @@ __device__ __forceinline__ int bvhHit(const DeviceScene& sc, const Ray& r, float
 __device__ __forceinline__ bool bvhTest(const DeviceScene& sc, const Ray& r, float dist) {
     return traceAnyCall(sc.accel, r.ori.x, r.ori.y, r.ori.z, r.dir.x, r.dir.y, r.dir.z, dist);
 }
+#endif
 __device__ __forceinline__ bool visible(const DeviceScene& sc, v3 x, v3 y) {  // intersection.glsl:429-433
     float dist = distance(x, y) - 2e-5f;
     v3 wi = normalize(y - x);

@@ -393,7 +393,7 @@ __device__ __forceinline__ void traverse_warp(const DeviceAccel& a, const TraceR
                 }
                 dist = tt;
             }
-            const int next = h ? k + p + 1 : sk;
+            const int next = h ? k + p + 1 : max(sk, k + p + 1);  // the max holds by construction
             if (next >= M || next - k >= 32) {
                 k = next;
                 break;
@@ -401,6 +401,19 @@ __device__ __forceinline__ void traverse_warp(const DeviceAccel& a, const TraceR
             p = next - k;
         }
     }
+}
+
+// The accelerator of lane `src` of `group`: lanes of one warp may trace in
+// different scenes (the batched renderer's persistent and queue schedules),
+// and a walk reads the tables of the ray it serves.
+__device__ __forceinline__ DeviceAccel group_accel(unsigned group, const DeviceAccel& a, int src) {
+    DeviceAccel w;
+    w.nodes = reinterpret_cast<const float4*>(
+        __shfl_sync(group, reinterpret_cast<unsigned long long>(a.nodes), src));
+    w.tris = reinterpret_cast<const float4*>(
+        __shfl_sync(group, reinterpret_cast<unsigned long long>(a.tris), src));
+    w.M = __shfl_sync(group, a.M, src);
+    return w;
 }
 
 // Finishes, one at a time with the whole warp, the rays of the warp's lanes
@@ -422,13 +435,94 @@ __device__ __forceinline__ void finish_long_rays(const DeviceAccel& a, const Tra
         float wd = __shfl_sync(full, dist, src);
         int wk = __shfl_sync(full, k, src), wc = __shfl_sync(full, closest, src);
         const TraceRay w = make_trace_ray(o, d);
+        const DeviceAccel wa = group_accel(full, a, src);
         switch (w.mode) {
-            case 3: traverse_warp<ANY, 3>(a, w, wd, wk, wc); break;
-            case 4: traverse_warp<ANY, 4>(a, w, wd, wk, wc); break;
-            case 0: traverse_warp<ANY, 0>(a, w, wd, wk, wc); break;
-            case 1: traverse_warp<ANY, 1>(a, w, wd, wk, wc); break;
-            default: traverse_warp<ANY, 2>(a, w, wd, wk, wc); break;
+            case 3: traverse_warp<ANY, 3>(wa, w, wd, wk, wc); break;
+            case 4: traverse_warp<ANY, 4>(wa, w, wd, wk, wc); break;
+            case 0: traverse_warp<ANY, 0>(wa, w, wd, wk, wc); break;
+            case 1: traverse_warp<ANY, 1>(wa, w, wd, wk, wc); break;
+            default: traverse_warp<ANY, 2>(wa, w, wd, wk, wc); break;
         }
+        if (lane == src) {
+            dist = wd;
+            k = wk;
+            closest = wc;
+        }
+    }
+}
+
+// Entries a ray with a near-zero direction component traverses on its lane
+// before its warp (or the group of lanes that called together) takes it
+// over.
+constexpr int kLongRayBudget = 1024;
+
+// traverse_warp for a group of lanes `group` (the lanes of the warp that
+// called together; a window is as wide as the group, entry k + rank on the
+// lane of that rank).  Only MODE 4 rays are handed over, so only that mode
+// is instantiated.
+template <bool ANY>
+__device__ __forceinline__ void traverse_group(unsigned group, const DeviceAccel& a, const TraceRay& r,
+                                               float& dist, int& k, int& closest) {
+    const int lane = threadIdx.x & 31;
+    const int width = __popc(group);
+    const int rank = __popc(group & ((1u << lane) - 1u));
+    const float4* __restrict__ base = a.nodes + (size_t)r.face * (size_t)a.M * 2;
+    const int M = a.M;
+    while (k < M) {
+        const int j = k + rank;
+        float4 lo = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1)), hi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (j < M) {
+            lo = __ldg(base + 2 * (size_t)j);
+            hi = __ldg(base + 2 * (size_t)j + 1);
+        }
+        float tmin = 0.0f, t = 0.0f;
+        const bool geom = j < M && box_hit_m<4>(lo, hi, r, tmin);
+        const int prim = __float_as_int(lo.w);
+        const bool tri = geom && prim >= 0 && tri_hit(a.tris, prim, r, t);
+        const int skip = max(__float_as_int(hi.w), j + 1);
+        const unsigned G = __ballot_sync(group, geom), T = __ballot_sync(group, tri);  // lane bits
+        int p = 0;
+        for (;;) {
+            const int src = __ffs(__ballot_sync(group, rank == p)) - 1;  // lane holding window position p
+            const float tm = __shfl_sync(group, tmin, src);
+            const float tt = __shfl_sync(group, t, src);
+            const int pr = __shfl_sync(group, prim, src);
+            const int sk = __shfl_sync(group, skip, src);
+            const bool h = ((G >> src) & 1u) && !(tm > dist);
+            if (h && ((T >> src) & 1u) && tt < dist) {
+                closest = pr;
+                if (ANY) {
+                    k = M;
+                    return;
+                }
+                dist = tt;
+            }
+            const int next = h ? k + p + 1 : max(sk, k + p + 1);  // the max holds by construction
+            if (next >= M || next - k >= width) {
+                k = next;
+                break;
+            }
+            p = next - k;
+        }
+    }
+}
+
+// finish_long_rays for the lanes in `group`, which all call it.
+template <bool ANY>
+__device__ __forceinline__ void finish_long_rays_group(unsigned group, const DeviceAccel& a, const TraceRay& r,
+                                                       float& dist, int& k, int& closest, bool done) {
+    const int lane = threadIdx.x & 31;
+    unsigned pending = __ballot_sync(group, !done);
+    while (pending) {
+        const int src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const float3 o = make_float3(__shfl_sync(group, r.o.x, src), __shfl_sync(group, r.o.y, src),
+                                     __shfl_sync(group, r.o.z, src));
+        const float3 d = make_float3(__shfl_sync(group, r.d.x, src), __shfl_sync(group, r.d.y, src),
+                                     __shfl_sync(group, r.d.z, src));
+        float wd = __shfl_sync(group, dist, src);
+        int wk = __shfl_sync(group, k, src), wc = __shfl_sync(group, closest, src);
+        traverse_group<ANY>(group, group_accel(group, a, src), make_trace_ray(o, d), wd, wk, wc);
         if (lane == src) {
             dist = wd;
             k = wk;
