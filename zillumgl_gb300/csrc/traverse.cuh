@@ -261,8 +261,8 @@ __device__ __forceinline__ int traverse_vm(const DeviceAccel& a, const TraceRay&
 // which accepts every box whose slab holds the origin on that axis (on the
 // 4M-triangle soup with 2^24 incoherent rays, 55 such rays visit up to
 // 58,981 entries; the median ray visits 99 and no other ray more than
-// 1,581).  Traversed by one lane, such a ray is a
-// chain of dependent loads that outlasts the rest of its launch.  So a lane
+// 1,581).  Traversed by one lane, such a ray is a chain of dependent loads
+// that outlasts the rest of its launch.  So a lane
 // traverses alone for a budget of entries (traverse_lane), and a ray still
 // unfinished then is walked by its whole warp (traverse_warp): each lane
 // loads one entry of a window of 32 consecutive entries and evaluates its
