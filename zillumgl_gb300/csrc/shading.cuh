@@ -773,7 +773,7 @@ static ZGL_TRACE_CALL bool traceAnyCall(DeviceAccel a, float ox, float oy, float
 // through the calls below; every other unit keeps the plain calls above, so
 // the kernels that never meet a long ray keep their register budget and code
 // as they were (sharing one function between both paths made the
-// small-scene, batch and adjoint kernels 2-21% slower).
+// small-scene, batch and adjoint kernels 2-25% slower).
 constexpr int kLongRayMinEntries = 1 << 21;
 static __device__ __noinline__ ClosestHit traceClosestLong(DeviceAccel a, float ox, float oy, float oz, float dx,
                                                            float dy, float dz) {
