@@ -108,7 +108,7 @@ zgl_status zgl_bvh_build_host(const float* vertices, size_t n_vertices,
  *   ZGL_TRACE_AUTO (0, default): one thread per ray; a ray with a
  *     direction component below 1e-6 in magnitude (boxHit's near-zero
  *     branch can make it visit tens of thousands of table entries) that has
- *     not finished after 1024 entries is finished by its whole warp, 32
+ *     not finished after 256 entries is finished by its whole warp, 32
  *     consecutive entries at a time.
  *   ZGL_TRACE_THREAD_PER_RAY (1): one thread per ray, every ray on its own
  *     lane to the end (the reference's schedule).

@@ -100,7 +100,7 @@ def test_group_walks_with_divergent_groups_and_mixed_accelerators(zgl_lib, cuda,
                       any_hit=any_hit)
     rb = oracle.trace(pb.bounds, pb.hitTable, vb, ib, o[odd], d[odd], tmax=tmax[odd] if any_hit else None,
                       any_hit=any_hit)
-    assert int((ra[2] > 1024).sum()) >= 50 and int((rb[2] > 1024).sum()) >= 20, "too few rays past the budget"
+    assert int((ra[2] > 256).sum()) >= 50 and int((rb[2] > 256).sum()) >= 20, "too few rays past the budget"
     to, td, tm = (torch.from_numpy(x).to(cuda) for x in (o, d, tmax))
     out_id = torch.full((n,), -7, dtype=torch.int32, device=cuda)
     out_t = torch.zeros(n, dtype=torch.float32, device=cuda)

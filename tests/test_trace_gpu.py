@@ -122,7 +122,7 @@ def _long_rays(rng, n):
 @pytest.mark.parametrize("schedule", ["auto", "prefetch"])
 @pytest.mark.parametrize("n", [4001, 20000])
 def test_long_rays_finished_by_the_warp_bit_exact(soup, cuda, schedule, n):
-    """Rays that outrun the 1024-entry lane budget are finished by their
+    """Rays that outrun the 256-entry lane budget are finished by their
     warps 32 entries at a time: ids, distances and any-hit flags equal the
     oracle's, with long and short rays in one warp and a partial last warp."""
     import torch
@@ -132,7 +132,7 @@ def test_long_rays_finished_by_the_warp_bit_exact(soup, cuda, schedule, n):
     o, d = o[:n], d[:n]
     tmax = shadow_tmax(o.shape[0], 42) * 2.0
     vis, _ = acc.trace_count(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda))
-    assert int((vis.cpu().numpy() > 1024).sum()) >= 10, "too few rays past the lane budget"
+    assert int((vis.cpu().numpy() > 256).sum()) >= 10, "too few rays past the lane budget"
     acc.set_trace_schedule(schedule)
     try:
         _check_closest(acc, packed, v, idx, o, d, cuda)

@@ -454,7 +454,7 @@ __device__ __forceinline__ void finish_long_rays(const DeviceAccel& a, const Tra
 // Entries a ray with a near-zero direction component traverses on its lane
 // before its warp (or the group of lanes that called together) takes it
 // over.
-constexpr int kLongRayBudget = 1024;
+constexpr int kLongRayBudget = 256;
 
 // traverse_warp for a group of lanes `group` (the lanes of the warp that
 // called together; a window is as wide as the group, entry k + rank on the
